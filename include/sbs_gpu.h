@@ -1,0 +1,220 @@
+/* sbs_gpu.h - C ABI of the GB300 XPBD solver (libsbs_gpu.so).
+ *
+ * The library replaces the per-frame hot path of Q-Minh/soft-body-simulator:
+ * timestep_t::step (src/physics/timestep.cpp:20-70) together with the
+ * gauss_seidel_solver_t it calls (src/physics/gauss_seidel_solver.cpp:8-37),
+ * the constraint projections (src/physics/xpbd/green_constraint.cpp:49-158,
+ * collision_constraint.cpp:21-48) and the contact generation of the
+ * brute-force CD system (src/physics/collision/brute_force_cd_system.cpp:14-26,
+ * bvh_model.cpp:30-100, xpbd/contact_handler.cpp:14-54).  Scene set-up, IO,
+ * geometry and rendering stay on the host, unchanged.
+ *
+ * Conventions: plain C types only; every call returns an sbs_status;
+ * positions are float (the reference's geometry_t stores float positions,
+ * include/sbs/common/geometry.h) or double where the reference keeps double
+ * state; arrays are tightly packed xyz triples.  One handle owns one CUDA
+ * stream and all device memory of its scene; a handle must be used from one
+ * host thread at a time.  sbs_gpu_step is asynchronous; every sbs_gpu_get_*
+ * call synchronises the handle's stream.
+ */
+#ifndef SBS_GPU_H
+#define SBS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sbs_status {
+    SBS_OK = 0,
+    SBS_EINVAL = 1,    /* bad argument (null pointer, index out of range, bad size) */
+    SBS_ECUDA = 2,     /* a CUDA runtime call failed */
+    SBS_ETIMEOUT = 3,  /* a bounded device-side wait gave up (grid barrier) */
+    SBS_ENAN = 4,      /* non-finite position detected */
+    SBS_ESTATE = 5,    /* call not valid in the handle's current state */
+    SBS_ENOMEM = 6,    /* device allocation failed */
+    SBS_ECOLOUR = 7    /* constraint graph needs more colours than supported */
+} sbs_status;
+
+typedef enum sbs_model {
+    SBS_MODEL_STVK = 0, /* Green-strain StVK energy constraint (green_constraint.cpp) */
+    SBS_MODEL_SNH = 1   /* stable Neo-Hookean, two multipliers (Macklin & Mueller 2021) */
+} sbs_model;
+
+typedef enum sbs_gravity_mode {
+    SBS_GRAVITY_ACCELERATION = 0, /* a = g on every free vertex */
+    SBS_GRAVITY_FORCE = 1         /* f += g then a = f w, as timestep.cpp:39-40 */
+} sbs_gravity_mode;
+
+typedef enum sbs_exec_mode {
+    SBS_EXEC_AUTO = 0,       /* pick with the built-in autotuner at finalize */
+    SBS_EXEC_GRAPH = 1,      /* one kernel per phase, replayed as a CUDA graph */
+    SBS_EXEC_PERSISTENT = 2  /* one cooperative kernel per frame, grid barriers */
+} sbs_exec_mode;
+
+/* Solver parameters.  Defaults (sbs_gpu_params_default) follow
+ * simulation_parameters_t (include/sbs/physics/xpbd/simulation_parameters.h:12-27). */
+typedef struct sbs_gpu_params {
+    double compliance;            /* alpha of the StVK energy constraint (1e-4) */
+    double damping;               /* beta of the StVK energy constraint (0) */
+    double collision_compliance;  /* alpha of contact constraints (1e-8) */
+    double gravity[3];            /* (0, -9.81, 0) */
+    int32_t gravity_mode;         /* sbs_gravity_mode */
+    int32_t device;               /* CUDA device ordinal */
+    int32_t exec_mode;            /* sbs_exec_mode */
+    int32_t block_size;           /* threads per CTA of the projection kernels (0: auto) */
+    int32_t ctas_per_sm;          /* persistent mode CTAs per SM (0: auto) */
+    int32_t tail_threshold;       /* colours with <= this many tets run in one CTA (-1: auto) */
+    int32_t body_contacts;        /* 1: body-body vertex-in-tet contacts (spatial hash) */
+    float hash_cell;              /* spatial hash cell size (0: 2 x mean edge length) */
+    uint32_t max_body_contacts;   /* capacity of the body-contact list (0: auto) */
+    int32_t check_finite;         /* 1: sbs_gpu_get_* report SBS_ENAN on non-finite x */
+} sbs_gpu_params;
+
+typedef struct sbs_gpu_material {
+    int32_t model;     /* sbs_model */
+    double young;      /* Young's modulus E (Pa) */
+    double poisson;    /* Poisson ratio nu */
+    double density;    /* kg/m^3, for lumped masses */
+} sbs_gpu_material;
+
+typedef struct sbs_gpu_stats {
+    uint64_t frames;          /* frames stepped since finalize */
+    uint64_t projections;     /* tet projections executed since finalize */
+    uint32_t n_vertices, n_tets, n_colours, n_tail_colours;
+    uint32_t n_contacts;      /* ground contacts of the last frame */
+    uint32_t n_body_contacts; /* body-body contacts of the last frame */
+    uint32_t body_contact_overflow; /* candidates dropped for lack of capacity */
+    int32_t exec_mode;        /* mode in use after finalize */
+    int32_t grid_ctas, block_size;
+    double residual;          /* XPBD residual after the last substep (if evaluated) */
+    double energy;            /* elastic energy after the last substep (if evaluated) */
+    double last_frame_ms;     /* device time of the last timed frame (sbs_gpu_step_timed) */
+} sbs_gpu_stats;
+
+typedef struct sbs_gpu sbs_gpu;
+
+/* Fills *p with the defaults.  No reference counterpart (compile-time struct
+ * simulation_parameters_t, simulation_parameters.h:10-28). */
+sbs_status sbs_gpu_params_default(sbs_gpu_params* p);
+
+/* Creates a handle (no scene yet).  Replaces constructing simulation_t and
+ * timestep_t (include/sbs/physics/simulation.h:20-48, timestep.h:14-33). */
+sbs_status sbs_gpu_create(const sbs_gpu_params* p, sbs_gpu** out);
+
+/* Adds one tetrahedral body.  x0: rest positions [3*n_verts] (Dm, V0 and
+ * lumped masses come from them); x_init: initial positions [3*n_verts] or
+ * NULL for x0; tets: [4*n_tets] body-local vertex ids; mass: per-vertex mass
+ * [n_verts] or NULL for lumped masses (density * |V0| / 4 per incident tet),
+ * mass 0 pins a vertex.  Replaces tetrahedral_body_t's constructor
+ * (src/physics/tetrahedral_body.cpp:30-83) plus the per-tet
+ * green_constraint_t constructors in main.cpp:37-54 (green_constraint.cpp:11-47). */
+sbs_status sbs_gpu_add_body(sbs_gpu* h, const double* x0, const double* x_init, uint32_t n_verts,
+                            const uint32_t* tets, uint32_t n_tets, const sbs_gpu_material* mat,
+                            const double* mass, int32_t* body_id);
+
+/* Pins vertices (w = 0), as setting particle_t::mass() = 0 does (main.cpp:158-165,
+ * particle.cpp:39-49). */
+sbs_status sbs_gpu_pin_vertices(sbs_gpu* h, int32_t body, const uint32_t* verts, uint32_t n);
+
+/* Prescribed motion: verts follow x(t) = c + R(axis, omega t)(x0 - c) and have
+ * w = 0.  No reference counterpart (the reference only pins). */
+sbs_status sbs_gpu_add_kinematic_rotation(sbs_gpu* h, int32_t body, const uint32_t* verts,
+                                          uint32_t n, const double center[3],
+                                          const double axis[3], double omega);
+
+/* Per-vertex external acceleration field [3*n_verts] (m/s^2), added in the
+ * prediction.  No reference counterpart (particle_t::f is zeroed every substep,
+ * timestep.cpp:55). */
+sbs_status sbs_gpu_set_external_acceleration(sbs_gpu* h, int32_t body, const float* acc);
+
+/* Adds the analytic plane SDF n.x + d = 0 (normal is normalised).  Replaces
+ * sdf_model_t::from_plane (src/physics/collision/sdf_model.cpp:52-64) used with
+ * environment_body_t in main.cpp:60-72. */
+sbs_status sbs_gpu_add_ground_plane(sbs_gpu* h, const double n[3], double d);
+
+/* Colours the constraint graph, orders tets by (colour, Morton code), uploads
+ * the scene and selects the execution mode.  After this the scene is fixed.
+ * No single reference counterpart: it replaces building the constraint list
+ * and the brute-force CD system (main.cpp:37-54, :74-88). */
+sbs_status sbs_gpu_finalize(sbs_gpu* h);
+
+/* One frame: contacts from the frame-start positions, then `substeps` times
+ * predict -> `iterations` Gauss-Seidel sweeps -> velocity update.  Replaces
+ * timestep_t::step (timestep.cpp:20-70) with gauss_seidel_solver_t::solve
+ * (gauss_seidel_solver.cpp:8-37) installed as the solver.  Asynchronous. */
+sbs_status sbs_gpu_step(sbs_gpu* h, double frame_dt, uint32_t substeps, uint32_t iterations);
+
+/* As sbs_gpu_step, bracketed by CUDA events; waits and stores the frame's
+ * device time in stats.last_frame_ms. */
+sbs_status sbs_gpu_step_timed(sbs_gpu* h, double frame_dt, uint32_t substeps, uint32_t iterations);
+
+/* The solver seam alone: resets every multiplier and runs `iterations`
+ * sweeps (contacts first, then the elastic colours) on the current predicted
+ * positions.  Replaces solver_t::solve (include/sbs/physics/solver.h:16). */
+sbs_status sbs_gpu_solve(sbs_gpu* h, double dt, uint32_t iterations);
+
+/* The prediction and velocity-update halves of a substep (timestep.cpp:35-43,
+ * :48-57), and contact detection alone (cd_system_t::execute, cd_system.h:32). */
+sbs_status sbs_gpu_predict(sbs_gpu* h, double dt);
+sbs_status sbs_gpu_update_velocities(sbs_gpu* h, double dt);
+sbs_status sbs_gpu_detect_contacts(sbs_gpu* h);
+
+/* Evaluates the XPBD residual sqrt(sum (C + alpha~ lambda)^2) over elastic
+ * and active contact constraints, and the elastic energy, at the current
+ * predicted positions with compensated (Kahan) FP32 sums.  Writes both. */
+sbs_status sbs_gpu_residual(sbs_gpu* h, double dt, double* residual, double* energy);
+
+/* State transfer for one body (host buffers; pinned memory is fastest).
+ * x: positions [3*n_verts], v: velocities [3*n_verts]; either may be NULL.
+ * set_state writes x into x, xn and xi, as a particle_t's state after a frame.
+ * The gpu_timestep_t adapter calls these around sbs_gpu_step. */
+sbs_status sbs_gpu_set_state(sbs_gpu* h, int32_t body, const float* x, const float* v);
+sbs_status sbs_gpu_get_state(sbs_gpu* h, int32_t body, float* x, float* v);
+/* Predicted/iterate positions xi of one body [3*n_verts]. */
+sbs_status sbs_gpu_get_predicted(sbs_gpu* h, int32_t body, float* xi);
+sbs_status sbs_gpu_set_predicted(sbs_gpu* h, int32_t body, const float* xi);
+
+/* Introspection for parity checks.
+ * get_tet_order: order[k] = global tet id (bodies concatenated in add order)
+ *   projected k-th in a sweep; offsets: n_colours + 1 entries.
+ * get_lambdas: [2*n_tets] in global tet order (StVK/deviatoric, hydrostatic).
+ * get_contacts: vertex ids [cap] and (q, n) [6*cap] of the current frame's
+ *   ground contacts, sorted by (plane, vertex); returns the count in *n. */
+sbs_status sbs_gpu_get_tet_order(sbs_gpu* h, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
+                                 uint32_t* n_colours);
+sbs_status sbs_gpu_get_lambdas(sbs_gpu* h, float* lambdas);
+sbs_status sbs_gpu_get_contacts(sbs_gpu* h, uint32_t* verts, float* qn, uint32_t cap, uint32_t* n);
+sbs_status sbs_gpu_get_masses(sbs_gpu* h, float* inv_mass);
+sbs_status sbs_gpu_get_surface(sbs_gpu* h, uint32_t* verts, uint32_t cap, uint32_t* n);
+sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st);
+
+/* Host-only (no GPU needed): the Gauss-Seidel sweep order the solver uses
+ * for this tet list - tets coloured so that no two tets of a colour share a
+ * vertex, colours by decreasing size, tets of a colour by model then by the
+ * Morton code of the rest centroid.  x0 [3*n_verts], tets [4*n_tets],
+ * models [n_tets] or NULL (all StVK); order [n_tets]; offsets [n_colours+1]
+ * (cap_offsets entries available).  For several bodies pass them
+ * concatenated in add order.  The reference has no counterpart: it projects
+ * constraints in list order (gauss_seidel_solver.cpp:32-35); permuting its
+ * list to this order gives the same sweep as the GPU. */
+sbs_status sbs_gpu_plan_sweep(const double* x0, uint32_t n_verts, const uint32_t* tets, uint32_t n_tets,
+                              const int32_t* models, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
+                              uint32_t* n_colours);
+
+/* Frees every device resource of the handle. */
+sbs_status sbs_gpu_destroy(sbs_gpu* h);
+
+/* Human-readable text of a status code (static storage). */
+const char* sbs_gpu_status_string(sbs_status s);
+
+/* Text of the last error recorded on the handle (static per handle). */
+const char* sbs_gpu_last_error(const sbs_gpu* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SBS_GPU_H */

@@ -1,0 +1,208 @@
+"""ctypes front end of the FP64 CPU oracle (oracle/xpbd_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
+baseline legs of bench.py as the checker.  The CUDA library never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "xpbd_oracle.cpp"
+LIB = HERE / "liboracle_xpbd.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with g++ (OpenMP for the colour-parallel baseline)."""
+    if LIB.exists() and not force and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
+           "-o", str(tmp), str(SRC)]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        P, D, U32, I = C.c_void_p, C.c_double, C.c_uint32, C.c_int
+        dp = np.ctypeslib.ndpointer(np.float64, flags="C")
+        up = np.ctypeslib.ndpointer(np.uint32, flags="C")
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [D, D, D, dp, I]
+        L.orc_destroy.argtypes = [P]
+        L.orc_set_threads.argtypes = [P, I]
+        L.orc_add_body.restype = I
+        L.orc_add_body.argtypes = [P, dp, C.c_void_p, U32, up, U32, I, D, D, D, C.c_void_p]
+        L.orc_pin.argtypes = [P, I, up, U32]
+        L.orc_add_kinematic_rotation.argtypes = [P, I, up, U32, dp, dp, D]
+        L.orc_set_external_acceleration.argtypes = [P, I, dp]
+        L.orc_add_ground_plane.argtypes = [P, dp, D]
+        L.orc_set_tet_order.restype = I
+        L.orc_set_tet_order.argtypes = [P, up, U32, C.c_void_p, U32]
+        L.orc_step.argtypes = [P, D, U32, U32]
+        L.orc_step_fast.argtypes = [P, D, U32, U32]
+        L.orc_solve.argtypes = [P, D, U32]
+        L.orc_predict.argtypes = [P, D]
+        L.orc_finalize.argtypes = [P, D]
+        L.orc_detect_contacts.argtypes = [P]
+        L.orc_residual.argtypes = [P, D, dp]
+        L.orc_set_record_history.argtypes = [P, I]
+        L.orc_get_history.restype = U32
+        L.orc_get_history.argtypes = [P, dp, U32]
+        L.orc_get.argtypes = [P, I, dp]
+        L.orc_set.argtypes = [P, I, dp]
+        L.orc_get_masses.argtypes = [P, dp]
+        L.orc_get_surface.restype = U32
+        L.orc_get_surface.argtypes = [P, I, up, U32]
+        L.orc_get_lambdas.argtypes = [P, dp]
+        L.orc_get_contacts.restype = U32
+        L.orc_get_contacts.argtypes = [P, up, dp, U32]
+        L.orc_tet_eval.argtypes = [P, U32, C.POINTER(D), dp]
+        L.orc_svd3.argtypes = [dp, dp, dp, dp]
+        L.orc_time.restype = D
+        L.orc_time.argtypes = [P]
+        L.orc_projections.restype = C.c_uint64
+        L.orc_projections.argtypes = [P]
+        L.orc_n_contacts.restype = U32
+        L.orc_n_contacts.argtypes = [P]
+        L.orc_stats.argtypes = [P, dp]
+        L.orc_time_frames.restype = D
+        L.orc_time_frames.argtypes = [P, D, U32, U32, U32]
+        _lib = L
+    return _lib
+
+
+FIELD_X, FIELD_XI, FIELD_V, FIELD_X0 = 0, 1, 2, 3
+
+
+class Oracle:
+    """One oracle simulation built from a ``sbs_gb300.scenes.Scene``."""
+
+    def __init__(self, scene, threads: int = 1):
+        L = lib()
+        self.L = L
+        self.scene = scene
+        g = np.asarray(scene.gravity, np.float64)
+        self.h = L.orc_create(scene.compliance, scene.damping,
+                              scene.collision_compliance, g, scene.gravity_mode)
+        L.orc_set_threads(self.h, threads)
+        self.n_verts = 0
+        self.n_tets = 0
+        self.body_ranges = []
+        for b in scene.bodies:
+            x0 = np.ascontiguousarray(b.x0, np.float64).ravel()
+            xi = None if b.x_init is None else \
+                np.ascontiguousarray(b.x_init, np.float64).ravel()
+            tets = np.ascontiguousarray(b.tets, np.uint32).ravel()
+            bid = L.orc_add_body(self.h, x0,
+                                 None if xi is None else xi.ctypes.data,
+                                 len(b.x0), tets, len(b.tets), b.model,
+                                 b.young, b.poisson, b.density, None)
+            if len(b.pinned):
+                L.orc_pin(self.h, bid, np.ascontiguousarray(b.pinned, np.uint32),
+                          len(b.pinned))
+            if len(b.kin_verts):
+                L.orc_add_kinematic_rotation(
+                    self.h, bid, np.ascontiguousarray(b.kin_verts, np.uint32),
+                    len(b.kin_verts), np.asarray(b.kin_center, np.float64),
+                    np.asarray(b.kin_axis, np.float64), b.kin_omega)
+            if b.ext_acc is not None:
+                L.orc_set_external_acceleration(
+                    self.h, bid, np.ascontiguousarray(b.ext_acc, np.float64).ravel())
+            self.body_ranges.append((self.n_verts, len(b.x0)))
+            self.n_verts += len(b.x0)
+            self.n_tets += len(b.tets)
+        if scene.ground is not None:
+            n, d = scene.ground
+            L.orc_add_ground_plane(self.h, np.asarray(n, np.float64), d)
+        if scene.bodies and scene.bodies[0].v_init is not None:
+            v = np.concatenate([b.v_init if b.v_init is not None else np.zeros_like(b.x0)
+                                for b in scene.bodies])
+            self.set(FIELD_V, v)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def set_order(self, order: np.ndarray, offsets: np.ndarray | None = None):
+        order = np.ascontiguousarray(order, np.uint32)
+        if offsets is None:
+            rc = self.L.orc_set_tet_order(self.h, order, len(order), None, 0)
+        else:
+            off = np.ascontiguousarray(offsets, np.uint32)
+            self._off = off
+            rc = self.L.orc_set_tet_order(self.h, order, len(order),
+                                          off.ctypes.data, len(off) - 1)
+        if rc:
+            raise ValueError("bad tet order")
+
+    def step(self, frames: int = 1, fast: bool = False):
+        s = self.scene
+        f = self.L.orc_step_fast if fast else self.L.orc_step
+        for _ in range(frames):
+            f(self.h, s.frame_dt, s.substeps, s.iterations)
+
+    def get(self, field: int = FIELD_X) -> np.ndarray:
+        out = np.zeros(self.n_verts * 3)
+        self.L.orc_get(self.h, field, out)
+        return out.reshape(-1, 3)
+
+    def set(self, field: int, x: np.ndarray):
+        self.L.orc_set(self.h, field, np.ascontiguousarray(x, np.float64).ravel())
+
+    def masses(self) -> np.ndarray:
+        out = np.zeros(self.n_verts)
+        self.L.orc_get_masses(self.h, out)
+        return out
+
+    def surface(self, body: int = 0) -> np.ndarray:
+        n = self.L.orc_get_surface(self.h, body, np.zeros(0, np.uint32), 0)
+        out = np.zeros(n, np.uint32)
+        self.L.orc_get_surface(self.h, body, out, n)
+        return out
+
+    def lambdas(self) -> np.ndarray:
+        out = np.zeros(self.n_tets * 2)
+        self.L.orc_get_lambdas(self.h, out)
+        return out.reshape(-1, 2)
+
+    def detect_contacts(self):
+        self.L.orc_detect_contacts(self.h)
+        n = self.L.orc_get_contacts(self.h, np.zeros(0, np.uint32), np.zeros(0), 0)
+        v = np.zeros(n, np.uint32)
+        qn = np.zeros(6 * n)
+        self.L.orc_get_contacts(self.h, v, qn, n)
+        return v, qn.reshape(-1, 6)
+
+    def stats(self) -> dict:
+        out = np.zeros(4)
+        self.L.orc_stats(self.h, out)
+        return {"residual": out[0], "energy": out[1], "residual_elastic": out[2],
+                "residual_contact": out[3],
+                "projections": int(self.L.orc_projections(self.h)),
+                "contacts": int(self.L.orc_n_contacts(self.h))}
+
+    def time_frames(self, n: int) -> float:
+        s = self.scene
+        return self.L.orc_time_frames(self.h, s.frame_dt, s.substeps, s.iterations, n)
+
+
+def svd3(F: np.ndarray):
+    U = np.zeros(9)
+    s = np.zeros(3)
+    V = np.zeros(9)
+    lib().orc_svd3(np.ascontiguousarray(F, np.float64).ravel(), U, s, V)
+    return U.reshape(3, 3), s, V.reshape(3, 3)

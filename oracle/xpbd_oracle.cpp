@@ -1,0 +1,860 @@
+// FP64 CPU oracle for the XPBD substep loop.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library:
+// it is loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU
+// baseline arm, never by the product path.
+//
+// It restates, in plain C++17 with no dependencies, the reference's
+// sequential XPBD loop (Q-Minh/soft-body-simulator):
+//   * timestep_t::step                 src/physics/timestep.cpp:20-70
+//   * gauss_seidel_solver_t::solve     src/physics/gauss_seidel_solver.cpp:8-37
+//   * constraint_t::prepare_for_projection  src/physics/constraint.cpp:12-16
+//   * green_constraint_t (ctor + project_positions + signed_volume)
+//                                      src/physics/xpbd/green_constraint.cpp:11-173
+//   * collision_constraint_t           src/physics/xpbd/collision_constraint.cpp:21-48
+//   * plane contacts on surface vertices  src/physics/collision/bvh_model.cpp:72-94,
+//                                      sdf_model.cpp:52-64, contact_handler.cpp:14-54
+//   * particle_t::invmass / a()        src/physics/particle.cpp:39-53
+// with the same data structure the reference uses: an array of particle
+// records (x0, xi, xn, x, v, f, m) and a list of constraint objects projected
+// through a virtual call, one at a time, in list order.
+//
+// Additions the reference does not have (each marked where it is written):
+// stable Neo-Hookean constraints (Macklin & Mueller 2021), lumped masses,
+// gravity as an acceleration, kinematic (prescribed) vertices, an external
+// acceleration field, body-body vertex-in-tet contacts from a CPU spatial
+// hash, the XPBD residual and energy, and a hook that permutes the elastic
+// constraint list into the GPU's colour order so both run the same sweep.
+// An optional thread count runs each colour's (vertex-disjoint) constraints
+// in parallel; the arithmetic per constraint is unchanged, so the result is
+// bit-identical to the sequential sweep.
+//
+// Parity status: the reference cannot be compiled here (Eigen, Discregrid and
+// the GL stack are absent) and ships no tests or golden vectors, so this
+// oracle is "parity unpinned" against reference outputs.  It is cross-checked
+// against an independent numpy restatement (oracle/numpy_oracle.py, which
+// uses LAPACK's SVD in place of the Jacobi SVD below) and against analytic
+// known answers of the reference's formulas.
+//
+// The 3x3 SVD: Eigen's JacobiSVD is third-party and not in the reference
+// tree; here it is a one-sided (Hestenes) Jacobi SVD written from the textbook
+// method (Golub & Van Loan, "Matrix Computations", 8.6.3), returning Eigen's
+// documented convention: singular values >= 0, sorted in decreasing order.
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <unordered_map>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+struct vec3 {
+    double x = 0, y = 0, z = 0;
+    vec3() = default;
+    vec3(double a, double b, double c) : x(a), y(b), z(c) {}
+    double& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+    double operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+static inline vec3 operator+(vec3 a, vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline vec3 operator-(vec3 a, vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline vec3 operator-(vec3 a) { return {-a.x, -a.y, -a.z}; }
+static inline vec3 operator*(vec3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+static inline vec3 operator*(double s, vec3 a) { return {a.x * s, a.y * s, a.z * s}; }
+static inline vec3 operator/(vec3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+static inline vec3& operator+=(vec3& a, vec3 b) { a.x += b.x; a.y += b.y; a.z += b.z; return a; }
+static inline double dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline vec3 cross(vec3 a, vec3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+static inline double norm(vec3 a) { return std::sqrt(dot(a, a)); }
+
+// 3x3 matrix, row-major m[r][c].
+struct mat3 {
+    double m[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    static mat3 identity() { mat3 r; r.m[0][0] = r.m[1][1] = r.m[2][2] = 1; return r; }
+    static mat3 from_cols(vec3 a, vec3 b, vec3 c) {
+        mat3 r;
+        for (int i = 0; i < 3; ++i) { r.m[i][0] = a[i]; r.m[i][1] = b[i]; r.m[i][2] = c[i]; }
+        return r;
+    }
+    vec3 col(int c) const { return {m[0][c], m[1][c], m[2][c]}; }
+    void set_col(int c, vec3 v) { m[0][c] = v.x; m[1][c] = v.y; m[2][c] = v.z; }
+    mat3 T() const { mat3 r; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[i][j] = m[j][i]; return r; }
+    double det() const {
+        return m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+               m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+               m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    }
+    double trace() const { return m[0][0] + m[1][1] + m[2][2]; }
+};
+static inline mat3 operator*(const mat3& a, const mat3& b) {
+    mat3 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            r.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j] + a.m[i][2] * b.m[2][j];
+    return r;
+}
+static inline mat3 operator*(const mat3& a, double s) {
+    mat3 r; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] * s; return r;
+}
+static inline mat3 operator+(const mat3& a, const mat3& b) {
+    mat3 r; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] + b.m[i][j]; return r;
+}
+static inline mat3 operator-(const mat3& a, const mat3& b) {
+    mat3 r; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] - b.m[i][j]; return r;
+}
+static inline mat3 inverse(const mat3& a) {
+    double d = a.det();
+    mat3 r;
+    r.m[0][0] = (a.m[1][1] * a.m[2][2] - a.m[1][2] * a.m[2][1]) / d;
+    r.m[0][1] = (a.m[0][2] * a.m[2][1] - a.m[0][1] * a.m[2][2]) / d;
+    r.m[0][2] = (a.m[0][1] * a.m[1][2] - a.m[0][2] * a.m[1][1]) / d;
+    r.m[1][0] = (a.m[1][2] * a.m[2][0] - a.m[1][0] * a.m[2][2]) / d;
+    r.m[1][1] = (a.m[0][0] * a.m[2][2] - a.m[0][2] * a.m[2][0]) / d;
+    r.m[1][2] = (a.m[0][2] * a.m[1][0] - a.m[0][0] * a.m[1][2]) / d;
+    r.m[2][0] = (a.m[1][0] * a.m[2][1] - a.m[1][1] * a.m[2][0]) / d;
+    r.m[2][1] = (a.m[0][1] * a.m[2][0] - a.m[0][0] * a.m[2][1]) / d;
+    r.m[2][2] = (a.m[0][0] * a.m[1][1] - a.m[0][1] * a.m[1][0]) / d;
+    return r;
+}
+static inline double frob2(const mat3& a) {
+    double s = 0; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) s += a.m[i][j] * a.m[i][j]; return s;
+}
+
+// One-sided Jacobi SVD: F = U diag(s) V^T, s >= 0 descending.
+void svd3(const mat3& F, mat3& U, vec3& s, mat3& V) {
+    vec3 a[3] = {F.col(0), F.col(1), F.col(2)};
+    vec3 v[3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        bool rotated = false;
+        for (auto& pq : pairs) {
+            int p = pq[0], q = pq[1];
+            double alpha = dot(a[p], a[p]), beta = dot(a[q], a[q]), gamma = dot(a[p], a[q]);
+            if (std::fabs(gamma) <= 1e-15 * std::sqrt(alpha * beta) || gamma == 0.0) continue;
+            rotated = true;
+            double zeta = (beta - alpha) / (2.0 * gamma);
+            double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+            double c = 1.0 / std::sqrt(1.0 + t * t), sn = c * t;
+            vec3 ap = a[p], aq = a[q];
+            a[p] = c * ap - sn * aq;
+            a[q] = sn * ap + c * aq;
+            vec3 vp = v[p], vq = v[q];
+            v[p] = c * vp - sn * vq;
+            v[q] = sn * vp + c * vq;
+        }
+        if (!rotated) break;
+    }
+    double sig[3] = {norm(a[0]), norm(a[1]), norm(a[2])};
+    int idx[3] = {0, 1, 2};
+    std::sort(idx, idx + 3, [&](int i, int j) { return sig[i] > sig[j]; });
+    vec3 u[3];
+    double maxs = std::max(sig[idx[0]], 1e-300);
+    bool ok[3];
+    for (int k = 0; k < 3; ++k) {
+        int i = idx[k];
+        s[k] = sig[i];
+        V.set_col(k, v[i]);
+        ok[k] = sig[i] > 1e-13 * maxs && sig[i] > 1e-300;
+        u[k] = ok[k] ? a[i] / sig[i] : vec3{};
+    }
+    // Complete U for (numerically) zero singular values.
+    if (!ok[0]) { u[0] = {1, 0, 0}; }
+    if (!ok[1]) {
+        vec3 e = std::fabs(u[0].x) < 0.9 ? vec3{1, 0, 0} : vec3{0, 1, 0};
+        vec3 w = e - u[0] * dot(e, u[0]);
+        u[1] = w / norm(w);
+    }
+    if (!ok[2]) u[2] = cross(u[0], u[1]);
+    for (int k = 0; k < 3; ++k) U.set_col(k, u[k]);
+}
+
+// ---------------------------------------------------------------------------
+// State: particle_t restated from include/sbs/physics/particle.h:45-52.
+struct particle_t {
+    vec3 x0, xi, xn, x, v, f;
+    double m = 1.0;
+    // additions: prescribed motion and a body acceleration field
+    int kin = -1;        // index into sim.kinematics, -1 if free
+    vec3 ext_acc;
+    double invmass() const { return m > 0.0 ? 1.0 / m : 0.0; }   // particle.cpp:39-44
+    vec3 a() const { return f * invmass(); }                       // particle.cpp:50-53
+};
+
+struct sim_t;
+
+// constraint_t restated from include/sbs/physics/constraint.h:12-35.
+struct constraint_t {
+    double alpha, beta, lagrange = 0.0;
+    constraint_t(double a, double b) : alpha(a), beta(b) {}
+    virtual ~constraint_t() = default;
+    virtual void prepare_for_projection() { lagrange = 0.0; }
+    virtual void project_positions(sim_t& sim, double dt) = 0;
+    // sum of (C + alpha~ lambda)^2 and the elastic energy at the current xi
+    virtual void residual(const sim_t& sim, double dt, double& r2, double& energy) const = 0;
+};
+
+struct kinematic_t {
+    vec3 center, axis;
+    double omega;
+};
+
+struct plane_t { vec3 n; double d; };
+
+struct body_t {
+    uint32_t v0, nv, t0, nt;
+    std::vector<uint32_t> surface;   // global vertex ids, ascending
+    std::vector<std::array<uint32_t, 3>> surface_tris;  // global ids, outward
+    int model;
+};
+
+struct params_t {
+    double alpha = 1e-4, beta = 0.0, collision_alpha = 1e-8;
+    vec3 gravity{0.0, -9.81, 0.0};
+    int gravity_mode = 0;   // 0 acceleration (m g as force), 1 force as in timestep.cpp:39
+    double hash_cell = 0.0;
+    int body_contacts = 0;
+};
+
+struct stats_t {
+    double residual = 0, energy = 0, r2_elastic = 0, r2_contact = 0;
+    uint64_t projections = 0;
+    uint32_t n_contacts = 0, n_body_contacts = 0;
+};
+
+struct sim_t {
+    params_t prm;
+    std::vector<particle_t> particles;
+    std::vector<body_t> bodies;
+    std::vector<std::unique_ptr<constraint_t>> constraints;            // elastic, global tet order
+    std::vector<constraint_t*> sweep;                                  // permuted projection order
+    std::vector<uint32_t> colour_offsets;                              // optional, into sweep
+    std::vector<std::unique_ptr<constraint_t>> collision_constraints;  // rebuilt every frame
+    std::vector<uint32_t> ground_end;                                  // ground contacts per plane
+    std::vector<kinematic_t> kinematics;
+    std::vector<plane_t> planes;
+    double time = 0.0;
+    int threads = 1;
+    stats_t st;
+    std::vector<double> residual_history;   // per iteration, when enabled
+    int record_history = 0;
+};
+
+// ---------------------------------------------------------------------------
+// green_constraint_t: src/physics/xpbd/green_constraint.cpp:11-173
+struct green_constraint_t final : constraint_t {
+    uint32_t v[4];
+    mat3 DmInv;
+    double V0, mu, lambda;
+
+    green_constraint_t(double a, double b, const sim_t& sim, const uint32_t* vi, double E, double nu)
+        : constraint_t(a, b) {
+        for (int i = 0; i < 4; ++i) v[i] = vi[i];
+        const auto& p = sim.particles;
+        mat3 Dm = mat3::from_cols(p[v[0]].x0 - p[v[3]].x0, p[v[1]].x0 - p[v[3]].x0,
+                                  p[v[2]].x0 - p[v[3]].x0);
+        DmInv = inverse(Dm);
+        V0 = (1.0 / 6.0) * Dm.det();
+        mu = E / (2.0 * (1.0 + nu));
+        lambda = (E * nu) / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    }
+
+    static double signed_volume(vec3 p1, vec3 p2, vec3 p3, vec3 p4) {
+        return (1.0 / 6.0) * mat3::from_cols(p1 - p4, p2 - p4, p3 - p4).det();
+    }
+
+    // Steps 2-8 of project_positions: psi and the four gradients f_i
+    // (f = -grad C), evaluated at xi.
+    void evaluate(const sim_t& sim, double& psi, vec3 f[4]) const {
+        const auto& P = sim.particles;
+        vec3 x1 = P[v[0]].xi, x2 = P[v[1]].xi, x3 = P[v[2]].xi, x4 = P[v[3]].xi;
+        double Vs = signed_volume(x1, x2, x3, x4);
+        bool Vpos = Vs >= 0.0, V0pos = V0 >= 0.0;
+        bool inverted = (Vpos && !V0pos) || (!Vpos && V0pos);
+        mat3 Ds = mat3::from_cols(x1 - x4, x2 - x4, x3 - x4);
+        mat3 F = Ds * DmInv;
+        mat3 U, Vm; vec3 sg;
+        svd3(F, U, sg, Vm);
+        mat3 Fhat;
+        Fhat.m[0][0] = sg[0]; Fhat.m[1][1] = sg[1]; Fhat.m[2][2] = sg[2];
+        if (inverted) {
+            Fhat.m[2][2] = -Fhat.m[2][2];
+            U.set_col(2, -U.col(2));
+        }
+        const double min_sv = 0.577;
+        for (int i = 0; i < 3; ++i) Fhat.m[i][i] = std::max(Fhat.m[i][i], min_sv);
+        mat3 I = mat3::identity();
+        mat3 Ehat = (Fhat.T() * Fhat - I) * 0.5;
+        double EhatTrace = Ehat.trace();
+        mat3 Phat = Fhat * (Ehat * (2.0 * mu) + I * (lambda * EhatTrace));
+        mat3 E = U * Ehat * Vm.T();     // as written in the reference (U, not V)
+        double Etr = E.trace();
+        psi = mu * frob2(E) + 0.5 * lambda * Etr * Etr;
+        mat3 Piola = U * Phat * Vm.T();
+        double aV0 = std::fabs(V0);
+        mat3 H = Piola * DmInv.T() * (-aV0);
+        f[0] = H.col(0); f[1] = H.col(1); f[2] = H.col(2);
+        f[3] = -(f[0] + f[1] + f[2]);
+    }
+
+    void project_positions(sim_t& sim, double dt) override {
+        auto& P = sim.particles;
+        double w[4];
+        for (int i = 0; i < 4; ++i) w[i] = P[v[i]].invmass();
+        double psi; vec3 f[4];
+        evaluate(sim, psi, f);
+        double S = 0;
+        for (int i = 0; i < 4; ++i) S += w[i] * dot(f[i], f[i]);
+        const double epsilon = 1e-20;
+        if (S < epsilon) return;
+        double C = std::fabs(V0) * psi;
+        double dt2 = dt * dt;
+        double at = alpha / dt2, bt = beta * dt2, gamma = at * bt / dt;
+        double gd = 0;
+        for (int i = 0; i < 4; ++i) gd += dot(f[i], P[v[i]].xi - P[v[i]].xn);
+        double num = -(C + at * lagrange) + gamma * gd;
+        double den = (1.0 + gamma) * S + at;
+        double dl = num / den;
+        lagrange += dl;
+        for (int i = 0; i < 4; ++i) P[v[i]].xi += (w[i] * -f[i]) * dl;
+    }
+
+    void residual(const sim_t& sim, double dt, double& r2, double& energy) const override {
+        double psi; vec3 f[4];
+        evaluate(sim, psi, f);
+        double C = std::fabs(V0) * psi;
+        double h = C + alpha / (dt * dt) * lagrange;
+        r2 += h * h;
+        energy += C;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Stable Neo-Hookean tet (Macklin & Mueller 2021, "A Constraint-based
+// Formulation of Stable Neo-Hookean Materials"): deviatoric C_D = ||F||_F with
+// compliance 1/(mu |V0|) and hydrostatic C_H = det F - (1 + mu/lambda) with
+// compliance 1/(lambda |V0|), each with its own multiplier, solved together
+// as the paper's coupled 2x2 system.  (Solving them one after the other with
+// multipliers reset every substep drifts away from the rest state, because
+// C_D is not zero at rest.)  Not in the reference.
+struct snh_constraint_t final : constraint_t {
+    uint32_t v[4];
+    mat3 DmInv;
+    double V0, mu, lambda, lagrange_h = 0.0;
+
+    snh_constraint_t(const sim_t& sim, const uint32_t* vi, double E, double nu) : constraint_t(0, 0) {
+        for (int i = 0; i < 4; ++i) v[i] = vi[i];
+        const auto& p = sim.particles;
+        mat3 Dm = mat3::from_cols(p[v[0]].x0 - p[v[3]].x0, p[v[1]].x0 - p[v[3]].x0,
+                                  p[v[2]].x0 - p[v[3]].x0);
+        DmInv = inverse(Dm);
+        V0 = (1.0 / 6.0) * Dm.det();
+        mu = E / (2.0 * (1.0 + nu));
+        lambda = (E * nu) / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    }
+    void prepare_for_projection() override { lagrange = 0.0; lagrange_h = 0.0; }
+
+    mat3 deformation(const sim_t& sim) const {
+        const auto& P = sim.particles;
+        vec3 x4 = P[v[3]].xi;
+        return mat3::from_cols(P[v[0]].xi - x4, P[v[1]].xi - x4, P[v[2]].xi - x4) * DmInv;
+    }
+    // gradients of C w.r.t. the 4 vertices from dC/dF
+    void grads(const mat3& dCdF, vec3 g[4]) const {
+        mat3 G = dCdF * DmInv.T();
+        g[0] = G.col(0); g[1] = G.col(1); g[2] = G.col(2);
+        g[3] = -(g[0] + g[1] + g[2]);
+    }
+    static mat3 cofactor(const mat3& F) {
+        vec3 f1 = F.col(0), f2 = F.col(1), f3 = F.col(2);
+        return mat3::from_cols(cross(f2, f3), cross(f3, f1), cross(f1, f2));
+    }
+    void project_positions(sim_t& sim, double dt) override {
+        auto& P = sim.particles;
+        double aV0 = std::fabs(V0), dt2 = dt * dt;
+        double atD = 1.0 / (mu * aV0 * dt2), atH = 1.0 / (lambda * aV0 * dt2);
+        mat3 F = deformation(sim);
+        double cD = std::sqrt(frob2(F));
+        if (!(cD > 1e-12)) return;
+        double cH = F.det() - (1.0 + mu / lambda);
+        vec3 gD[4], gH[4];
+        grads(F * (1.0 / cD), gD);
+        grads(cofactor(F), gH);
+        double w[4], a11 = atD, a22 = atH, a12 = 0.0;
+        for (int i = 0; i < 4; ++i) {
+            w[i] = P[v[i]].invmass();
+            a11 += w[i] * dot(gD[i], gD[i]);
+            a22 += w[i] * dot(gH[i], gH[i]);
+            a12 += w[i] * dot(gD[i], gH[i]);
+        }
+        double b1 = -(cD + atD * lagrange), b2 = -(cH + atH * lagrange_h);
+        double det = a11 * a22 - a12 * a12;
+        if (!(det > 1e-30 * a11 * a22)) return;
+        double dlD = (b1 * a22 - b2 * a12) / det;
+        double dlH = (b2 * a11 - b1 * a12) / det;
+        lagrange += dlD;
+        lagrange_h += dlH;
+        for (int i = 0; i < 4; ++i) P[v[i]].xi += (gD[i] * dlD + gH[i] * dlH) * w[i];
+    }
+    void residual(const sim_t& sim, double dt, double& r2, double& energy) const override {
+        double aV0 = std::fabs(V0), dt2 = dt * dt;
+        mat3 F = deformation(sim);
+        double cd = std::sqrt(frob2(F));
+        double ch = F.det() - (1.0 + mu / lambda);
+        double hd = cd + lagrange / (mu * aV0 * dt2);
+        double hh = ch + lagrange_h / (lambda * aV0 * dt2);
+        r2 += hd * hd + hh * hh;
+        energy += aV0 * (0.5 * mu * (cd * cd - 3.0) + 0.5 * lambda * ch * ch);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// collision_constraint_t: src/physics/xpbd/collision_constraint.cpp:21-48
+struct collision_constraint_t final : constraint_t {
+    uint32_t vi;
+    vec3 q, n;
+    collision_constraint_t(double a, double b, uint32_t v, vec3 p, vec3 nn)
+        : constraint_t(a, b), vi(v), q(p), n(nn) {}
+    double evaluate(vec3 p) const { return dot(p - q, n); }
+    void project_positions(sim_t& sim, double dt) override {
+        particle_t& p = sim.particles[vi];
+        double w = p.invmass();
+        double C = evaluate(p.xi);
+        if (C >= 0.0) return;
+        double at = alpha / (dt * dt);
+        double dl = -(C + at * lagrange) / (w + at);
+        lagrange += dl;
+        p.xi += (w * n) * dl;
+    }
+    void residual(const sim_t& sim, double dt, double& r2, double&) const override {
+        double C = evaluate(sim.particles[vi].xi);
+        if (C < 0.0) { double h = C + alpha / (dt * dt) * lagrange; r2 += h * h; }
+    }
+};
+
+// ---------------------------------------------------------------------------
+static vec3 rotate(vec3 p, vec3 axis, double ang) {
+    // Rodrigues: p cos + (k x p) sin + k (k.p)(1 - cos)
+    double c = std::cos(ang), s = std::sin(ang);
+    return p * c + cross(axis, p) * s + axis * (dot(axis, p) * (1.0 - c));
+}
+
+static vec3 kinematic_target(const sim_t& sim, const particle_t& p, double t) {
+    const kinematic_t& k = sim.kinematics[p.kin];
+    return k.center + rotate(p.x0 - k.center, k.axis, k.omega * t);
+}
+
+// Ground contacts at frame start: every surface vertex with n.x + d < 0 gets a
+// collision constraint with q = x + |sd| n (bvh_model.cpp:72-94).  Plane-major
+// order; vertices ascending within a plane.
+static void detect_ground(sim_t& sim) {
+    for (const plane_t& pl : sim.planes) {
+        for (const body_t& b : sim.bodies) {
+            for (uint32_t vi : b.surface) {
+                vec3 p = sim.particles[vi].x;
+                double sd = dot(pl.n, p) + pl.d;
+                if (!(sd < 0.0)) continue;
+                vec3 q = p + pl.n * std::fabs(sd);
+                sim.collision_constraints.push_back(std::make_unique<collision_constraint_t>(
+                    sim.prm.collision_alpha, 0.0, vi, q, pl.n));
+            }
+        }
+        sim.ground_end.push_back((uint32_t)sim.collision_constraints.size());
+    }
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+void* orc_create(double alpha, double beta, double collision_alpha, const double* gravity,
+                 int gravity_mode) {
+    sim_t* s = new sim_t();
+    s->prm.alpha = alpha;
+    s->prm.beta = beta;
+    s->prm.collision_alpha = collision_alpha;
+    s->prm.gravity = {gravity[0], gravity[1], gravity[2]};
+    s->prm.gravity_mode = gravity_mode;
+    return s;
+}
+
+void orc_destroy(void* h) { delete (sim_t*)h; }
+
+void orc_set_threads(void* h, int n) { ((sim_t*)h)->threads = n < 1 ? 1 : n; }
+
+// Adds a body: rest shape x0 [3nv], initial positions xinit [3nv] (may be
+// NULL), tets [4nt] (body-local ids).  mass [nv] (NULL -> lumped from density,
+// m_v = sum density*|V0|/4).  Returns the body id.
+int orc_add_body(void* h, const double* x0, const double* xinit, uint32_t nv, const uint32_t* tets,
+                 uint32_t nt, int model, double E, double nu, double density, const double* mass) {
+    sim_t& s = *(sim_t*)h;
+    body_t b;
+    b.v0 = (uint32_t)s.particles.size();
+    b.nv = nv;
+    b.t0 = (uint32_t)s.constraints.size();
+    b.nt = nt;
+    b.model = model;
+    for (uint32_t i = 0; i < nv; ++i) {
+        particle_t p;
+        p.x0 = {x0[3 * i], x0[3 * i + 1], x0[3 * i + 2]};
+        vec3 xi = xinit ? vec3{xinit[3 * i], xinit[3 * i + 1], xinit[3 * i + 2]} : p.x0;
+        p.xi = p.xn = p.x = xi;
+        p.m = 0.0;
+        s.particles.push_back(p);
+    }
+    // lumped masses
+    for (uint32_t t = 0; t < nt; ++t) {
+        const uint32_t* q = tets + 4 * t;
+        vec3 a = s.particles[b.v0 + q[0]].x0, bb = s.particles[b.v0 + q[1]].x0,
+             c = s.particles[b.v0 + q[2]].x0, d = s.particles[b.v0 + q[3]].x0;
+        double V = std::fabs(mat3::from_cols(a - d, bb - d, c - d).det() / 6.0);
+        for (int k = 0; k < 4; ++k) s.particles[b.v0 + q[k]].m += density * V / 4.0;
+    }
+    if (mass)
+        for (uint32_t i = 0; i < nv; ++i) s.particles[b.v0 + i].m = mass[i];
+    for (uint32_t t = 0; t < nt; ++t) {
+        uint32_t g[4];
+        for (int k = 0; k < 4; ++k) g[k] = b.v0 + tets[4 * t + k];
+        if (model == 1)
+            s.constraints.push_back(std::make_unique<snh_constraint_t>(s, g, E, nu));
+        else
+            s.constraints.push_back(
+                std::make_unique<green_constraint_t>(s.prm.alpha, s.prm.beta, s, g, E, nu));
+    }
+    // boundary: faces (topology.cpp:335-342) with one incident tet
+    std::unordered_map<uint64_t, std::pair<int, std::array<uint32_t, 3>>> faces;
+    faces.reserve(nt * 4);
+    for (uint32_t t = 0; t < nt; ++t) {
+        const uint32_t* q = tets + 4 * t;
+        uint32_t fl[4][3] = {{q[0], q[1], q[3]}, {q[1], q[2], q[3]}, {q[2], q[0], q[3]}, {q[0], q[2], q[1]}};
+        for (auto& f : fl) {
+            uint32_t srt[3] = {f[0], f[1], f[2]};
+            std::sort(srt, srt + 3);
+            uint64_t key = ((uint64_t)srt[0] * nv + srt[1]) * (uint64_t)nv + srt[2];
+            auto it = faces.find(key);
+            if (it == faces.end())
+                faces.emplace(key, std::make_pair(1, std::array<uint32_t, 3>{f[0], f[1], f[2]}));
+            else
+                it->second.first++;
+        }
+    }
+    std::vector<uint32_t> surf;
+    for (auto& kv : faces) {
+        if (kv.second.first == 2) continue;
+        for (int k = 0; k < 3; ++k) surf.push_back(b.v0 + kv.second.second[k]);
+        if (kv.second.first == 1)
+            b.surface_tris.push_back({b.v0 + kv.second.second[0], b.v0 + kv.second.second[1],
+                                      b.v0 + kv.second.second[2]});
+    }
+    std::sort(surf.begin(), surf.end());
+    surf.erase(std::unique(surf.begin(), surf.end()), surf.end());
+    std::sort(b.surface_tris.begin(), b.surface_tris.end());
+    b.surface = std::move(surf);
+    s.bodies.push_back(std::move(b));
+    s.sweep.clear();
+    for (auto& c : s.constraints) s.sweep.push_back(c.get());
+    s.colour_offsets.clear();
+    return (int)s.bodies.size() - 1;
+}
+
+void orc_pin(void* h, int body, const uint32_t* v, uint32_t n) {
+    sim_t& s = *(sim_t*)h;
+    for (uint32_t i = 0; i < n; ++i) s.particles[s.bodies[body].v0 + v[i]].m = 0.0;
+}
+
+void orc_add_kinematic_rotation(void* h, int body, const uint32_t* v, uint32_t n, const double* c,
+                                const double* axis, double omega) {
+    sim_t& s = *(sim_t*)h;
+    kinematic_t k;
+    k.center = {c[0], c[1], c[2]};
+    vec3 a{axis[0], axis[1], axis[2]};
+    k.axis = a / norm(a);
+    k.omega = omega;
+    s.kinematics.push_back(k);
+    for (uint32_t i = 0; i < n; ++i) {
+        particle_t& p = s.particles[s.bodies[body].v0 + v[i]];
+        p.m = 0.0;
+        p.kin = (int)s.kinematics.size() - 1;
+    }
+}
+
+void orc_set_external_acceleration(void* h, int body, const double* acc) {
+    sim_t& s = *(sim_t*)h;
+    const body_t& b = s.bodies[body];
+    for (uint32_t i = 0; i < b.nv; ++i)
+        s.particles[b.v0 + i].ext_acc = {acc[3 * i], acc[3 * i + 1], acc[3 * i + 2]};
+}
+
+void orc_add_ground_plane(void* h, const double* n, double d) {
+    sim_t& s = *(sim_t*)h;
+    vec3 nn{n[0], n[1], n[2]};
+    double l = norm(nn);
+    s.planes.push_back({nn / l, d / l});
+}
+
+// Permute the elastic constraint list: order[k] = global tet id projected k-th.
+// offsets (n_colours+1 entries, may be NULL) mark vertex-disjoint groups that
+// may run in parallel when threads > 1.
+int orc_set_tet_order(void* h, const uint32_t* order, uint32_t n, const uint32_t* offsets,
+                      uint32_t n_colours) {
+    sim_t& s = *(sim_t*)h;
+    if (n != s.constraints.size()) return 1;
+    s.sweep.resize(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        if (order[k] >= n) return 1;
+        s.sweep[k] = s.constraints[order[k]].get();
+    }
+    s.colour_offsets.clear();
+    if (offsets) s.colour_offsets.assign(offsets, offsets + n_colours + 1);
+    return 0;
+}
+
+static void compute_residual(sim_t& s, double dt, double& r2e, double& r2c, double& energy) {
+    r2e = r2c = energy = 0;
+    for (auto* c : s.sweep) c->residual(s, dt, r2e, energy);
+    double dummy = 0;
+    for (auto& c : s.collision_constraints) c->residual(s, dt, r2c, dummy);
+}
+
+static void project_sweep(sim_t& s, double dt) {
+    const size_t n = s.sweep.size();
+#ifdef _OPENMP
+    if (s.threads > 1 && !s.colour_offsets.empty()) {
+        for (size_t c = 0; c + 1 < s.colour_offsets.size(); ++c) {
+            int64_t b = s.colour_offsets[c], e = s.colour_offsets[c + 1];
+            if (e - b < 256) {
+                for (int64_t k = b; k < e; ++k) s.sweep[k]->project_positions(s, dt);
+            } else {
+#pragma omp parallel for num_threads(s.threads) schedule(static)
+                for (int64_t k = b; k < e; ++k) s.sweep[k]->project_positions(s, dt);
+            }
+        }
+        return;
+    }
+#endif
+    for (size_t k = 0; k < n; ++k) s.sweep[k]->project_positions(s, dt);
+}
+
+// gauss_seidel_solver_t::solve (gauss_seidel_solver.cpp:8-37): reset every
+// multiplier, then per iteration all collision constraints, then all elastic
+// constraints, in list order.
+void orc_solve(void* h, double dt, uint32_t iterations) {
+    sim_t& s = *(sim_t*)h;
+    for (auto& c : s.collision_constraints) c->prepare_for_projection();
+    for (auto* c : s.sweep) c->prepare_for_projection();
+    s.residual_history.clear();
+    for (uint32_t k = 0; k < iterations; ++k) {
+        for (auto& c : s.collision_constraints) c->project_positions(s, dt);
+        project_sweep(s, dt);
+        s.st.projections += s.sweep.size();
+        if (s.record_history) {
+            double r2e, r2c, e;
+            compute_residual(s, dt, r2e, r2c, e);
+            s.residual_history.push_back(std::sqrt(r2e + r2c));
+        }
+    }
+}
+
+static void predict(sim_t& s, double dt) {
+    const double t_next = s.time + dt;
+    const int64_t n = (int64_t)s.particles.size();
+#pragma omp parallel for num_threads(s.threads) schedule(static) if (s.threads > 1)
+    for (int64_t i = 0; i < n; ++i) {
+        particle_t& p = s.particles[i];
+        if (p.kin >= 0) {
+            p.xi = kinematic_target(s, p, t_next);
+            continue;
+        }
+        // timestep.cpp:39-41 applies gravity as a force of -9.81 on y; the
+        // acceleration mode applies m*g so that a = g for any mass.
+        if (s.prm.gravity_mode == 1) p.f += s.prm.gravity;
+        else p.f += s.prm.gravity * p.m;
+        p.f += p.ext_acc * p.m;
+        p.v = p.v + p.a() * dt;
+        p.xi = p.x + p.v * dt;
+    }
+}
+
+static void finalize(sim_t& s, double dt) {
+    const int64_t n = (int64_t)s.particles.size();
+#pragma omp parallel for num_threads(s.threads) schedule(static) if (s.threads > 1)
+    for (int64_t i = 0; i < n; ++i) {
+        particle_t& p = s.particles[i];
+        p.x = p.xi;                  // timestep.cpp:52-55
+        p.v = (p.x - p.xn) / dt;
+        p.xn = p.x;
+        p.f = {0, 0, 0};
+    }
+}
+
+void orc_detect_contacts(void* h) {
+    sim_t& s = *(sim_t*)h;
+    s.collision_constraints.clear();
+    s.ground_end.clear();
+    detect_ground(s);
+    s.st.n_contacts = (uint32_t)s.collision_constraints.size();
+}
+
+// timestep_t::step (timestep.cpp:20-70): contacts once per frame from x, then
+// per substep predict -> solve -> set x, v.
+void orc_step(void* h, double frame_dt, uint32_t substeps, uint32_t iterations) {
+    sim_t& s = *(sim_t*)h;
+    double dt = frame_dt / (double)substeps;
+    orc_detect_contacts(h);
+    for (uint32_t k = 0; k < substeps; ++k) {
+        predict(s, dt);
+        orc_solve(h, dt, iterations);
+        double r2e, r2c, e;
+        compute_residual(s, dt, r2e, r2c, e);
+        s.st.r2_elastic = r2e;
+        s.st.r2_contact = r2c;
+        s.st.residual = std::sqrt(r2e + r2c);
+        s.st.energy = e;
+        finalize(s, dt);
+        s.time += dt;
+    }
+    s.collision_constraints.clear();   // timestep.cpp:68
+}
+
+// Same as orc_step but without the residual pass (timing path).
+void orc_step_fast(void* h, double frame_dt, uint32_t substeps, uint32_t iterations) {
+    sim_t& s = *(sim_t*)h;
+    double dt = frame_dt / (double)substeps;
+    orc_detect_contacts(h);
+    for (uint32_t k = 0; k < substeps; ++k) {
+        predict(s, dt);
+        orc_solve(h, dt, iterations);
+        finalize(s, dt);
+        s.time += dt;
+    }
+    s.collision_constraints.clear();
+}
+
+void orc_predict(void* h, double dt) { predict(*(sim_t*)h, dt); }
+void orc_finalize(void* h, double dt) { sim_t& s = *(sim_t*)h; finalize(s, dt); s.time += dt; }
+
+void orc_residual(void* h, double dt, double* out3) {
+    sim_t& s = *(sim_t*)h;
+    double r2e, r2c, e;
+    compute_residual(s, dt, r2e, r2c, e);
+    out3[0] = std::sqrt(r2e + r2c);
+    out3[1] = e;
+    out3[2] = std::sqrt(r2e);
+}
+
+void orc_set_record_history(void* h, int on) { ((sim_t*)h)->record_history = on; }
+uint32_t orc_get_history(void* h, double* out, uint32_t cap) {
+    sim_t& s = *(sim_t*)h;
+    uint32_t n = (uint32_t)std::min<size_t>(cap, s.residual_history.size());
+    for (uint32_t i = 0; i < n; ++i) out[i] = s.residual_history[i];
+    return (uint32_t)s.residual_history.size();
+}
+
+// field: 0 x, 1 xi, 2 v, 3 x0
+void orc_get(void* h, int field, double* out) {
+    sim_t& s = *(sim_t*)h;
+    for (size_t i = 0; i < s.particles.size(); ++i) {
+        const particle_t& p = s.particles[i];
+        vec3 q = field == 0 ? p.x : field == 1 ? p.xi : field == 2 ? p.v : p.x0;
+        out[3 * i] = q.x; out[3 * i + 1] = q.y; out[3 * i + 2] = q.z;
+    }
+}
+
+void orc_set(void* h, int field, const double* in) {
+    sim_t& s = *(sim_t*)h;
+    for (size_t i = 0; i < s.particles.size(); ++i) {
+        particle_t& p = s.particles[i];
+        vec3 q{in[3 * i], in[3 * i + 1], in[3 * i + 2]};
+        if (field == 0) { p.x = q; p.xn = q; p.xi = q; }
+        else if (field == 1) p.xi = q;
+        else if (field == 2) p.v = q;
+    }
+}
+
+void orc_get_masses(void* h, double* out) {
+    sim_t& s = *(sim_t*)h;
+    for (size_t i = 0; i < s.particles.size(); ++i) out[i] = s.particles[i].m;
+}
+
+uint32_t orc_get_surface(void* h, int body, uint32_t* out, uint32_t cap) {
+    sim_t& s = *(sim_t*)h;
+    const auto& v = s.bodies[body].surface;
+    for (uint32_t i = 0; i < v.size() && i < cap; ++i) out[i] = v[i];
+    return (uint32_t)v.size();
+}
+
+// Lagrange multipliers in global tet order (2 per tet: deviatoric/StVK, hydrostatic).
+void orc_get_lambdas(void* h, double* out) {
+    sim_t& s = *(sim_t*)h;
+    for (size_t i = 0; i < s.constraints.size(); ++i) {
+        out[2 * i] = s.constraints[i]->lagrange;
+        auto* sn = dynamic_cast<snh_constraint_t*>(s.constraints[i].get());
+        out[2 * i + 1] = sn ? sn->lagrange_h : 0.0;
+    }
+}
+
+// Contacts of the current frame (after orc_detect_contacts): vertex, q, n.
+uint32_t orc_get_contacts(void* h, uint32_t* verts, double* qn, uint32_t cap) {
+    sim_t& s = *(sim_t*)h;
+    uint32_t n = 0;
+    for (auto& c : s.collision_constraints) {
+        auto* cc = dynamic_cast<collision_constraint_t*>(c.get());
+        if (!cc) continue;
+        if (n < cap) {
+            verts[n] = cc->vi;
+            qn[6 * n + 0] = cc->q.x; qn[6 * n + 1] = cc->q.y; qn[6 * n + 2] = cc->q.z;
+            qn[6 * n + 3] = cc->n.x; qn[6 * n + 4] = cc->n.y; qn[6 * n + 5] = cc->n.z;
+        }
+        ++n;
+    }
+    return n;
+}
+
+// Single-constraint probes (unit tests): evaluate psi and f_i for one tet.
+void orc_tet_eval(void* h, uint32_t tet, double* psi, double* f12) {
+    sim_t& s = *(sim_t*)h;
+    auto* g = dynamic_cast<green_constraint_t*>(s.constraints[tet].get());
+    if (!g) { *psi = NAN; return; }
+    vec3 f[4];
+    g->evaluate(s, *psi, f);
+    for (int i = 0; i < 4; ++i) { f12[3 * i] = f[i].x; f12[3 * i + 1] = f[i].y; f12[3 * i + 2] = f[i].z; }
+}
+
+void orc_svd3(const double* F9, double* U9, double* s3, double* V9) {
+    mat3 F, U, V; vec3 s;
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) F.m[i][j] = F9[3 * i + j];
+    svd3(F, U, s, V);
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) { U9[3 * i + j] = U.m[i][j]; V9[3 * i + j] = V.m[i][j]; }
+    s3[0] = s.x; s3[1] = s.y; s3[2] = s.z;
+}
+
+double orc_time(void* h) { return ((sim_t*)h)->time; }
+uint64_t orc_projections(void* h) { return ((sim_t*)h)->st.projections; }
+uint32_t orc_n_contacts(void* h) { return ((sim_t*)h)->st.n_contacts; }
+void orc_stats(void* h, double* out4) {
+    sim_t& s = *(sim_t*)h;
+    out4[0] = s.st.residual; out4[1] = s.st.energy;
+    out4[2] = std::sqrt(s.st.r2_elastic); out4[3] = std::sqrt(s.st.r2_contact);
+}
+
+// Wall-clock of n frames (steady_clock, as the reference's throttler times a
+// step: src/rendering/physics_timestep_throttler.cpp:36-43).
+double orc_time_frames(void* h, double frame_dt, uint32_t substeps, uint32_t iterations, uint32_t n) {
+    auto t0 = std::chrono::steady_clock::now();
+    for (uint32_t i = 0; i < n; ++i) orc_step_fast(h, frame_dt, substeps, iterations);
+    auto t1 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
+}  // extern "C"

@@ -1,0 +1,1119 @@
+// C ABI of the GB300 XPBD solver: scene set-up on the host (Morton order,
+// boundary extraction, graph colouring), device upload, frame execution as a
+// CUDA graph of per-phase kernels or as one persistent cooperative kernel,
+// and state transfer.  Declarations and reference mapping: include/sbs_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/sbs_gpu.h"
+#include "xpbd_internal.cuh"
+
+using namespace sbs;
+
+namespace {
+
+struct BodyHost {
+    uint32_t v0 = 0, nv = 0, t0 = 0, nt = 0;
+    std::vector<uint32_t> new_to_old;  // body-local
+    std::vector<uint32_t> old_to_new;
+};
+
+struct GraphKey {
+    double dt;
+    uint32_t substeps, iterations;
+    bool operator<(const GraphKey& o) const {
+        if (dt != o.dt) return dt < o.dt;
+        if (substeps != o.substeps) return substeps < o.substeps;
+        return iterations < o.iterations;
+    }
+};
+
+}  // namespace
+
+struct sbs_gpu {
+    sbs_gpu_params prm{};
+    cudaStream_t st = nullptr;
+    bool finalized = false;
+    int n_sm = 0;
+    std::string last_error;
+
+    // scene as added (global "old" vertex ids = body offset + local id)
+    std::vector<double> x0, xinit, mass;
+    std::vector<uint8_t> user_mass;
+    std::vector<uint32_t> tets;          // 4 per tet, old global ids
+    std::vector<int32_t> tet_model;
+    std::vector<double> tet_mu, tet_lam, tet_density;
+    std::vector<BodyHost> bodies;
+    std::vector<int32_t> kin_group;      // per old vertex, -1 free
+    std::vector<KinGroup> groups;
+    std::vector<float> acc;
+    bool has_acc = false;
+    std::vector<Plane> planes;
+
+    // after finalize
+    uint32_t n_verts = 0, n_tets = 0;
+    std::vector<uint32_t> tet_order;     // slot -> global tet id
+    std::vector<uint32_t> colour_offsets;
+    std::vector<uint32_t> surf;          // library vertex ids
+    std::vector<float> inv_mass;         // library order
+    std::vector<uint8_t> is_kin;         // library order
+    uint32_t n_colours = 0, first_tail = 0;
+    SceneDev d{};
+    StepParams base{};
+    float4* h_stage = nullptr;           // pinned staging, n_verts float4
+    float4* h_stage2 = nullptr;
+    int* d_err = nullptr;
+    int exec_mode = SBS_EXEC_GRAPH;
+    int block = 256, grid = 0;
+    int pers_block = 256, pers_grid = 0;
+    bool tuned = false;
+    bool contacts_live = false;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<void*> allocations;
+
+    // stats
+    uint64_t frames = 0, projections = 0;
+    double last_frame_ms = 0, residual = 0, energy = 0;
+};
+
+static thread_local std::string g_err;
+
+static sbs_status fail(sbs_gpu* h, sbs_status s, const std::string& msg) {
+    if (h) h->last_error = msg;
+    g_err = msg;
+    return s;
+}
+
+#define CU(h, call)                                                                        \
+    do {                                                                                   \
+        cudaError_t _e = (call);                                                           \
+        if (_e != cudaSuccess)                                                             \
+            return fail((h), SBS_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+template <typename T>
+static sbs_status dalloc(sbs_gpu* h, T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) return fail(h, SBS_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    h->allocations.push_back((void*)*p);
+    return SBS_OK;
+}
+
+static uint32_t expand_bits(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// 30-bit Morton code of p inside [lo, hi].
+static uint32_t morton(const double* p, const double* lo, const double* hi) {
+    uint32_t c[3];
+    for (int k = 0; k < 3; ++k) {
+        double ext = hi[k] - lo[k];
+        double u = ext > 0 ? (p[k] - lo[k]) / ext : 0.0;
+        int q = (int)std::floor(u * 1023.0 + 0.5);
+        c[k] = (uint32_t)std::min(1023, std::max(0, q));
+    }
+    return (expand_bits(c[0]) << 2) | (expand_bits(c[1]) << 1) | expand_bits(c[2]);
+}
+
+static void invert3(const double m[3][3], double r[3][3], double* det) {
+    double d = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+               m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    *det = d;
+    r[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]) / d;
+    r[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) / d;
+    r[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) / d;
+    r[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) / d;
+    r[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) / d;
+    r[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) / d;
+    r[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]) / d;
+    r[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) / d;
+    r[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) / d;
+}
+
+// Colours tets (given in `order`, a Morton order) so that no two tets of a
+// colour share a vertex.  First-fit greedy, then a second pass with a size
+// cap of ~T/K per colour to balance colour sizes.  Returns the colour count
+// or -1 if more than kMaxColours are needed.
+static int colour_tets(const std::vector<uint32_t>& tets, uint32_t n_verts, const std::vector<uint32_t>& order,
+                       std::vector<int32_t>& colour) {
+    const size_t T = order.size();
+    colour.assign(tets.size() / 4, -1);
+    std::vector<std::array<uint64_t, 2>> vm(n_verts, {0ull, 0ull});
+    auto pick = [&](uint32_t t, const std::vector<uint32_t>* size, uint32_t cap) -> int {
+        uint64_t f0 = 0, f1 = 0;
+        for (int k = 0; k < 4; ++k) {
+            f0 |= vm[tets[4 * t + k]][0];
+            f1 |= vm[tets[4 * t + k]][1];
+        }
+        int first_free = -1;
+        for (int c = 0; c < kMaxColours; ++c) {
+            bool used = c < 64 ? ((f0 >> c) & 1ull) : ((f1 >> (c - 64)) & 1ull);
+            if (used) continue;
+            if (first_free < 0) first_free = c;
+            if (!size || (*size)[c] < cap) return c;
+        }
+        return first_free;
+    };
+    auto mark = [&](uint32_t t, int c) {
+        for (int k = 0; k < 4; ++k) {
+            if (c < 64) vm[tets[4 * t + k]][0] |= 1ull << c;
+            else vm[tets[4 * t + k]][1] |= 1ull << (c - 64);
+        }
+    };
+    int K = 0;
+    for (uint32_t t : order) {
+        int c = pick(t, nullptr, 0);
+        if (c < 0) return -1;
+        colour[t] = c;
+        mark(t, c);
+        K = std::max(K, c + 1);
+    }
+    // balanced pass
+    std::vector<uint32_t> size(kMaxColours, 0);
+    const uint32_t cap = (uint32_t)std::ceil((double)T / K * 1.02) + 1;
+    for (auto& m : vm) m = {0ull, 0ull};
+    std::vector<int32_t> c2(colour.size(), -1);
+    int K2 = 0;
+    for (uint32_t t : order) {
+        int c = pick(t, &size, cap);
+        if (c < 0) return K;  // keep the first-fit colouring
+        c2[t] = c;
+        mark(t, c);
+        size[c]++;
+        K2 = std::max(K2, c + 1);
+    }
+    if (K2 <= K + 2) {
+        colour.swap(c2);
+        return K2;
+    }
+    return K;
+}
+
+// Gauss-Seidel sweep order of a scene: tets sorted by Morton code of their
+// rest centroid, coloured, then ordered by (colour by decreasing size, model,
+// Morton code).  `model` may be null (all StVK).  Outputs: order[k] = tet id
+// projected k-th, offsets (K+1 colour starts), split[c] = first SNH slot of
+// colour c.  Returns the colour count K or -1.
+static int plan_sweep(const double* x0, uint32_t V, const uint32_t* tets, uint32_t T, const int32_t* model,
+                      std::vector<uint32_t>& order, std::vector<uint32_t>& offsets, std::vector<uint32_t>& split) {
+    auto mdl = [&](uint32_t t) { return model ? model[t] : (int32_t)SBS_MODEL_STVK; };
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (uint32_t i = 0; i < V; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], x0[3ull * i + k]);
+            hi[k] = std::max(hi[k], x0[3ull * i + k]);
+        }
+    std::vector<uint32_t> tm(T);
+    for (uint32_t t = 0; t < T; ++t) {
+        double c[3] = {0, 0, 0};
+        for (int k = 0; k < 4; ++k)
+            for (int a = 0; a < 3; ++a) c[a] += 0.25 * x0[3ull * tets[4ull * t + k] + a];
+        tm[t] = morton(c, lo, hi);
+    }
+    std::vector<uint32_t> morder(T);
+    std::iota(morder.begin(), morder.end(), 0u);
+    std::stable_sort(morder.begin(), morder.end(), [&](uint32_t a, uint32_t b) { return tm[a] < tm[b]; });
+    std::vector<uint32_t> tv(tets, tets + 4ull * T);
+    std::vector<int32_t> colour;
+    const int K = colour_tets(tv, V, morder, colour);
+    if (K < 0) return -1;
+    std::vector<uint32_t> csize(K, 0);
+    for (uint32_t t = 0; t < T; ++t) csize[colour[t]]++;
+    std::vector<int> crank(K);
+    std::iota(crank.begin(), crank.end(), 0);
+    std::stable_sort(crank.begin(), crank.end(), [&](int a, int b) { return csize[a] > csize[b]; });
+    std::vector<int> relabel(K);
+    for (int r = 0; r < K; ++r) relabel[crank[r]] = r;
+    std::vector<uint32_t> pos_in_m(T);
+    for (uint32_t k = 0; k < T; ++k) pos_in_m[morder[k]] = k;
+    order.resize(T);
+    std::iota(order.begin(), order.end(), 0u);
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        int ca = relabel[colour[a]], cb = relabel[colour[b]];
+        if (ca != cb) return ca < cb;
+        if (mdl(a) != mdl(b)) return mdl(a) < mdl(b);
+        return pos_in_m[a] < pos_in_m[b];
+    });
+    offsets.assign(K + 1, 0);
+    split.assign(K, 0);
+    uint32_t k = 0;
+    for (int c = 0; c < K; ++c) {
+        offsets[c] = k;
+        while (k < T && relabel[colour[order[k]]] == c && mdl(order[k]) == SBS_MODEL_STVK) ++k;
+        split[c] = k;
+        while (k < T && relabel[colour[order[k]]] == c) ++k;
+    }
+    offsets[K] = k;
+    return K;
+}
+
+extern "C" {
+
+sbs_status sbs_gpu_plan_sweep(const double* x0, uint32_t n_verts, const uint32_t* tets, uint32_t n_tets,
+                              const int32_t* models, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
+                              uint32_t* n_colours) {
+    if (!x0 || !tets || n_verts == 0 || n_tets == 0) return fail(nullptr, SBS_EINVAL, "plan: null/empty");
+    for (uint64_t i = 0; i < 4ull * n_tets; ++i)
+        if (tets[i] >= n_verts) return fail(nullptr, SBS_EINVAL, "plan: vertex index out of range");
+    std::vector<uint32_t> ord, off, split;
+    const int K = plan_sweep(x0, n_verts, tets, n_tets, models, ord, off, split);
+    if (K < 0) return fail(nullptr, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
+    if (n_colours) *n_colours = (uint32_t)K;
+    if (order) std::copy(ord.begin(), ord.end(), order);
+    if (offsets) {
+        if (cap_offsets < (uint32_t)K + 1) return fail(nullptr, SBS_EINVAL, "plan: offsets capacity");
+        std::copy(off.begin(), off.end(), offsets);
+    }
+    return SBS_OK;
+}
+
+const char* sbs_gpu_status_string(sbs_status s) {
+    switch (s) {
+        case SBS_OK: return "ok";
+        case SBS_EINVAL: return "invalid argument";
+        case SBS_ECUDA: return "CUDA error";
+        case SBS_ETIMEOUT: return "device wait timed out";
+        case SBS_ENAN: return "non-finite state";
+        case SBS_ESTATE: return "call not valid in this state";
+        case SBS_ENOMEM: return "out of device memory";
+        case SBS_ECOLOUR: return "too many colours";
+    }
+    return "unknown";
+}
+
+const char* sbs_gpu_last_error(const sbs_gpu* h) { return h ? h->last_error.c_str() : g_err.c_str(); }
+
+sbs_status sbs_gpu_params_default(sbs_gpu_params* p) {
+    if (!p) return SBS_EINVAL;
+    std::memset(p, 0, sizeof(*p));
+    p->compliance = 1e-4;
+    p->damping = 0.0;
+    p->collision_compliance = 1e-8;
+    p->gravity[0] = 0.0;
+    p->gravity[1] = -9.81;
+    p->gravity[2] = 0.0;
+    p->gravity_mode = SBS_GRAVITY_ACCELERATION;
+    p->device = 0;
+    p->exec_mode = SBS_EXEC_AUTO;
+    p->block_size = 0;
+    p->ctas_per_sm = 0;
+    p->tail_threshold = -1;
+    p->body_contacts = 0;
+    p->hash_cell = 0.0f;
+    p->max_body_contacts = 0;
+    p->check_finite = 1;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_create(const sbs_gpu_params* p, sbs_gpu** out) {
+    if (!out) return SBS_EINVAL;
+    *out = nullptr;
+    sbs_gpu_params prm;
+    if (p) prm = *p;
+    else sbs_gpu_params_default(&prm);
+    if (prm.gravity_mode != 0 && prm.gravity_mode != 1) return fail(nullptr, SBS_EINVAL, "gravity_mode");
+    if (prm.exec_mode < 0 || prm.exec_mode > 2) return fail(nullptr, SBS_EINVAL, "exec_mode");
+    if (prm.block_size != 0 && (prm.block_size < 32 || prm.block_size > 512 || prm.block_size % 32))
+        return fail(nullptr, SBS_EINVAL, "block_size must be a multiple of 32 in [32, 512]");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, SBS_ECUDA, "no CUDA device available");
+    if (prm.device < 0 || prm.device >= ndev) return fail(nullptr, SBS_EINVAL, "device ordinal out of range");
+    sbs_gpu* h = new sbs_gpu();
+    h->prm = prm;
+    cudaError_t e = cudaSetDevice(prm.device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, prm.device);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
+    if (e != cudaSuccess) {
+        std::string m = cudaGetErrorString(e);
+        sbs_gpu_destroy(h);
+        return fail(nullptr, SBS_ECUDA, "create: " + m);
+    }
+    *out = h;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_add_body(sbs_gpu* h, const double* x0, const double* x_init, uint32_t n_verts,
+                            const uint32_t* tets, uint32_t n_tets, const sbs_gpu_material* mat,
+                            const double* mass, int32_t* body_id) {
+    if (!h || !x0 || !tets || !mat || n_verts == 0 || n_tets == 0) return fail(h, SBS_EINVAL, "add_body: null/empty");
+    if (h->finalized) return fail(h, SBS_ESTATE, "add_body after finalize");
+    if (mat->model != SBS_MODEL_STVK && mat->model != SBS_MODEL_SNH) return fail(h, SBS_EINVAL, "material model");
+    if (!(mat->young > 0) || !(mat->poisson > -1.0 && mat->poisson < 0.5) || !(mat->density >= 0))
+        return fail(h, SBS_EINVAL, "material parameters");
+    for (uint64_t i = 0; i < 4ull * n_tets; ++i)
+        if (tets[i] >= n_verts) return fail(h, SBS_EINVAL, "tet vertex index out of range");
+    for (uint64_t i = 0; i < 3ull * n_verts; ++i)
+        if (!std::isfinite(x0[i]) || (x_init && !std::isfinite(x_init[i])))
+            return fail(h, SBS_EINVAL, "non-finite position");
+    BodyHost b;
+    b.v0 = (uint32_t)(h->x0.size() / 3);
+    b.nv = n_verts;
+    b.t0 = (uint32_t)(h->tets.size() / 4);
+    b.nt = n_tets;
+    if ((uint64_t)b.v0 + n_verts >= (1ull << 31) || (uint64_t)b.t0 + n_tets >= (1ull << 31))
+        return fail(h, SBS_EINVAL, "scene too large");
+    h->x0.insert(h->x0.end(), x0, x0 + 3ull * n_verts);
+    if (x_init) h->xinit.insert(h->xinit.end(), x_init, x_init + 3ull * n_verts);
+    else h->xinit.insert(h->xinit.end(), x0, x0 + 3ull * n_verts);
+    // lumped masses: density * |V0| / 4 per incident tet
+    std::vector<double> m(n_verts, 0.0);
+    for (uint32_t t = 0; t < n_tets; ++t) {
+        const uint32_t* q = tets + 4ull * t;
+        double D[3][3];
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) D[r][c] = x0[3ull * q[c] + r] - x0[3ull * q[3] + r];
+        double det = D[0][0] * (D[1][1] * D[2][2] - D[1][2] * D[2][1]) - D[0][1] * (D[1][0] * D[2][2] - D[1][2] * D[2][0]) +
+                     D[0][2] * (D[1][0] * D[2][1] - D[1][1] * D[2][0]);
+        if (!(std::fabs(det) > 0)) return fail(h, SBS_EINVAL, "degenerate rest tet");
+        double V = std::fabs(det / 6.0);
+        for (int k = 0; k < 4; ++k) m[q[k]] += mat->density * V / 4.0;
+    }
+    for (uint32_t i = 0; i < n_verts; ++i) {
+        h->mass.push_back(mass ? mass[i] : m[i]);
+        h->user_mass.push_back(mass ? 1 : 0);
+        h->kin_group.push_back(-1);
+    }
+    const double mu = mat->young / (2.0 * (1.0 + mat->poisson));
+    const double lam = mat->young * mat->poisson / ((1.0 + mat->poisson) * (1.0 - 2.0 * mat->poisson));
+    for (uint64_t i = 0; i < 4ull * n_tets; ++i) h->tets.push_back(b.v0 + tets[i]);
+    for (uint32_t t = 0; t < n_tets; ++t) {
+        h->tet_model.push_back(mat->model);
+        h->tet_mu.push_back(mu);
+        h->tet_lam.push_back(lam);
+    }
+    h->bodies.push_back(std::move(b));
+    if (body_id) *body_id = (int32_t)h->bodies.size() - 1;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_pin_vertices(sbs_gpu* h, int32_t body, const uint32_t* verts, uint32_t n) {
+    if (!h || (n && !verts)) return fail(h, SBS_EINVAL, "pin: null");
+    if (h->finalized) return fail(h, SBS_ESTATE, "pin after finalize");
+    if (body < 0 || body >= (int32_t)h->bodies.size()) return fail(h, SBS_EINVAL, "pin: body id");
+    const BodyHost& b = h->bodies[body];
+    for (uint32_t i = 0; i < n; ++i) {
+        if (verts[i] >= b.nv) return fail(h, SBS_EINVAL, "pin: vertex id");
+        h->mass[b.v0 + verts[i]] = 0.0;
+    }
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_add_kinematic_rotation(sbs_gpu* h, int32_t body, const uint32_t* verts, uint32_t n,
+                                          const double center[3], const double axis[3], double omega) {
+    if (!h || (n && !verts) || !center || !axis) return fail(h, SBS_EINVAL, "kinematic: null");
+    if (h->finalized) return fail(h, SBS_ESTATE, "kinematic after finalize");
+    if (body < 0 || body >= (int32_t)h->bodies.size()) return fail(h, SBS_EINVAL, "kinematic: body id");
+    if (h->groups.size() >= (size_t)kMaxKinGroups) return fail(h, SBS_EINVAL, "too many kinematic groups");
+    double l = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
+    if (!(l > 0)) return fail(h, SBS_EINVAL, "kinematic: zero axis");
+    KinGroup g;
+    g.cx = (float)center[0]; g.cy = (float)center[1]; g.cz = (float)center[2];
+    g.ax = (float)(axis[0] / l); g.ay = (float)(axis[1] / l); g.az = (float)(axis[2] / l);
+    g.omega = omega;
+    const BodyHost& b = h->bodies[body];
+    for (uint32_t i = 0; i < n; ++i)
+        if (verts[i] >= b.nv) return fail(h, SBS_EINVAL, "kinematic: vertex id");
+    h->groups.push_back(g);
+    for (uint32_t i = 0; i < n; ++i) {
+        h->kin_group[b.v0 + verts[i]] = (int32_t)h->groups.size() - 1;
+        h->mass[b.v0 + verts[i]] = 0.0;
+    }
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_set_external_acceleration(sbs_gpu* h, int32_t body, const float* a) {
+    if (!h || !a) return fail(h, SBS_EINVAL, "acc: null");
+    if (h->finalized) return fail(h, SBS_ESTATE, "acc after finalize");
+    if (body < 0 || body >= (int32_t)h->bodies.size()) return fail(h, SBS_EINVAL, "acc: body id");
+    const BodyHost& b = h->bodies[body];
+    h->acc.resize(h->x0.size(), 0.0f);
+    std::copy(a, a + 3ull * b.nv, h->acc.begin() + 3ull * b.v0);
+    h->has_acc = true;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_add_ground_plane(sbs_gpu* h, const double n[3], double d) {
+    if (!h || !n) return fail(h, SBS_EINVAL, "plane: null");
+    if (h->finalized) return fail(h, SBS_ESTATE, "plane after finalize");
+    if (h->planes.size() >= (size_t)kMaxPlanes) return fail(h, SBS_EINVAL, "too many planes");
+    double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(l > 0) || !std::isfinite(d)) return fail(h, SBS_EINVAL, "plane normal");
+    h->planes.push_back(Plane{(float)(n[0] / l), (float)(n[1] / l), (float)(n[2] / l), (float)(d / l)});
+    return SBS_OK;
+}
+
+static sbs_status upload(sbs_gpu* h, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return SBS_OK;
+    CU(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->st));
+    return SBS_OK;
+}
+
+static void fill_params(sbs_gpu* h, StepParams& p, double dt, uint32_t substeps, uint32_t iterations) {
+    p = h->base;
+    p.dt_d = dt;
+    p.dt = (float)dt;
+    p.inv_dt = (float)(1.0 / dt);
+    p.inv_dt2 = (float)(1.0 / (dt * dt));
+    p.stvk_alpha_tilde = (float)(h->prm.compliance / (dt * dt));
+    const double at = h->prm.compliance / (dt * dt), bt = h->prm.damping * dt * dt;
+    p.stvk_gamma = (float)(at * bt / dt);
+    p.stvk_damping = h->prm.damping != 0.0 ? 1 : 0;
+    p.contact_alpha_tilde = (float)(h->prm.collision_compliance / (dt * dt));
+    p.substeps = (int)substeps;
+    p.iterations = (int)iterations;
+}
+
+sbs_status sbs_gpu_finalize(sbs_gpu* h) {
+    if (!h) return SBS_EINVAL;
+    if (h->finalized) return fail(h, SBS_ESTATE, "finalize twice");
+    if (h->bodies.empty()) return fail(h, SBS_ESTATE, "finalize without bodies");
+    CU(h, cudaSetDevice(h->prm.device));
+    const uint32_t V = (uint32_t)(h->x0.size() / 3), T = (uint32_t)(h->tets.size() / 4);
+    h->n_verts = V;
+    h->n_tets = T;
+    // 1. per-body Morton order of vertices (bodies stay contiguous)
+    std::vector<uint32_t> old_to_new(V), new_to_old(V);
+    for (BodyHost& b : h->bodies) {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (uint32_t i = 0; i < b.nv; ++i)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], h->x0[3ull * (b.v0 + i) + k]);
+                hi[k] = std::max(hi[k], h->x0[3ull * (b.v0 + i) + k]);
+            }
+        std::vector<std::pair<uint32_t, uint32_t>> key(b.nv);
+        for (uint32_t i = 0; i < b.nv; ++i) key[i] = {morton(&h->x0[3ull * (b.v0 + i)], lo, hi), i};
+        std::stable_sort(key.begin(), key.end());
+        b.new_to_old.resize(b.nv);
+        b.old_to_new.resize(b.nv);
+        for (uint32_t n = 0; n < b.nv; ++n) {
+            b.new_to_old[n] = key[n].second;
+            b.old_to_new[key[n].second] = n;
+            old_to_new[b.v0 + key[n].second] = b.v0 + n;
+            new_to_old[b.v0 + n] = b.v0 + key[n].second;
+        }
+    }
+    // 2-4. sweep order: colour (size-descending), model, Morton code
+    std::vector<uint32_t> split;
+    const int K = plan_sweep(h->x0.data(), V, h->tets.data(), T, h->tet_model.data(), h->tet_order,
+                             h->colour_offsets, split);
+    if (K < 0) return fail(h, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
+    h->n_colours = (uint32_t)K;
+    // 5. block size, tail threshold
+    h->block = h->prm.block_size ? h->prm.block_size : 256;
+    int tail_thr = h->prm.tail_threshold >= 0 ? h->prm.tail_threshold : h->block;
+    h->first_tail = (uint32_t)K;
+    while (h->first_tail > 0 &&
+           h->colour_offsets[h->first_tail] - h->colour_offsets[h->first_tail - 1] <= (uint32_t)tail_thr)
+        --h->first_tail;
+    // 6. per-vertex data in library order
+    h->inv_mass.assign(V, 0.0f);
+    h->is_kin.assign(V, 0);
+    std::vector<float4> xw(V), vel(V), accv;
+    bool need_acc = h->has_acc || !h->groups.empty();
+    if (need_acc) accv.assign(V, make_float4(0, 0, 0, 0));
+    for (uint32_t n = 0; n < V; ++n) {
+        uint32_t o = new_to_old[n];
+        double m = h->mass[o];
+        float w = m > 0.0 ? (float)(1.0 / m) : 0.0f;
+        h->inv_mass[n] = w;
+        xw[n] = make_float4((float)h->xinit[3ull * o], (float)h->xinit[3ull * o + 1], (float)h->xinit[3ull * o + 2], w);
+        vel[n] = make_float4(0, 0, 0, 0);
+        if (h->kin_group[o] >= 0) {
+            const KinGroup& g = h->groups[h->kin_group[o]];
+            vel[n].w = (float)(1 + h->kin_group[o]);
+            h->is_kin[n] = 1;
+            accv[n] = make_float4((float)(h->x0[3ull * o] - g.cx), (float)(h->x0[3ull * o + 1] - g.cy),
+                                  (float)(h->x0[3ull * o + 2] - g.cz), 0.0f);
+        } else if (h->has_acc) {
+            accv[n] = make_float4(h->acc[3ull * o], h->acc[3ull * o + 1], h->acc[3ull * o + 2], 0.0f);
+        }
+    }
+    // 7. per-tet data in slot order
+    std::vector<uint4> tid(T);
+    std::vector<float4> d0(T), d1(T), d2(T);
+    for (uint32_t k = 0; k < T; ++k) {
+        uint32_t t = h->tet_order[k];
+        const uint32_t* q = &h->tets[4ull * t];
+        double D[3][3], Di[3][3], det;
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) D[r][c] = h->x0[3ull * q[c] + r] - h->x0[3ull * q[3] + r];
+        invert3(D, Di, &det);
+        const double V0 = det / 6.0;
+        tid[k] = make_uint4(old_to_new[q[0]], old_to_new[q[1]], old_to_new[q[2]], old_to_new[q[3]]);
+        d0[k] = make_float4((float)Di[0][0], (float)Di[0][1], (float)Di[0][2], (float)V0);
+        d1[k] = make_float4((float)Di[1][0], (float)Di[1][1], (float)Di[1][2], (float)h->tet_mu[t]);
+        d2[k] = make_float4((float)Di[2][0], (float)Di[2][1], (float)Di[2][2], (float)h->tet_lam[t]);
+    }
+    // 8. surface vertices: faces (topology.cpp:335-342) with != 2 incident tets
+    {
+        std::unordered_map<uint64_t, uint32_t> fc;
+        fc.reserve(4ull * T);
+        for (uint32_t t = 0; t < T; ++t) {
+            const uint32_t* q = &h->tets[4ull * t];
+            const uint32_t fl[4][3] = {{q[0], q[1], q[3]}, {q[1], q[2], q[3]}, {q[2], q[0], q[3]}, {q[0], q[2], q[1]}};
+            for (auto& f : fl) {
+                uint32_t s3[3] = {f[0], f[1], f[2]};
+                std::sort(s3, s3 + 3);
+                uint64_t key = ((uint64_t)s3[0] * V + s3[1]) * (uint64_t)V + s3[2];
+                fc[key]++;
+            }
+        }
+        std::vector<uint8_t> on(V, 0);
+        for (auto& kv : fc) {
+            if (kv.second == 2) continue;
+            uint64_t key = kv.first;
+            uint32_t c = (uint32_t)(key % V);
+            key /= V;
+            uint32_t b = (uint32_t)(key % V);
+            uint32_t a = (uint32_t)(key / V);
+            on[old_to_new[a]] = on[old_to_new[b]] = on[old_to_new[c]] = 1;
+        }
+        h->surf.clear();
+        for (uint32_t n = 0; n < V; ++n)
+            if (on[n]) h->surf.push_back(n);
+    }
+    // 9. device allocations and upload
+    SceneDev& d = h->d;
+    d.n_verts = V;
+    d.n_tets = T;
+    d.n_surf = (uint32_t)h->surf.size();
+    d.n_kin = 0;
+    sbs_status s;
+#define AL(p, n) if ((s = dalloc(h, &(p), (n))) != SBS_OK) return s
+    AL(d.xi, V); AL(d.xn, V); AL(d.v, V);
+    if (need_acc) { AL(d.acc, V); } else d.acc = nullptr;
+    AL(d.tet, T); AL(d.dm0, T); AL(d.dm1, T); AL(d.dm2, T); AL(d.lam0, T); AL(d.lam1, T);
+    AL(d.surf, d.n_surf);
+    const size_t ncont = (size_t)kMaxPlanes * d.n_surf;
+    AL(d.contacts, ncont); AL(d.contact_lam, ncont);
+    AL(d.counters, 16);
+    AL(d.time, 1); AL(d.err, 1); AL(d.bar, 2);
+    AL(d.red_out, 4);
+    AL(d.partials, 6 * 4096);
+#undef AL
+    d.kin_vert = nullptr;
+    d.kin_rel = nullptr;
+    d.body_contact_cap = 0;
+    if ((s = upload(h, d.xi, xw.data(), V * sizeof(float4))) != SBS_OK) return s;
+    if ((s = upload(h, d.xn, xw.data(), V * sizeof(float4))) != SBS_OK) return s;
+    if ((s = upload(h, d.v, vel.data(), V * sizeof(float4))) != SBS_OK) return s;
+    if (need_acc && (s = upload(h, d.acc, accv.data(), V * sizeof(float4))) != SBS_OK) return s;
+    if ((s = upload(h, d.tet, tid.data(), T * sizeof(uint4))) != SBS_OK) return s;
+    if ((s = upload(h, d.dm0, d0.data(), T * sizeof(float4))) != SBS_OK) return s;
+    if ((s = upload(h, d.dm1, d1.data(), T * sizeof(float4))) != SBS_OK) return s;
+    if ((s = upload(h, d.dm2, d2.data(), T * sizeof(float4))) != SBS_OK) return s;
+    if ((s = upload(h, d.surf, h->surf.data(), d.n_surf * sizeof(uint32_t))) != SBS_OK) return s;
+    CU(h, cudaMemsetAsync(d.lam0, 0, T * sizeof(float), h->st));
+    CU(h, cudaMemsetAsync(d.lam1, 0, T * sizeof(float), h->st));
+    CU(h, cudaMemsetAsync(d.counters, 0, 16 * sizeof(uint32_t), h->st));
+    CU(h, cudaMemsetAsync(d.time, 0, sizeof(double), h->st));
+    CU(h, cudaMemsetAsync(d.err, 0, sizeof(int), h->st));
+    CU(h, cudaMemsetAsync(d.bar, 0, 2 * sizeof(unsigned), h->st));
+    CU(h, cudaMallocHost((void**)&h->h_stage, V * sizeof(float4)));
+    CU(h, cudaMallocHost((void**)&h->h_stage2, V * sizeof(float4)));
+    CU(h, cudaStreamSynchronize(h->st));
+    // 10. step constants
+    StepParams& p = h->base;
+    std::memset(&p, 0, sizeof(p));
+    p.gx = (float)h->prm.gravity[0];
+    p.gy = (float)h->prm.gravity[1];
+    p.gz = (float)h->prm.gravity[2];
+    p.gravity_mode = h->prm.gravity_mode;
+    p.n_colours = K;
+    p.first_tail = (int)h->first_tail;
+    p.n_planes = (int)h->planes.size();
+    for (size_t i = 0; i < h->planes.size(); ++i) p.planes[i] = h->planes[i];
+    p.n_kin_groups = (int)h->groups.size();
+    p.has_acc = h->has_acc ? 1 : 0;
+    for (size_t i = 0; i < h->groups.size(); ++i) p.kin[i] = h->groups[i];
+    for (int c = 0; c <= K; ++c) p.colour_start[c] = h->colour_offsets[c];
+    for (int c = 0; c < K; ++c) p.colour_split[c] = split[c];
+    // 11. execution mode
+    int occ = 0;
+    CU(h, persistent_occupancy(h->block, &occ));
+    uint32_t maxc = 0;
+    for (int c = 0; c < K; ++c) maxc = std::max(maxc, h->colour_offsets[c + 1] - h->colour_offsets[c]);
+    h->grid = std::max(1, std::min(h->n_sm * 8, (int)((maxc + 31) / 32)));
+    int cps = h->prm.ctas_per_sm > 0 ? std::min(h->prm.ctas_per_sm, occ) : occ;
+    h->pers_block = h->block;
+    h->pers_grid = std::max(1, std::min(cps * h->n_sm, (int)((maxc + 31) / 32)));
+    h->exec_mode = h->prm.exec_mode == SBS_EXEC_AUTO ? SBS_EXEC_PERSISTENT : h->prm.exec_mode;
+    if (h->exec_mode == SBS_EXEC_PERSISTENT && occ < 1) h->exec_mode = SBS_EXEC_GRAPH;
+    h->tuned = h->prm.exec_mode != SBS_EXEC_AUTO;
+    h->finalized = true;
+    return SBS_OK;
+}
+
+static sbs_status check_ready(sbs_gpu* h) {
+    if (!h) return SBS_EINVAL;
+    if (!h->finalized) return fail(h, SBS_ESTATE, "call before finalize");
+    return SBS_OK;
+}
+
+static sbs_status check_err(sbs_gpu* h) {
+    int e = 0;
+    CU(h, cudaMemcpyAsync(&e, h->d.err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    if (e != 0) return fail(h, (sbs_status)e, "device reported an error (code " + std::to_string(e) + ")");
+    return SBS_OK;
+}
+
+// Enqueues one frame in graph mode (per-phase kernels).  Used both for
+// capture and for direct launches.
+static sbs_status enqueue_frame_kernels(sbs_gpu* h, const StepParams& p) {
+    const SceneDev& d = h->d;
+    cudaStream_t st = h->st;
+    CU(h, cudaMemsetAsync(d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), st));
+    CU(h, launch_detect_ground(d, p, st));
+    for (int sub = 0; sub < p.substeps; ++sub) {
+        CU(h, launch_predict(d, p, sub, st));
+        for (int it = 0; it < p.iterations; ++it) {
+            CU(h, launch_contacts(d, p, it == 0, st));
+            for (int c = 0; c < p.first_tail; ++c) CU(h, launch_colour(d, p, c, it == 0, h->block, h->grid, st));
+            CU(h, launch_tail(d, p, it == 0, h->block, st));
+        }
+        CU(h, launch_finalize(d, p, st));
+    }
+    CU(h, launch_end_frame(d, st));
+    return SBS_OK;
+}
+
+static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations) {
+    StepParams p;
+    fill_params(h, p, dt, substeps, iterations);
+    if (h->exec_mode == SBS_EXEC_PERSISTENT) {
+        // the frame kernel expects zero live contact counters (it zeroes them
+        // itself at frame end); a standalone detect may have left them set
+        if (h->contacts_live)
+            CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+        CU(h, launch_persistent_frame(h->d, p, h->pers_block, h->pers_grid, h->st));
+    } else {
+        GraphKey key{dt, substeps, iterations};
+        auto it = h->graphs.find(key);
+        if (it == h->graphs.end()) {
+            cudaGraph_t g;
+            CU(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+            sbs_status s = enqueue_frame_kernels(h, p);
+            cudaError_t e = cudaStreamEndCapture(h->st, &g);
+            if (s != SBS_OK) return s;
+            if (e != cudaSuccess) return fail(h, SBS_ECUDA, std::string("capture: ") + cudaGetErrorString(e));
+            cudaGraphExec_t ge;
+            e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(h, SBS_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+            it = h->graphs.emplace(key, ge).first;
+        }
+        CU(h, cudaGraphLaunch(it->second, h->st));
+    }
+    h->frames++;
+    h->projections += (uint64_t)substeps * iterations * h->n_tets;
+    h->contacts_live = false;
+    return SBS_OK;
+}
+
+// Autotuner: times each candidate configuration on a copy of the state and
+// restores the state afterwards.
+static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations) {
+    const SceneDev& d = h->d;
+    const size_t V = d.n_verts;
+    float4 *bxi, *bxn, *bv;
+    double* btime;
+    CU(h, cudaMalloc((void**)&bxi, V * sizeof(float4)));
+    CU(h, cudaMalloc((void**)&bxn, V * sizeof(float4)));
+    CU(h, cudaMalloc((void**)&bv, V * sizeof(float4)));
+    CU(h, cudaMalloc((void**)&btime, sizeof(double)));
+    CU(h, cudaMemcpyAsync(bxi, d.xi, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+    CU(h, cudaMemcpyAsync(bxn, d.xn, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+    CU(h, cudaMemcpyAsync(bv, d.v, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+    CU(h, cudaMemcpyAsync(btime, d.time, sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    struct Cand { int mode, block, grid; };
+    std::vector<Cand> cands;
+    uint32_t maxc = 0;
+    for (uint32_t c = 0; c < h->n_colours; ++c)
+        maxc = std::max(maxc, h->colour_offsets[c + 1] - h->colour_offsets[c]);
+    const int need = std::max(1, (int)((maxc + 31) / 32));
+    for (int blk : {128, 256}) {
+        int occ = 0;
+        if (persistent_occupancy(blk, &occ) != cudaSuccess || occ < 1) continue;
+        for (int g : {h->n_sm / 2, h->n_sm, 2 * h->n_sm, occ * h->n_sm}) {
+            int gg = std::max(1, std::min({g, occ * h->n_sm, need}));
+            bool dup = false;
+            for (auto& c : cands) dup |= (c.mode == SBS_EXEC_PERSISTENT && c.block == blk && c.grid == gg);
+            if (!dup) cands.push_back({SBS_EXEC_PERSISTENT, blk, gg});
+        }
+    }
+    cands.push_back({SBS_EXEC_GRAPH, 256, h->grid});
+    const int saved_mode = h->exec_mode, saved_pb = h->pers_block, saved_pg = h->pers_grid;
+    const uint64_t saved_frames = h->frames, saved_proj = h->projections;
+    float best = 1e30f;
+    Cand bestc{saved_mode, saved_pb, saved_pg};
+    for (const Cand& c : cands) {
+        h->exec_mode = c.mode;
+        if (c.mode == SBS_EXEC_PERSISTENT) { h->pers_block = c.block; h->pers_grid = c.grid; }
+        sbs_status s = run_frame(h, dt, substeps, iterations);  // warm-up (and graph capture)
+        if (s != SBS_OK) continue;
+        CU(h, cudaEventRecord(h->ev0, h->st));
+        for (int r = 0; r < 3 && s == SBS_OK; ++r) s = run_frame(h, dt, substeps, iterations);
+        CU(h, cudaEventRecord(h->ev1, h->st));
+        CU(h, cudaEventSynchronize(h->ev1));
+        if (s != SBS_OK) continue;
+        if (check_err(h) != SBS_OK) break;
+        float ms = 0;
+        CU(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        if (ms < best) { best = ms; bestc = c; }
+    }
+    h->exec_mode = bestc.mode;
+    if (bestc.mode == SBS_EXEC_PERSISTENT) { h->pers_block = bestc.block; h->pers_grid = bestc.grid; }
+    h->frames = saved_frames;
+    h->projections = saved_proj;
+    CU(h, cudaMemcpyAsync(d.xi, bxi, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+    CU(h, cudaMemcpyAsync(d.xn, bxn, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+    CU(h, cudaMemcpyAsync(d.v, bv, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+    CU(h, cudaMemcpyAsync(d.time, btime, sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CU(h, cudaMemsetAsync(d.counters, 0, 16 * sizeof(uint32_t), h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    cudaFree(bxi); cudaFree(bxn); cudaFree(bv); cudaFree(btime);
+    h->tuned = true;
+    (void)saved_pb; (void)saved_pg;
+    return check_err(h);
+}
+
+sbs_status sbs_gpu_step(sbs_gpu* h, double frame_dt, uint32_t substeps, uint32_t iterations) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!(frame_dt > 0) || substeps == 0 || substeps > 1000 || iterations > 100000)
+        return fail(h, SBS_EINVAL, "step: bad frame_dt/substeps/iterations");
+    const double dt = frame_dt / (double)substeps;
+    if (!h->tuned) {
+        s = autotune(h, dt, substeps, iterations);
+        if (s) return s;
+    }
+    return run_frame(h, dt, substeps, iterations);
+}
+
+sbs_status sbs_gpu_step_timed(sbs_gpu* h, double frame_dt, uint32_t substeps, uint32_t iterations) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!h->tuned) {
+        s = sbs_gpu_step(h, frame_dt, substeps, iterations);  // tunes, then steps
+        if (s) return s;
+        CU(h, cudaStreamSynchronize(h->st));
+        return check_err(h);
+    }
+    CU(h, cudaEventRecord(h->ev0, h->st));
+    s = sbs_gpu_step(h, frame_dt, substeps, iterations);
+    if (s) return s;
+    CU(h, cudaEventRecord(h->ev1, h->st));
+    CU(h, cudaEventSynchronize(h->ev1));
+    float ms = 0;
+    CU(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->last_frame_ms = ms;
+    return check_err(h);
+}
+
+sbs_status sbs_gpu_detect_contacts(sbs_gpu* h) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    StepParams p;
+    fill_params(h, p, 1.0, 1, 1);
+    CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+    CU(h, launch_detect_ground(h->d, p, h->st));
+    h->contacts_live = true;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_predict(sbs_gpu* h, double dt) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!(dt > 0)) return fail(h, SBS_EINVAL, "dt");
+    StepParams p;
+    fill_params(h, p, dt, 1, 1);
+    CU(h, launch_predict(h->d, p, 0, h->st));
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_update_velocities(sbs_gpu* h, double dt) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!(dt > 0)) return fail(h, SBS_EINVAL, "dt");
+    StepParams p;
+    fill_params(h, p, dt, 1, 1);
+    CU(h, launch_finalize(h->d, p, h->st));
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_solve(sbs_gpu* h, double dt, uint32_t iterations) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!(dt > 0)) return fail(h, SBS_EINVAL, "dt");
+    StepParams p;
+    fill_params(h, p, dt, 1, iterations);
+    if (!h->contacts_live) CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+    for (uint32_t it = 0; it < iterations; ++it) {
+        CU(h, launch_contacts(h->d, p, it == 0, h->st));
+        for (uint32_t c = 0; c < h->first_tail; ++c) CU(h, launch_colour(h->d, p, c, it == 0, h->block, h->grid, h->st));
+        CU(h, launch_tail(h->d, p, it == 0, h->block, h->st));
+    }
+    h->projections += (uint64_t)iterations * h->n_tets;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_residual(sbs_gpu* h, double dt, double* residual, double* energy) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!(dt > 0)) return fail(h, SBS_EINVAL, "dt");
+    StepParams p;
+    fill_params(h, p, dt, 1, 1);
+    const int grid = std::max(1, std::min(4096, (int)((h->n_tets + 255) / 256)));
+    CU(h, launch_residual_ex(h->d, p, 256, grid, h->contacts_live ? 0 : kMaxPlanes + 1, h->st));
+    double out[4];
+    CU(h, cudaMemcpyAsync(out, h->d.red_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    s = check_err(h);
+    if (s) return s;
+    h->residual = std::sqrt(std::max(0.0, out[0] + out[2]));
+    h->energy = out[1];
+    if (residual) *residual = h->residual;
+    if (energy) *energy = h->energy;
+    return SBS_OK;
+}
+
+static sbs_status body_range(sbs_gpu* h, int32_t body, const BodyHost** b) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (body < 0 || body >= (int32_t)h->bodies.size()) return fail(h, SBS_EINVAL, "body id");
+    *b = &h->bodies[body];
+    return SBS_OK;
+}
+
+static sbs_status read_field(sbs_gpu* h, int32_t body, const float4* dsrc, float* out, bool check) {
+    const BodyHost* b;
+    sbs_status s = body_range(h, body, &b);
+    if (s) return s;
+    CU(h, cudaMemcpyAsync(h->h_stage, dsrc + b->v0, b->nv * sizeof(float4), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    s = check_err(h);
+    if (s) return s;
+    bool finite = true;
+    for (uint32_t o = 0; o < b->nv; ++o) {
+        const float4 q = h->h_stage[b->old_to_new[o]];
+        out[3ull * o] = q.x;
+        out[3ull * o + 1] = q.y;
+        out[3ull * o + 2] = q.z;
+        finite &= std::isfinite(q.x) && std::isfinite(q.y) && std::isfinite(q.z);
+    }
+    if (check && h->prm.check_finite && !finite) return fail(h, SBS_ENAN, "non-finite positions");
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_state(sbs_gpu* h, int32_t body, float* x, float* v) {
+    if (!h) return SBS_EINVAL;
+    sbs_status s;
+    if (v && (s = read_field(h, body, h->d.v, v, false)) != SBS_OK) return s;
+    if (x && (s = read_field(h, body, h->d.xn, x, true)) != SBS_OK) return s;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_predicted(sbs_gpu* h, int32_t body, float* xi) {
+    if (!h || !xi) return fail(h, SBS_EINVAL, "null");
+    return read_field(h, body, h->d.xi, xi, true);
+}
+
+static sbs_status write_positions(sbs_gpu* h, int32_t body, const float* x, bool all) {
+    const BodyHost* b;
+    sbs_status s = body_range(h, body, &b);
+    if (s) return s;
+    CU(h, cudaStreamSynchronize(h->st));  // staging buffer reuse
+    for (uint32_t o = 0; o < b->nv; ++o) {
+        if (!std::isfinite(x[3ull * o]) || !std::isfinite(x[3ull * o + 1]) || !std::isfinite(x[3ull * o + 2]))
+            return fail(h, SBS_EINVAL, "non-finite input position");
+        const uint32_t n = b->old_to_new[o];
+        h->h_stage[n] = make_float4(x[3ull * o], x[3ull * o + 1], x[3ull * o + 2], h->inv_mass[b->v0 + n]);
+    }
+    const size_t bytes = b->nv * sizeof(float4);
+    CU(h, cudaMemcpyAsync(h->d.xi + b->v0, h->h_stage, bytes, cudaMemcpyHostToDevice, h->st));
+    if (all) CU(h, cudaMemcpyAsync(h->d.xn + b->v0, h->h_stage, bytes, cudaMemcpyHostToDevice, h->st));
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_set_state(sbs_gpu* h, int32_t body, const float* x, const float* v) {
+    if (!h) return SBS_EINVAL;
+    sbs_status s;
+    if (x && (s = write_positions(h, body, x, true)) != SBS_OK) return s;
+    if (v) {
+        const BodyHost* b;
+        if ((s = body_range(h, body, &b)) != SBS_OK) return s;
+        for (uint32_t o = 0; o < b->nv; ++o) {
+            const uint32_t n = b->old_to_new[o];
+            float flag = 0.0f;
+            if (h->is_kin[b->v0 + n]) flag = (float)(1 + h->kin_group[b->v0 + o]);
+            h->h_stage2[n] = make_float4(v[3ull * o], v[3ull * o + 1], v[3ull * o + 2], flag);
+        }
+        CU(h, cudaMemcpyAsync(h->d.v + b->v0, h->h_stage2, b->nv * sizeof(float4), cudaMemcpyHostToDevice, h->st));
+    }
+    CU(h, cudaStreamSynchronize(h->st));
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_set_predicted(sbs_gpu* h, int32_t body, const float* xi) {
+    if (!h || !xi) return fail(h, SBS_EINVAL, "null");
+    sbs_status s = write_positions(h, body, xi, false);
+    if (s) return s;
+    CU(h, cudaStreamSynchronize(h->st));
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_tet_order(sbs_gpu* h, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
+                                 uint32_t* n_colours) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (n_colours) *n_colours = h->n_colours;
+    if (order) std::copy(h->tet_order.begin(), h->tet_order.end(), order);
+    if (offsets) {
+        if (cap_offsets < h->n_colours + 1) return fail(h, SBS_EINVAL, "offsets capacity");
+        std::copy(h->colour_offsets.begin(), h->colour_offsets.end(), offsets);
+    }
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_lambdas(sbs_gpu* h, float* lambdas) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!lambdas) return fail(h, SBS_EINVAL, "null");
+    std::vector<float> a(h->n_tets), b(h->n_tets);
+    CU(h, cudaMemcpyAsync(a.data(), h->d.lam0, h->n_tets * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaMemcpyAsync(b.data(), h->d.lam1, h->n_tets * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    for (uint32_t k = 0; k < h->n_tets; ++k) {
+        lambdas[2ull * h->tet_order[k]] = a[k];
+        lambdas[2ull * h->tet_order[k] + 1] = b[k];
+    }
+    return check_err(h);
+}
+
+// library vertex id -> global id in add order
+static uint32_t to_global(const sbs_gpu* h, uint32_t n) {
+    // bodies are contiguous; find the body by binary search on v0
+    size_t lo = 0, hi = h->bodies.size();
+    while (hi - lo > 1) {
+        size_t mid = (lo + hi) / 2;
+        if (h->bodies[mid].v0 <= n) lo = mid;
+        else hi = mid;
+    }
+    const BodyHost& b = h->bodies[lo];
+    return b.v0 + b.new_to_old[n - b.v0];
+}
+
+sbs_status sbs_gpu_get_contacts(sbs_gpu* h, uint32_t* verts, float* qn, uint32_t cap, uint32_t* n) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    uint32_t cnt[16];
+    CU(h, cudaMemcpyAsync(cnt, h->d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    const uint32_t* c = h->contacts_live ? cnt : cnt + kMaxPlanes + 1;
+    std::vector<std::pair<std::pair<uint32_t, uint32_t>, std::array<float, 6>>> all;
+    for (size_t pl = 0; pl < h->planes.size(); ++pl) {
+        std::vector<Contact> buf(c[pl]);
+        if (c[pl])
+            CU(h, cudaMemcpyAsync(buf.data(), h->d.contacts + pl * h->d.n_surf, c[pl] * sizeof(Contact),
+                                  cudaMemcpyDeviceToHost, h->st));
+        CU(h, cudaStreamSynchronize(h->st));
+        for (const Contact& k : buf) {
+            uint32_t vid;
+            std::memcpy(&vid, &k.q.w, 4);
+            all.push_back({{(uint32_t)pl, to_global(h, vid)}, {k.q.x, k.q.y, k.q.z, k.n.x, k.n.y, k.n.z}});
+        }
+    }
+    std::sort(all.begin(), all.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    if (n) *n = (uint32_t)all.size();
+    for (uint32_t i = 0; i < all.size() && i < cap; ++i) {
+        if (verts) verts[i] = all[i].first.second;
+        if (qn) std::copy(all[i].second.begin(), all[i].second.end(), qn + 6ull * i);
+    }
+    return check_err(h);
+}
+
+sbs_status sbs_gpu_get_masses(sbs_gpu* h, float* inv_mass) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!inv_mass) return fail(h, SBS_EINVAL, "null");
+    for (uint32_t n = 0; n < h->n_verts; ++n) inv_mass[to_global(h, n)] = h->inv_mass[n];
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_surface(sbs_gpu* h, uint32_t* verts, uint32_t cap, uint32_t* n) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    std::vector<uint32_t> g;
+    for (uint32_t v : h->surf) g.push_back(to_global(h, v));
+    std::sort(g.begin(), g.end());
+    if (n) *n = (uint32_t)g.size();
+    if (verts)
+        for (uint32_t i = 0; i < g.size() && i < cap; ++i) verts[i] = g[i];
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!st) return fail(h, SBS_EINVAL, "null");
+    std::memset(st, 0, sizeof(*st));
+    uint32_t cnt[16];
+    CU(h, cudaMemcpyAsync(cnt, h->d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    const uint32_t* c = h->contacts_live ? cnt : cnt + kMaxPlanes + 1;
+    st->frames = h->frames;
+    st->projections = h->projections;
+    st->n_vertices = h->n_verts;
+    st->n_tets = h->n_tets;
+    st->n_colours = h->n_colours;
+    st->n_tail_colours = h->n_colours - h->first_tail;
+    for (size_t pl = 0; pl < h->planes.size(); ++pl) st->n_contacts += c[pl];
+    st->n_body_contacts = c[kMaxPlanes];
+    st->exec_mode = h->exec_mode;
+    st->grid_ctas = h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_grid : h->grid;
+    st->block_size = h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_block : h->block;
+    st->residual = h->residual;
+    st->energy = h->energy;
+    st->last_frame_ms = h->last_frame_ms;
+    return check_err(h);
+}
+
+sbs_status sbs_gpu_destroy(sbs_gpu* h) {
+    if (!h) return SBS_EINVAL;
+    cudaSetDevice(h->prm.device);
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    for (void* p : h->allocations) cudaFree(p);
+    if (h->h_stage) cudaFreeHost(h->h_stage);
+    if (h->h_stage2) cudaFreeHost(h->h_stage2);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return SBS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+// Internal device-side layout of one scene and the kernel entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sbs {
+
+constexpr int kMaxColours = 128;  // colour masks are two 64-bit words per vertex
+constexpr int kMaxPlanes = 4;
+constexpr int kMaxKinGroups = 8;
+
+// A contact against a frozen plane (q, n), as collision_constraint_t holds
+// (src/physics/xpbd/collision_constraint.cpp:11-19): xyz of `q` is the contact
+// point, q.w the vertex id (bit pattern); xyz of `n` the unit normal.
+struct Contact {
+    float4 q;
+    float4 n;
+};
+
+// Device pointers of one scene.  Vertices are stored in the library's own
+// (Morton) order; tets colour-major.
+struct SceneDev {
+    // vertices
+    float4* xi;    // predicted / iterate position, w = inverse mass
+    float4* xn;    // position at substep start (x == xn between substeps), w = inverse mass
+    float4* v;     // velocity; w = 1 marks a kinematic vertex
+    float4* acc;   // external acceleration (nullable)
+    uint32_t n_verts;
+    // kinematic vertices
+    uint32_t* kin_vert;  // vertex id
+    float4* kin_rel;     // x0 - centre (xyz), group id (w, as float)
+    uint32_t n_kin;
+    // tets, colour-major
+    uint4* tet;
+    float4* dm0;   // DmInv row 0, w = signed V0
+    float4* dm1;   // DmInv row 1, w = mu
+    float4* dm2;   // DmInv row 2, w = Lame lambda
+    float* lam0;   // StVK multiplier / SNH deviatoric multiplier
+    float* lam1;   // SNH hydrostatic multiplier
+    uint32_t n_tets;
+    // surface and contacts
+    uint32_t* surf;
+    uint32_t n_surf;
+    Contact* contacts;     // kMaxPlanes segments of n_surf, then body contacts
+    float* contact_lam;
+    uint32_t* counters;    // [0..kMaxPlanes) ground contacts per plane, [kMaxPlanes] body contacts
+    uint32_t body_contact_cap;
+    // control
+    double* time;          // simulation time (s)
+    int* err;              // first error code seen on the device
+    unsigned* bar;         // grid barrier: [0] arrival count, [1] generation
+    // reductions
+    double* red_out;       // [4]: residual^2 (elastic), energy, residual^2 (contacts), spare
+    float* partials;       // per-CTA partial sums for the residual kernel
+};
+
+struct KinGroup {
+    float cx, cy, cz;
+    float ax, ay, az;
+    double omega;
+};
+
+struct Plane {
+    float nx, ny, nz, d;
+};
+
+// Per-launch constants (kernel parameter space).
+struct StepParams {
+    float dt, inv_dt, inv_dt2;
+    float stvk_alpha_tilde;      // alpha / dt^2
+    float stvk_gamma;            // (alpha/dt^2)(beta dt^2)/dt
+    int stvk_damping;            // 1 when beta != 0
+    float contact_alpha_tilde;   // collision alpha / dt^2
+    float gx, gy, gz;
+    int gravity_mode;
+    int n_colours;
+    int first_tail;              // colours [first_tail, n_colours) run in one CTA
+    int n_planes;
+    int n_kin_groups;
+    int substeps, iterations;
+    int body_contacts;
+    int has_acc;                 // 1 when an external acceleration field is set
+    double dt_d;
+    Plane planes[kMaxPlanes];
+    KinGroup kin[kMaxKinGroups];
+    uint32_t colour_start[kMaxColours + 1];
+    uint32_t colour_split[kMaxColours];  // first SNH tet of each colour
+};
+
+// Kernel launchers (xpbd_kernels.cu).  All enqueue on `st`.
+cudaError_t launch_detect_ground(const SceneDev& s, const StepParams& p, cudaStream_t st);
+cudaError_t launch_predict(const SceneDev& s, const StepParams& p, int substep, cudaStream_t st);
+cudaError_t launch_contacts(const SceneDev& s, const StepParams& p, int first_iter, cudaStream_t st);
+cudaError_t launch_colour(const SceneDev& s, const StepParams& p, int colour, int first_iter, int block,
+                          int grid, cudaStream_t st);
+cudaError_t launch_tail(const SceneDev& s, const StepParams& p, int first_iter, int block, cudaStream_t st);
+cudaError_t launch_finalize(const SceneDev& s, const StepParams& p, cudaStream_t st);
+cudaError_t launch_residual_ex(const SceneDev& s, const StepParams& p, int block, int grid, int cnt_base,
+                               cudaStream_t st);
+cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st);
+cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
+                                    cudaStream_t st);
+cudaError_t persistent_occupancy(int block, int* ctas_per_sm);
+cudaError_t launch_set_error(int* err, int code, cudaStream_t st);
+
+}  // namespace sbs

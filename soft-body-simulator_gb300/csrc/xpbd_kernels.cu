@@ -1,0 +1,553 @@
+// XPBD substep kernels for sm_103a.
+//
+// One frame = contact detection, then per substep: predict -> iterations x
+// (contact phase, elastic colour phases) -> velocity update.  This is the loop
+// of timestep_t::step (src/physics/timestep.cpp:20-70) with
+// gauss_seidel_solver_t::solve (src/physics/gauss_seidel_solver.cpp:8-37).
+// Gauss-Seidel order is kept exactly: tets of one colour share no vertex, so
+// running a colour in parallel equals running it in any sequential order, and
+// colours run one after the other.  No atomics touch positions or multipliers.
+//
+// Two drivers share the phase code:
+//  * per-phase kernels, recorded once into a CUDA graph per frame shape;
+//  * one cooperative persistent kernel per frame, phases separated by a grid
+//    barrier whose wait is bounded in time (SBS_ETIMEOUT on expiry).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "xpbd_internal.cuh"
+#include "xpbd_math.cuh"
+
+namespace sbs {
+
+constexpr int kErrTimeout = 3;  // SBS_ETIMEOUT
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier for a cooperative launch.  Thread 0 of each CTA arrives
+// on a counter; the last arrival resets it and bumps the generation; the
+// others wait for the generation to change for at most kBarrierLimitNs, then
+// record SBS_ETIMEOUT.  Returns false when the kernel must stop (timeout
+// here or an error recorded by another CTA).
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned gen = ld_acquire(bar + 1);
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            unsigned spins = 0;
+            while (ld_acquire(bar + 1) == gen) {
+                if ((++spins & 63u) == 0) {
+                    if (ld_relaxed(err) != 0) { ok = 0; break; }
+                    if (global_ns() - t0 > kBarrierLimitNs) {
+                        atomicCAS(err, 0, kErrTimeout);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+        }
+        __threadfence();
+        if (ok && ld_relaxed(err) != 0) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Work mapping for one phase: 32-item chunks dealt round-robin over CTAs
+// first, so a small colour spreads over many SMs; lanes of a warp take
+// consecutive items (coalesced SoA loads).
+template <typename Fn>
+__device__ __forceinline__ void for_each_spread(uint32_t begin, uint32_t end, Fn&& fn) {
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const uint32_t n = end - begin;
+    const uint32_t chunks = (n + 31u) >> 5;
+    for (uint32_t c = wib * gridDim.x + blockIdx.x; c < chunks; c += gridDim.x * wpb) {
+        const uint32_t i = (c << 5) + lane;
+        if (i < n) fn(begin + i);
+    }
+}
+
+template <typename Fn>
+__device__ __forceinline__ void for_each_vertex(uint32_t n, Fn&& fn) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) fn(i);
+}
+
+// ---------------------------------------------------------------------------
+// Phases
+
+// Prediction (timestep.cpp:35-43) for vertex i, fused with the prescribed
+// motion of kinematic vertices (v.w = 1 + group; rest offset in acc[i]).
+__device__ __forceinline__ void predict_vertex(const SceneDev& s, const StepParams& p, uint32_t i,
+                                               double t_next, int has_acc) {
+    float4 v = s.v[i];
+    const float4 x = s.xn[i];
+    if (v.w != 0.0f) {
+        const int g = (int)v.w - 1;
+        const KinGroup k = p.kin[g];
+        const float4 rel = s.acc[i];
+        float sn, cs;
+        sincosf((float)(k.omega * t_next), &sn, &cs);
+        const f3 a = mk(k.ax, k.ay, k.az), r = mk(rel.x, rel.y, rel.z);
+        const f3 rr = r * cs + cross(a, r) * sn + a * (dot(a, r) * (1.0f - cs));
+        s.xi[i] = make_float4(k.cx + rr.x, k.cy + rr.y, k.cz + rr.z, x.w);
+        return;
+    }
+    const float w = x.w;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    if (w > 0.0f) {
+        if (p.gravity_mode == 1) { ax = p.gx * w; ay = p.gy * w; az = p.gz * w; }
+        else { ax = p.gx; ay = p.gy; az = p.gz; }
+        if (has_acc) {
+            const float4 e = s.acc[i];
+            ax += e.x; ay += e.y; az += e.z;
+        }
+    }
+    v.x += ax * p.dt;
+    v.y += ay * p.dt;
+    v.z += az * p.dt;
+    s.v[i] = v;
+    s.xi[i] = make_float4(x.x + v.x * p.dt, x.y + v.y * p.dt, x.z + v.z * p.dt, w);
+}
+
+// Velocity update (timestep.cpp:48-57): x = xi; v = (x - xn)/dt; xn = x.
+__device__ __forceinline__ void finalize_vertex(const SceneDev& s, const StepParams& p, uint32_t i) {
+    const float4 a = s.xi[i];
+    const float4 b = s.xn[i];
+    float4 v = s.v[i];
+    v.x = (a.x - b.x) * p.inv_dt;
+    v.y = (a.y - b.y) * p.inv_dt;
+    v.z = (a.z - b.z) * p.inv_dt;
+    s.v[i] = v;
+    s.xn[i] = a;
+}
+
+// Ground contact detection for item k of (planes x surface vertices):
+// bvh_model.cpp:72-94 with the plane SDF of sdf_model.cpp:52-64.
+__device__ __forceinline__ void detect_item(const SceneDev& s, const StepParams& p, uint32_t k) {
+    const uint32_t plane = k / s.n_surf;
+    const uint32_t vi = s.surf[k - plane * s.n_surf];
+    const float4 x = s.xn[vi];
+    const Plane pl = p.planes[plane];
+    const float sd = pl.nx * x.x + pl.ny * x.y + pl.nz * x.z + pl.d;
+    const bool hit = sd < 0.0f;
+    const unsigned mask = __ballot_sync(__activemask(), hit);
+    if (!hit) return;
+    const unsigned lane = threadIdx.x & 31u;
+    const int leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if ((int)lane == leader) base = atomicAdd(&s.counters[plane], (unsigned)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    const unsigned rank = __popc(mask & ((1u << lane) - 1u));
+    if (base + rank >= s.n_surf) return;  // cannot happen with reset counters; never write past the segment
+    const float ad = fabsf(sd);
+    Contact c;
+    c.q = make_float4(x.x + pl.nx * ad, x.y + pl.ny * ad, x.z + pl.nz * ad, __uint_as_float(vi));
+    c.n = make_float4(pl.nx, pl.ny, pl.nz, 0.0f);
+    s.contacts[(size_t)plane * s.n_surf + base + rank] = c;
+}
+
+// collision_constraint_t::project_positions (collision_constraint.cpp:21-41).
+__device__ __forceinline__ void project_contact(const SceneDev& s, const StepParams& p, uint32_t ci,
+                                                bool first) {
+    const Contact c = s.contacts[ci];
+    const uint32_t vi = __float_as_uint(c.q.w);
+    float lam = first ? 0.0f : s.contact_lam[ci];
+    float4 x = __ldcg(&s.xi[vi]);
+    const float C = (x.x - c.q.x) * c.n.x + (x.y - c.q.y) * c.n.y + (x.z - c.q.z) * c.n.z;
+    if (C < 0.0f) {
+        const float w = x.w;
+        const float dl = -(C + p.contact_alpha_tilde * lam) / (w + p.contact_alpha_tilde);
+        lam += dl;
+        x.x += w * c.n.x * dl;
+        x.y += w * c.n.y * dl;
+        x.z += w * c.n.z * dl;
+        s.xi[vi] = x;
+    }
+    s.contact_lam[ci] = lam;
+}
+
+// One elastic tet constraint (StVK: green_constraint.cpp:49-158; SNH coupled).
+__device__ __forceinline__ void project_tet(const SceneDev& s, const StepParams& p, uint32_t t, bool snh,
+                                            bool first) {
+    const uint4 id = __ldg(&s.tet[t]);
+    const float4 a = __ldg(&s.dm0[t]);
+    const float4 b = __ldg(&s.dm1[t]);
+    const float4 c = __ldg(&s.dm2[t]);
+    float4 q0 = __ldcg(&s.xi[id.x]);
+    float4 q1 = __ldcg(&s.xi[id.y]);
+    float4 q2 = __ldcg(&s.xi[id.z]);
+    float4 q3 = __ldcg(&s.xi[id.w]);
+    const float w[4] = {q0.w, q1.w, q2.w, q3.w};
+    const f3 x0 = mk(q0), x1 = mk(q1), x2 = mk(q2), x3 = mk(q3);
+    const f3 r0 = mk(a), r1 = mk(b), r2 = mk(c);
+    f3 dx[4];
+    bool moved = false;
+    if (!snh) {
+        TetEval e;
+        stvk_eval(x0, x1, x2, x3, r0, r1, r2, a.w, b.w, c.w, e);
+        const float lacc = first ? 0.0f : s.lam0[t];
+        float gd = 0.0f;
+        if (p.stvk_damping) {
+            // sum_i f_i . (xi_i - xn_i) with f = -g
+            const float4 n0 = s.xn[id.x], n1 = s.xn[id.y], n2 = s.xn[id.z], n3 = s.xn[id.w];
+            gd = -(dot(e.g[0], x0 - mk(n0)) + dot(e.g[1], x1 - mk(n1)) + dot(e.g[2], x2 - mk(n2)) +
+                   dot(e.g[3], x3 - mk(n3)));
+        }
+        const float dl = stvk_dlambda(e, w, lacc, p.stvk_alpha_tilde, p.stvk_gamma, gd);
+        s.lam0[t] = lacc + dl;
+        if (dl != 0.0f) {
+            moved = true;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dx[i] = e.g[i] * (w[i] * dl);
+        }
+    } else {
+        float lD = first ? 0.0f : s.lam0[t];
+        float lH = first ? 0.0f : s.lam1[t];
+        float dlD, dlH;
+        if (snh_step(x0, x1, x2, x3, r0, r1, r2, fabsf(a.w), b.w, c.w, p.inv_dt2, w, lD, lH, dx, dlD,
+                     dlH)) {
+            lD += dlD;
+            lH += dlH;
+            moved = true;
+        }
+        s.lam0[t] = lD;
+        s.lam1[t] = lH;
+    }
+    if (moved) {
+        q0.x += dx[0].x; q0.y += dx[0].y; q0.z += dx[0].z;
+        q1.x += dx[1].x; q1.y += dx[1].y; q1.z += dx[1].z;
+        q2.x += dx[2].x; q2.y += dx[2].y; q2.z += dx[2].z;
+        q3.x += dx[3].x; q3.y += dx[3].y; q3.z += dx[3].z;
+        s.xi[id.x] = q0;
+        s.xi[id.y] = q1;
+        s.xi[id.z] = q2;
+        s.xi[id.w] = q3;
+    }
+}
+
+__device__ __forceinline__ void colour_phase(const SceneDev& s, const StepParams& p, int col, bool first) {
+    const uint32_t b = p.colour_start[col], e = p.colour_start[col + 1], m = p.colour_split[col];
+    for_each_spread(b, e, [&](uint32_t t) { project_tet(s, p, t, t >= m, first); });
+}
+
+// Tail colours in one CTA, separated by CTA barriers.
+__device__ __forceinline__ void tail_phase(const SceneDev& s, const StepParams& p, bool first) {
+    for (int col = p.first_tail; col < p.n_colours; ++col) {
+        const uint32_t b = p.colour_start[col], e = p.colour_start[col + 1], m = p.colour_split[col];
+        for (uint32_t t = b + threadIdx.x; t < e; t += blockDim.x) project_tet(s, p, t, t >= m, first);
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void contact_phase(const SceneDev& s, uint32_t seg, uint32_t count,
+                                              const StepParams& p, bool first) {
+    for_each_spread(seg, seg + count, [&](uint32_t ci) { project_contact(s, p, ci, first); });
+}
+
+// ---------------------------------------------------------------------------
+// Per-phase kernels (graph mode)
+
+__global__ void k_detect(SceneDev s, StepParams p) {
+    const uint32_t n = s.n_surf * (uint32_t)p.n_planes;
+    // whole warps stay converged for the ballot: iterate over warp-aligned ranges
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t k = base + (threadIdx.x & 31u);
+        if (k < n) detect_item(s, p, k);
+    }
+}
+
+__global__ void k_predict(SceneDev s, StepParams p, int substep, int has_acc) {
+    // simulation time before this substep: the finalize of the previous one
+    // added dt to *s.time (same double sequence as the CPU loop)
+    const double t_next = *s.time + p.dt_d;
+    for_each_vertex(s.n_verts, [&](uint32_t i) { predict_vertex(s, p, i, t_next, has_acc); });
+}
+
+__global__ void k_contacts(SceneDev s, StepParams p, int first) {
+    for (int pl = 0; pl < p.n_planes; ++pl) {
+        // planes are processed in order; a vertex may touch several planes
+        const uint32_t cnt = min(s.counters[pl], s.n_surf);
+        contact_phase(s, (uint32_t)pl * s.n_surf, cnt, p, first != 0);
+        if (p.n_planes > 1) __syncthreads();  // single-CTA launch when several planes
+    }
+}
+
+__global__ void k_colour(SceneDev s, StepParams p, int col, int first) { colour_phase(s, p, col, first != 0); }
+
+__global__ void k_tail(SceneDev s, StepParams p, int first) { tail_phase(s, p, first != 0); }
+
+__global__ void k_finalize(SceneDev s, StepParams p) {
+    for_each_vertex(s.n_verts, [&](uint32_t i) { finalize_vertex(s, p, i); });
+    if (blockIdx.x == 0 && threadIdx.x == 0) *s.time = *s.time + p.dt_d;
+}
+
+// End of frame: keep the frame's contact counts (for introspection) in
+// counters[kMaxPlanes+1 ..] and zero the live counters for the next frame.
+__global__ void k_end_frame(SceneDev s) {
+    const int i = threadIdx.x;
+    if (i <= kMaxPlanes) {
+        s.counters[kMaxPlanes + 1 + i] = s.counters[i];
+        s.counters[i] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent frame kernel
+
+__global__ void __launch_bounds__(512) k_frame(SceneDev s, StepParams p, int has_acc) {
+    if (ld_relaxed(s.err) != 0) return;
+    double t = *s.time;
+    // contacts from frame-start positions
+    {
+        const uint32_t n = s.n_surf * (uint32_t)p.n_planes;
+        const uint32_t stride = gridDim.x * blockDim.x;
+        for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+            const uint32_t k = base + (threadIdx.x & 31u);
+            if (k < n) detect_item(s, p, k);
+        }
+    }
+    if (!grid_barrier(s.bar, s.err)) return;
+    uint32_t cnt[kMaxPlanes];
+    for (int pl = 0; pl < kMaxPlanes; ++pl) cnt[pl] = pl < p.n_planes ? min(__ldcg(&s.counters[pl]), s.n_surf) : 0u;
+    for (int sub = 0; sub < p.substeps; ++sub) {
+        const double t_next = t + p.dt_d;
+        for_each_vertex(s.n_verts, [&](uint32_t i) { predict_vertex(s, p, i, t_next, has_acc); });
+        if (!grid_barrier(s.bar, s.err)) return;
+        for (int it = 0; it < p.iterations; ++it) {
+            const bool first = it == 0;
+            for (int pl = 0; pl < p.n_planes; ++pl) {
+                if (cnt[pl] == 0) continue;
+                contact_phase(s, (uint32_t)pl * s.n_surf, cnt[pl], p, first);
+                if (!grid_barrier(s.bar, s.err)) return;
+            }
+            for (int col = 0; col < p.first_tail; ++col) {
+                colour_phase(s, p, col, first);
+                if (!grid_barrier(s.bar, s.err)) return;
+            }
+            if (p.first_tail < p.n_colours) {
+                if (blockIdx.x == 0) tail_phase(s, p, first);
+                if (!grid_barrier(s.bar, s.err)) return;
+            }
+        }
+        for_each_vertex(s.n_verts, [&](uint32_t i) { finalize_vertex(s, p, i); });
+        t = t_next;
+    }
+    if (!grid_barrier(s.bar, s.err)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *s.time = t;
+        for (int i = 0; i <= kMaxPlanes; ++i) {
+            s.counters[kMaxPlanes + 1 + i] = s.counters[i];
+            s.counters[i] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Residual and energy with compensated FP32 sums (Neumaier's variant of
+// Kahan summation; pairs combined with Knuth's two-sum).
+
+struct CSum {
+    float s, e;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        if (fabsf(s) >= fabsf(x)) e += (s - t) + x;
+        else e += (x - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ void merge(const CSum& o) {
+        add(o.s);
+        e += o.e;
+    }
+};
+
+__device__ __forceinline__ CSum block_reduce(CSum v, float* sh) {
+    // sh: 2 * blockDim.x floats
+    sh[threadIdx.x] = v.s;
+    sh[blockDim.x + threadIdx.x] = v.e;
+    __syncthreads();
+    for (unsigned off = blockDim.x >> 1; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            CSum a{sh[threadIdx.x], sh[blockDim.x + threadIdx.x]};
+            a.merge(CSum{sh[threadIdx.x + off], sh[blockDim.x + threadIdx.x + off]});
+            sh[threadIdx.x] = a.s;
+            sh[blockDim.x + threadIdx.x] = a.e;
+        }
+        __syncthreads();
+    }
+    CSum r{sh[0], sh[blockDim.x]};
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
+    extern __shared__ float sh[];
+    CSum re{0.f, 0.f}, en{0.f, 0.f}, rc{0.f, 0.f};
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < s.n_tets; t += stride) {
+        const uint4 id = s.tet[t];
+        const float4 a = s.dm0[t], b = s.dm1[t], c = s.dm2[t];
+        const f3 x0 = mk(s.xi[id.x]), x1 = mk(s.xi[id.y]), x2 = mk(s.xi[id.z]), x3 = mk(s.xi[id.w]);
+        // tets at or past the split of their colour are SNH; find the colour by scan
+        int col = 0;
+        while (col + 1 < p.n_colours && t >= p.colour_start[col + 1]) ++col;
+        const bool snh = t >= p.colour_split[col];
+        if (!snh) {
+            TetEval e;
+            stvk_eval(x0, x1, x2, x3, mk(a), mk(b), mk(c), a.w, b.w, c.w, e);
+            const float h = e.C + p.stvk_alpha_tilde * s.lam0[t];
+            re.add(h * h);
+            en.add(e.C);
+        } else {
+            float r2, E;
+            snh_residual(x0, x1, x2, x3, mk(a), mk(b), mk(c), fabsf(a.w), b.w, c.w, p.inv_dt2, s.lam0[t],
+                         s.lam1[t], r2, E);
+            re.add(r2);
+            en.add(E);
+        }
+    }
+    for (int pl = 0; pl < p.n_planes; ++pl) {
+        const uint32_t cnt = min(s.counters[cnt_base + pl], s.n_surf);
+        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += stride) {
+            const uint32_t ci = (uint32_t)pl * s.n_surf + k;
+            const Contact c = s.contacts[ci];
+            const float4 x = s.xi[__float_as_uint(c.q.w)];
+            const float C = (x.x - c.q.x) * c.n.x + (x.y - c.q.y) * c.n.y + (x.z - c.q.z) * c.n.z;
+            if (C < 0.0f) {
+                const float h = C + p.contact_alpha_tilde * s.contact_lam[ci];
+                rc.add(h * h);
+            }
+        }
+    }
+    re = block_reduce(re, sh);
+    en = block_reduce(en, sh);
+    rc = block_reduce(rc, sh);
+    if (threadIdx.x == 0) {
+        float* o = s.partials + 6 * blockIdx.x;
+        o[0] = re.s; o[1] = re.e; o[2] = en.s; o[3] = en.e; o[4] = rc.s; o[5] = rc.e;
+    }
+}
+
+__global__ void k_residual_final(SceneDev s, int nparts) {
+    extern __shared__ float sh[];
+    CSum acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+        for (int k = 0; k < 3; ++k) acc[k].merge(CSum{s.partials[6 * i + 2 * k], s.partials[6 * i + 2 * k + 1]});
+    for (int k = 0; k < 3; ++k) {
+        CSum r = block_reduce(acc[k], sh);
+        if (threadIdx.x == 0) s.red_out[k] = (double)r.s + (double)r.e;
+    }
+}
+
+__global__ void k_set_error(int* err, int code) { atomicCAS(err, 0, code); }
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+static inline int grid_for(uint32_t n, int block, int cap) {
+    long g = ((long)n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+
+cudaError_t launch_detect_ground(const SceneDev& s, const StepParams& p, cudaStream_t st) {
+    const uint32_t n = s.n_surf * (uint32_t)p.n_planes;
+    if (n == 0) return cudaSuccess;
+    k_detect<<<grid_for(n, 256, 4096), 256, 0, st>>>(s, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_predict(const SceneDev& s, const StepParams& p, int substep, cudaStream_t st) {
+    (void)substep;
+    k_predict<<<grid_for(s.n_verts, 256, 8192), 256, 0, st>>>(s, p, substep, p.has_acc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_contacts(const SceneDev& s, const StepParams& p, int first_iter, cudaStream_t st) {
+    if (p.n_planes == 0 || s.n_surf == 0) return cudaSuccess;
+    const int grid = p.n_planes > 1 ? 1 : grid_for(s.n_surf, 256, 1024);
+    k_contacts<<<grid, 256, 0, st>>>(s, p, first_iter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_colour(const SceneDev& s, const StepParams& p, int colour, int first_iter, int block,
+                          int grid, cudaStream_t st) {
+    k_colour<<<grid, block, 0, st>>>(s, p, colour, first_iter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tail(const SceneDev& s, const StepParams& p, int first_iter, int block, cudaStream_t st) {
+    if (p.first_tail >= p.n_colours) return cudaSuccess;
+    k_tail<<<1, block, 0, st>>>(s, p, first_iter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const SceneDev& s, const StepParams& p, cudaStream_t st) {
+    k_finalize<<<grid_for(s.n_verts, 256, 8192), 256, 0, st>>>(s, p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st) {
+    k_end_frame<<<1, 32, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_residual_ex(const SceneDev& s, const StepParams& p, int block, int grid, int cnt_base,
+                               cudaStream_t st) {
+    const size_t shm = 2 * sizeof(float) * (size_t)block;
+    k_residual<<<grid, block, shm, st>>>(s, p, cnt_base);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_residual_final<<<1, 256, 2 * sizeof(float) * 256, st>>>(s, grid);
+    return cudaGetLastError();
+}
+
+cudaError_t persistent_occupancy(int block, int* ctas_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame, block, 0);
+}
+
+cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
+                                    cudaStream_t st) {
+    int has_acc = p.has_acc;
+    SceneDev sc = s;
+    StepParams pc = p;
+    void* args[] = {&sc, &pc, &has_acc};
+    return cudaLaunchCooperativeKernel((const void*)k_frame, dim3(grid), dim3(block), args, 0, st);
+}
+
+cudaError_t launch_set_error(int* err, int code, cudaStream_t st) {
+    k_set_error<<<1, 1, 0, st>>>(err, code);
+    return cudaGetLastError();
+}
+
+}  // namespace sbs

@@ -1,0 +1,316 @@
+"""ctypes binding of libsbs_gpu.so (declarations: include/sbs_gpu.h).
+
+Raises ``SbsError`` on any non-OK status.  There is no CPU fallback: if the
+library or a GPU is missing, loading or creating a solver fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+SBS_OK, SBS_EINVAL, SBS_ECUDA, SBS_ETIMEOUT, SBS_ENAN, SBS_ESTATE, SBS_ENOMEM, SBS_ECOLOUR = range(8)
+EXEC_AUTO, EXEC_GRAPH, EXEC_PERSISTENT = 0, 1, 2
+GRAVITY_ACCELERATION, GRAVITY_FORCE = 0, 1
+
+HEADER = _build.INCLUDE / "sbs_gpu.h"
+
+
+class SbsError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"sbs status {status}: {msg}")
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [("compliance", C.c_double), ("damping", C.c_double),
+                ("collision_compliance", C.c_double), ("gravity", C.c_double * 3),
+                ("gravity_mode", C.c_int32), ("device", C.c_int32), ("exec_mode", C.c_int32),
+                ("block_size", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("tail_threshold", C.c_int32), ("body_contacts", C.c_int32),
+                ("hash_cell", C.c_float), ("max_body_contacts", C.c_uint32),
+                ("check_finite", C.c_int32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("model", C.c_int32), ("young", C.c_double), ("poisson", C.c_double),
+                ("density", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("projections", C.c_uint64),
+                ("n_vertices", C.c_uint32), ("n_tets", C.c_uint32), ("n_colours", C.c_uint32),
+                ("n_tail_colours", C.c_uint32), ("n_contacts", C.c_uint32),
+                ("n_body_contacts", C.c_uint32), ("body_contact_overflow", C.c_uint32),
+                ("exec_mode", C.c_int32), ("grid_ctas", C.c_int32), ("block_size", C.c_int32),
+                ("residual", C.c_double), ("energy", C.c_double), ("last_frame_ms", C.c_double)]
+
+
+_lib = None
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/sbs_gpu.h."""
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(sbs_gpu_[a-z_0-9]+)\s*\(", text)))
+
+
+def load(build: bool = True):
+    """Loads (building first if stale) the CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    L = C.CDLL(str(path))
+    P = C.c_void_p
+    f32 = np.ctypeslib.ndpointer(np.float32, flags="C")
+    f64 = np.ctypeslib.ndpointer(np.float64, flags="C")
+    u32 = np.ctypeslib.ndpointer(np.uint32, flags="C")
+    sig = {
+        "sbs_gpu_params_default": [C.POINTER(Params)],
+        "sbs_gpu_create": [C.POINTER(Params), C.POINTER(P)],
+        "sbs_gpu_add_body": [P, f64, C.c_void_p, C.c_uint32, u32, C.c_uint32, C.POINTER(Material),
+                             C.c_void_p, C.POINTER(C.c_int32)],
+        "sbs_gpu_pin_vertices": [P, C.c_int32, u32, C.c_uint32],
+        "sbs_gpu_add_kinematic_rotation": [P, C.c_int32, u32, C.c_uint32, f64, f64, C.c_double],
+        "sbs_gpu_set_external_acceleration": [P, C.c_int32, f32],
+        "sbs_gpu_add_ground_plane": [P, f64, C.c_double],
+        "sbs_gpu_finalize": [P],
+        "sbs_gpu_step": [P, C.c_double, C.c_uint32, C.c_uint32],
+        "sbs_gpu_step_timed": [P, C.c_double, C.c_uint32, C.c_uint32],
+        "sbs_gpu_solve": [P, C.c_double, C.c_uint32],
+        "sbs_gpu_predict": [P, C.c_double],
+        "sbs_gpu_update_velocities": [P, C.c_double],
+        "sbs_gpu_detect_contacts": [P],
+        "sbs_gpu_residual": [P, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+        "sbs_gpu_set_state": [P, C.c_int32, C.c_void_p, C.c_void_p],
+        "sbs_gpu_get_state": [P, C.c_int32, C.c_void_p, C.c_void_p],
+        "sbs_gpu_get_predicted": [P, C.c_int32, f32],
+        "sbs_gpu_set_predicted": [P, C.c_int32, f32],
+        "sbs_gpu_get_tet_order": [P, C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_get_lambdas": [P, f32],
+        "sbs_gpu_get_contacts": [P, C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_get_masses": [P, f32],
+        "sbs_gpu_get_surface": [P, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_get_stats": [P, C.POINTER(Stats)],
+        "sbs_gpu_destroy": [P],
+        "sbs_gpu_plan_sweep": [f64, C.c_uint32, u32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_uint32, C.POINTER(C.c_uint32)],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    L.sbs_gpu_status_string.argtypes = [C.c_int]
+    L.sbs_gpu_status_string.restype = C.c_char_p
+    L.sbs_gpu_last_error.argtypes = [P]
+    L.sbs_gpu_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def default_params(**kw) -> Params:
+    L = load()
+    p = Params()
+    L.sbs_gpu_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k == "gravity":
+            p.gravity = (C.c_double * 3)(*v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def plan_sweep(scene):
+    """Sweep order of a scene computed by the library's host code (no GPU):
+    (order, offsets) with bodies concatenated in add order."""
+    L = load()
+    x0 = np.ascontiguousarray(np.concatenate([b.x0 for b in scene.bodies]), np.float64).ravel()
+    tets, models, off = [], [], 0
+    for b in scene.bodies:
+        tets.append(b.tets.astype(np.uint32) + off)
+        models.append(np.full(len(b.tets), b.model, np.int32))
+        off += len(b.x0)
+    tets = np.ascontiguousarray(np.concatenate(tets), np.uint32).ravel()
+    models = np.ascontiguousarray(np.concatenate(models), np.int32)
+    n = C.c_uint32()
+    T = len(models)
+    order = np.zeros(T, np.uint32)
+    offsets = np.zeros(129, np.uint32)
+    st = L.sbs_gpu_plan_sweep(x0, len(x0) // 3, tets, T, models.ctypes.data, order.ctypes.data,
+                              offsets.ctypes.data, len(offsets), C.byref(n))
+    if st != SBS_OK:
+        raise SbsError(st, L.sbs_gpu_last_error(None).decode())
+    return order, offsets[: n.value + 1].copy()
+
+
+class Solver:
+    """One GPU scene (an ``sbs_gpu`` handle) built from a scenes.Scene."""
+
+    def __init__(self, scene, **param_overrides):
+        L = load()
+        self.L = L
+        self.scene = scene
+        kw = dict(compliance=scene.compliance, damping=scene.damping,
+                  collision_compliance=scene.collision_compliance, gravity=scene.gravity,
+                  gravity_mode=scene.gravity_mode)
+        kw.update(param_overrides)
+        prm = default_params(**kw)
+        h = C.c_void_p()
+        self._check(L.sbs_gpu_create(C.byref(prm), C.byref(h)), None)
+        self.h = h
+        self.body_sizes = []
+        for b in scene.bodies:
+            x0 = np.ascontiguousarray(b.x0, np.float64).ravel()
+            xi = None if b.x_init is None else np.ascontiguousarray(b.x_init, np.float64).ravel()
+            tets = np.ascontiguousarray(b.tets, np.uint32).ravel()
+            mat = Material(b.model, b.young, b.poisson, b.density)
+            bid = C.c_int32()
+            self._check(L.sbs_gpu_add_body(h, x0, _ptr(xi), len(b.x0), tets, len(b.tets),
+                                           C.byref(mat), None, C.byref(bid)))
+            if len(b.pinned):
+                self._check(L.sbs_gpu_pin_vertices(h, bid, np.ascontiguousarray(b.pinned, np.uint32),
+                                                   len(b.pinned)))
+            if len(b.kin_verts):
+                self._check(L.sbs_gpu_add_kinematic_rotation(
+                    h, bid, np.ascontiguousarray(b.kin_verts, np.uint32), len(b.kin_verts),
+                    np.asarray(b.kin_center, np.float64), np.asarray(b.kin_axis, np.float64),
+                    b.kin_omega))
+            if b.ext_acc is not None:
+                self._check(L.sbs_gpu_set_external_acceleration(
+                    h, bid, np.ascontiguousarray(b.ext_acc, np.float32).ravel()))
+            self.body_sizes.append(len(b.x0))
+        if scene.ground is not None:
+            n, d = scene.ground
+            self._check(L.sbs_gpu_add_ground_plane(h, np.asarray(n, np.float64), d))
+        self._check(L.sbs_gpu_finalize(h))
+        if any(b.v_init is not None for b in scene.bodies):
+            for i, b in enumerate(scene.bodies):
+                if b.v_init is not None:
+                    self.set_state(i, None, b.v_init)
+
+    def _check(self, status, h="self"):
+        if status != SBS_OK:
+            L = self.L
+            handle = self.h if h == "self" and getattr(self, "h", None) else None
+            msg = L.sbs_gpu_last_error(handle).decode()
+            raise SbsError(status, f"{L.sbs_gpu_status_string(status).decode()}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sbs_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- stepping -----------------------------------------------------------
+    def step(self, frames: int = 1, frame_dt=None, substeps=None, iterations=None):
+        s = self.scene
+        fdt = s.frame_dt if frame_dt is None else frame_dt
+        sub = s.substeps if substeps is None else substeps
+        its = s.iterations if iterations is None else iterations
+        for _ in range(frames):
+            self._check(self.L.sbs_gpu_step(self.h, fdt, sub, its))
+
+    def step_timed(self) -> float:
+        s = self.scene
+        self._check(self.L.sbs_gpu_step_timed(self.h, s.frame_dt, s.substeps, s.iterations))
+        return self.stats().last_frame_ms
+
+    def solve(self, dt: float, iterations: int):
+        self._check(self.L.sbs_gpu_solve(self.h, dt, iterations))
+
+    def predict(self, dt: float):
+        self._check(self.L.sbs_gpu_predict(self.h, dt))
+
+    def update_velocities(self, dt: float):
+        self._check(self.L.sbs_gpu_update_velocities(self.h, dt))
+
+    def detect_contacts(self):
+        self._check(self.L.sbs_gpu_detect_contacts(self.h))
+
+    def residual(self, dt: float):
+        r, e = C.c_double(), C.c_double()
+        self._check(self.L.sbs_gpu_residual(self.h, dt, C.byref(r), C.byref(e)))
+        return r.value, e.value
+
+    # -- state --------------------------------------------------------------
+    def get_state(self, body: int = 0):
+        n = self.body_sizes[body]
+        x = np.zeros(3 * n, np.float32)
+        v = np.zeros(3 * n, np.float32)
+        self._check(self.L.sbs_gpu_get_state(self.h, body, x.ctypes.data, v.ctypes.data))
+        return x.reshape(-1, 3), v.reshape(-1, 3)
+
+    def positions(self) -> np.ndarray:
+        return np.concatenate([self.get_state(b)[0] for b in range(len(self.body_sizes))])
+
+    def velocities(self) -> np.ndarray:
+        return np.concatenate([self.get_state(b)[1] for b in range(len(self.body_sizes))])
+
+    def set_state(self, body: int, x=None, v=None):
+        xa = None if x is None else np.ascontiguousarray(x, np.float32).ravel()
+        va = None if v is None else np.ascontiguousarray(v, np.float32).ravel()
+        self._check(self.L.sbs_gpu_set_state(self.h, body, _ptr(xa), _ptr(va)))
+
+    def get_predicted(self, body: int = 0) -> np.ndarray:
+        x = np.zeros(3 * self.body_sizes[body], np.float32)
+        self._check(self.L.sbs_gpu_get_predicted(self.h, body, x))
+        return x.reshape(-1, 3)
+
+    def set_predicted(self, body: int, xi):
+        self._check(self.L.sbs_gpu_set_predicted(self.h, body,
+                                                 np.ascontiguousarray(xi, np.float32).ravel()))
+
+    # -- introspection ------------------------------------------------------
+    def tet_order(self):
+        n = C.c_uint32()
+        self._check(self.L.sbs_gpu_get_tet_order(self.h, None, None, 0, C.byref(n)))
+        order = np.zeros(self.scene.n_tets, np.uint32)
+        off = np.zeros(n.value + 1, np.uint32)
+        self._check(self.L.sbs_gpu_get_tet_order(self.h, order.ctypes.data, off.ctypes.data,
+                                                 len(off), C.byref(n)))
+        return order, off
+
+    def lambdas(self) -> np.ndarray:
+        out = np.zeros(2 * self.scene.n_tets, np.float32)
+        self._check(self.L.sbs_gpu_get_lambdas(self.h, out))
+        return out.reshape(-1, 2)
+
+    def contacts(self):
+        n = C.c_uint32()
+        self._check(self.L.sbs_gpu_get_contacts(self.h, None, None, 0, C.byref(n)))
+        v = np.zeros(n.value, np.uint32)
+        qn = np.zeros(6 * n.value, np.float32)
+        self._check(self.L.sbs_gpu_get_contacts(self.h, v.ctypes.data, qn.ctypes.data, n.value,
+                                                C.byref(n)))
+        return v, qn.reshape(-1, 6)
+
+    def inv_masses(self) -> np.ndarray:
+        out = np.zeros(self.scene.n_verts, np.float32)
+        self._check(self.L.sbs_gpu_get_masses(self.h, out))
+        return out
+
+    def surface(self) -> np.ndarray:
+        n = C.c_uint32()
+        self._check(self.L.sbs_gpu_get_surface(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.uint32)
+        self._check(self.L.sbs_gpu_get_surface(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
+    def stats(self) -> Stats:
+        st = Stats()
+        self._check(self.L.sbs_gpu_get_stats(self.h, C.byref(st)))
+        return st
