@@ -49,9 +49,11 @@ typedef enum sbs_gravity_mode {
 } sbs_gravity_mode;
 
 typedef enum sbs_exec_mode {
-    SBS_EXEC_AUTO = 0,       /* pick with the built-in autotuner at finalize */
+    SBS_EXEC_AUTO = 0,       /* pick with the built-in autotuner on the first step */
     SBS_EXEC_GRAPH = 1,      /* one kernel per phase, replayed as a CUDA graph */
-    SBS_EXEC_PERSISTENT = 2  /* one cooperative kernel per frame, grid barriers */
+    SBS_EXEC_PERSISTENT = 2, /* one cooperative kernel per frame, grid barriers */
+    SBS_EXEC_CLUSTER = 3     /* groups of bodies resident in the shared memory of a
+                                thread-block cluster, cluster barriers between phases */
 } sbs_exec_mode;
 
 /* Solver parameters.  Defaults (sbs_gpu_params_default) follow
@@ -67,9 +69,11 @@ typedef struct sbs_gpu_params {
     int32_t block_size;           /* threads per CTA of the projection kernels (0: auto) */
     int32_t ctas_per_sm;          /* persistent mode CTAs per SM (0: auto) */
     int32_t tail_threshold;       /* colours with <= this many tets run in one CTA (-1: auto) */
-    int32_t body_contacts;        /* 1: body-body vertex-in-tet contacts (spatial hash) */
-    float hash_cell;              /* spatial hash cell size (0: 2 x mean edge length) */
-    uint32_t max_body_contacts;   /* capacity of the body-contact list (0: auto) */
+    int32_t body_contacts;        /* 0 off; 1 vertex-in-tet contacts between bodies (spatial
+                                     hash); 2 also within a body (self contacts) */
+    float hash_cell;              /* spatial hash cell size in metres (0: 2 x mean edge length) */
+    uint32_t candidate_capacity;  /* >0: record up to this many broad-phase candidate pairs
+                                     per detection for sbs_gpu_get_candidates */
     int32_t check_finite;         /* 1: sbs_gpu_get_* report SBS_ENAN on non-finite x */
 } sbs_gpu_params;
 
@@ -188,6 +192,12 @@ sbs_status sbs_gpu_get_tet_order(sbs_gpu* h, uint32_t* order, uint32_t* offsets,
 sbs_status sbs_gpu_get_lambdas(sbs_gpu* h, float* lambdas);
 sbs_status sbs_gpu_get_contacts(sbs_gpu* h, uint32_t* verts, float* qn, uint32_t cap, uint32_t* n);
 sbs_status sbs_gpu_get_masses(sbs_gpu* h, float* inv_mass);
+/* Broad-phase candidate pairs of the last contact detection (needs
+ * params.candidate_capacity > 0), as (global vertex id << 32 | global tet id),
+ * sorted ascending; *n receives the total count (may exceed cap).  No
+ * reference counterpart: the reference's CD has no body-body pairs
+ * (contact_handler.cpp:17 handles SDF contacts only). */
+sbs_status sbs_gpu_get_candidates(sbs_gpu* h, uint64_t* pairs, uint64_t cap, uint64_t* n);
 sbs_status sbs_gpu_get_surface(sbs_gpu* h, uint32_t* verts, uint32_t cap, uint32_t* n);
 sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st);
 

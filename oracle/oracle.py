@@ -78,6 +78,12 @@ def lib():
         L.orc_n_contacts.restype = U32
         L.orc_n_contacts.argtypes = [P]
         L.orc_stats.argtypes = [P, dp]
+        L.orc_set_body_contacts.argtypes = [P, I, D]
+        L.orc_hash_candidates.restype = C.c_uint64
+        L.orc_hash_candidates.argtypes = [P, np.ctypeslib.ndpointer(np.float32, flags="C"), D, I,
+                                          C.c_void_p, C.c_uint64]
+        L.orc_n_body_contacts.restype = U32
+        L.orc_n_body_contacts.argtypes = [P]
         L.orc_time_frames.restype = D
         L.orc_time_frames.argtypes = [P, D, U32, U32, U32]
         _lib = L
@@ -106,10 +112,14 @@ class Oracle:
             xi = None if b.x_init is None else \
                 np.ascontiguousarray(b.x_init, np.float64).ravel()
             tets = np.ascontiguousarray(b.tets, np.uint32).ravel()
+            mass = None if getattr(b, "mass", None) is None else \
+                np.ascontiguousarray(b.mass, np.float64)
+            self._mass_keep = mass
             bid = L.orc_add_body(self.h, x0,
                                  None if xi is None else xi.ctypes.data,
                                  len(b.x0), tets, len(b.tets), b.model,
-                                 b.young, b.poisson, b.density, None)
+                                 b.young, b.poisson, b.density,
+                                 None if mass is None else mass.ctypes.data)
             if len(b.pinned):
                 L.orc_pin(self.h, bid, np.ascontiguousarray(b.pinned, np.uint32),
                           len(b.pinned))
@@ -127,6 +137,10 @@ class Oracle:
         if scene.ground is not None:
             n, d = scene.ground
             L.orc_add_ground_plane(self.h, np.asarray(n, np.float64), d)
+        if getattr(scene, "body_contacts", 0):
+            cell = scene.hash_cell if scene.hash_cell > 0 else mean_edge_cell(scene)
+            self.hash_cell = cell
+            L.orc_set_body_contacts(self.h, int(scene.body_contacts), cell)
         if scene.bodies and scene.bodies[0].v_init is not None:
             v = np.concatenate([b.v_init if b.v_init is not None else np.zeros_like(b.x0)
                                 for b in scene.bodies])
@@ -198,6 +212,56 @@ class Oracle:
     def time_frames(self, n: int) -> float:
         s = self.scene
         return self.L.orc_time_frames(self.h, s.frame_dt, s.substeps, s.iterations, n)
+
+
+def mean_edge_cell(scene) -> float:
+    """2 x the mean edge length of the rest meshes (the default hash cell)."""
+    tot, cnt = 0.0, 0
+    for b in scene.bodies:
+        t = b.tets.astype(np.int64)
+        for a, c in ((0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3)):
+            tot += np.linalg.norm(b.x0[t[:, a]] - b.x0[t[:, c]], axis=1).sum()
+            cnt += len(t)
+    return 2.0 * tot / cnt
+
+
+def hash_candidates(o: "Oracle", xf: np.ndarray, cell: float, self_contacts: bool = False):
+    """Broad-phase candidate pairs (vertex << 32 | tet) of the CPU hash for
+    float32 positions xf [V,3] (add order), sorted."""
+    xf = np.ascontiguousarray(xf, np.float32).ravel()
+    n = o.L.orc_hash_candidates(o.h, xf, cell, int(self_contacts), None, 0)
+    out = np.zeros(n, np.uint64)
+    o.L.orc_hash_candidates(o.h, xf, cell, int(self_contacts), out.ctypes.data, n)
+    return out
+
+
+def noise_floor(scene, frames: int, order=None, offsets=None, seed: int = 0) -> float:
+    """Max position deviation after `frames` between the oracle and the
+    oracle restarted from FP32-rounded initial positions nudged by one ulp.
+    It measures how far rounding at FP32 level alone carries the sequential
+    loop, the yardstick for multi-frame FP32-vs-FP64 comparisons."""
+    a = Oracle(scene)
+    b = Oracle(scene)
+    if order is not None:
+        a.set_order(order, offsets)
+        b.set_order(order, offsets)
+    x = b.get()
+    rng = np.random.default_rng(seed)
+    x32 = x.astype(np.float32)
+    toward = np.where(rng.random(x.shape) < 0.5, -np.inf, np.inf).astype(np.float32)
+    b.set(FIELD_X, np.nextafter(x32, toward).astype(np.float64))
+    a.step(frames)
+    b.step(frames)
+    return float(np.abs(a.get() - b.get()).max())
+
+
+def sync_state(src: "Oracle", dst_oracle: "Oracle | None" = None):
+    """FP32-rounded positions and velocities of `src` (also written back)."""
+    x = src.get().astype(np.float32).astype(np.float64)
+    v = src.get(FIELD_V).astype(np.float32).astype(np.float64)
+    src.set(FIELD_X, x)
+    src.set(FIELD_V, v)
+    return x, v
 
 
 def svd3(F: np.ndarray):

@@ -222,7 +222,14 @@ struct params_t {
     vec3 gravity{0.0, -9.81, 0.0};
     int gravity_mode = 0;   // 0 acceleration (m g as force), 1 force as in timestep.cpp:39
     double hash_cell = 0.0;
-    int body_contacts = 0;
+    int body_contacts = 0;  // 1: vertex-in-tet contacts between bodies, 2: also within a body
+};
+
+// Per-tet topology for the spatial hash (global vertex ids, add order).
+struct tet_topo_t {
+    uint32_t v[4];
+    uint32_t body;
+    uint8_t bmask;   // bit f: face f of faces_copy (topology.cpp:335-342) is on the boundary
 };
 
 struct stats_t {
@@ -242,6 +249,10 @@ struct sim_t {
     std::vector<uint32_t> ground_end;                                  // ground contacts per plane
     std::vector<kinematic_t> kinematics;
     std::vector<plane_t> planes;
+    std::vector<tet_topo_t> topo;          // global tet order
+    std::vector<uint32_t> vbody;           // per particle
+    std::vector<uint8_t> vsurf;            // per particle: surface vertex
+    std::vector<uint32_t> slot_of_tet;     // sweep slot of each tet (tie-breaks)
     double time = 0.0;
     int threads = 1;
     stats_t st;
@@ -472,6 +483,132 @@ static void detect_ground(sim_t& sim) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Body-body contacts (not in the reference; its CD only meets SDFs,
+// contact_handler.cpp:17).  Spatial hash: the cell of a point is
+// floor(x * inv_h) per axis with x and inv_h = 1/h rounded to float and the
+// product rounded to float, so CPU and GPU compute identical cells.
+// Surface vertices fill the cells; every tet with at least one boundary face
+// visits the cells of its AABB.  A candidate is a (surface vertex, tet) pair
+// with the vertex's cell inside the tet's cell range, the vertex not a vertex
+// of the tet, and the two from different bodies (or, with self contacts, from
+// any body).  Narrow phase: the vertex lies inside the tet (barycentric
+// coordinates >= 0); the contact is the half-space of the tet's boundary face
+// with the largest signed distance d <= 0 (the shallowest exit), frozen for
+// the frame like the reference's collision constraint: q = x - d n, outward n.
+// One contact per vertex: the largest d, ties to the lower sweep slot.
+
+static inline int32_t hash_cell_coord(float x, float inv_h) { return (int32_t)std::floor(x * inv_h); }
+
+static inline uint64_t hash_key(int32_t cx, int32_t cy, int32_t cz) {
+    const uint64_t m = (1ull << 21) - 1;
+    return (((uint64_t)(uint32_t)(cx + (1 << 20)) & m) << 42) | (((uint64_t)(uint32_t)(cy + (1 << 20)) & m) << 21) |
+           ((uint64_t)(uint32_t)(cz + (1 << 20)) & m);
+}
+
+// Candidate (vertex, tet) pairs for float positions xf [3 * n_particles].
+static void hash_candidates(const sim_t& s, const float* xf, float inv_h, int self,
+                            std::vector<std::pair<uint32_t, uint32_t>>& out) {
+    std::unordered_map<uint64_t, std::vector<uint32_t>> cells;
+    const uint32_t n = (uint32_t)s.particles.size();
+    for (uint32_t v = 0; v < n; ++v) {
+        if (!s.vsurf[v]) continue;
+        cells[hash_key(hash_cell_coord(xf[3 * v], inv_h), hash_cell_coord(xf[3 * v + 1], inv_h),
+                       hash_cell_coord(xf[3 * v + 2], inv_h))]
+            .push_back(v);
+    }
+    for (uint32_t t = 0; t < s.topo.size(); ++t) {
+        const tet_topo_t& tt = s.topo[t];
+        if (!tt.bmask) continue;
+        float lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = hi[a] = xf[3 * tt.v[0] + a];
+            for (int k = 1; k < 4; ++k) {
+                lo[a] = std::min(lo[a], xf[3 * tt.v[k] + a]);
+                hi[a] = std::max(hi[a], xf[3 * tt.v[k] + a]);
+            }
+        }
+        int32_t c0[3], c1[3];
+        for (int a = 0; a < 3; ++a) {
+            c0[a] = hash_cell_coord(lo[a], inv_h);
+            c1[a] = hash_cell_coord(hi[a], inv_h);
+        }
+        for (int32_t cx = c0[0]; cx <= c1[0]; ++cx)
+            for (int32_t cy = c0[1]; cy <= c1[1]; ++cy)
+                for (int32_t cz = c0[2]; cz <= c1[2]; ++cz) {
+                    auto it = cells.find(hash_key(cx, cy, cz));
+                    if (it == cells.end()) continue;
+                    for (uint32_t v : it->second) {
+                        if (v == tt.v[0] || v == tt.v[1] || v == tt.v[2] || v == tt.v[3]) continue;
+                        if (!self && s.vbody[v] == tt.body) continue;
+                        out.push_back({v, t});
+                    }
+                }
+    }
+}
+
+// Signed distances of p to the four face planes of tet t (outward normals,
+// faces in faces_copy order); returns false if p is outside.
+static bool inside_faces(const sim_t& s, const tet_topo_t& tt, vec3 p, double d[4], vec3 n[4]) {
+    static const int F[4][4] = {{0, 1, 3, 2}, {1, 2, 3, 0}, {2, 0, 3, 1}, {0, 2, 1, 3}};  // a b c opposite
+    bool inside = true;
+    for (int f = 0; f < 4; ++f) {
+        vec3 a = s.particles[tt.v[F[f][0]]].x, b = s.particles[tt.v[F[f][1]]].x, c = s.particles[tt.v[F[f][2]]].x,
+             o = s.particles[tt.v[F[f][3]]].x;
+        vec3 nn = cross(b - a, c - a);
+        double l = norm(nn);
+        if (!(l > 0)) return false;
+        nn = nn / l;
+        if (dot(nn, o - a) > 0) nn = -nn;
+        n[f] = nn;
+        d[f] = dot(p - a, nn);
+        if (d[f] > 0) inside = false;
+    }
+    return inside;
+}
+
+static void detect_bodies(sim_t& sim) {
+    if (!sim.prm.body_contacts || !(sim.prm.hash_cell > 0)) return;
+    const float inv_h = (float)(1.0 / sim.prm.hash_cell);
+    const uint32_t n = (uint32_t)sim.particles.size();
+    std::vector<float> xf(3 * (size_t)n);
+    for (uint32_t v = 0; v < n; ++v) {
+        xf[3 * v] = (float)sim.particles[v].x.x;
+        xf[3 * v + 1] = (float)sim.particles[v].x.y;
+        xf[3 * v + 2] = (float)sim.particles[v].x.z;
+    }
+    std::vector<std::pair<uint32_t, uint32_t>> cand;
+    hash_candidates(sim, xf.data(), inv_h, sim.prm.body_contacts == 2, cand);
+    struct best_t { double d; uint32_t slot, tet; int face; };
+    std::vector<best_t> best(n, best_t{-1e300, 0xFFFFFFFFu, 0, -1});
+    for (auto& c : cand) {
+        const tet_topo_t& tt = sim.topo[c.second];
+        double d[4]; vec3 nn[4];
+        if (!inside_faces(sim, tt, sim.particles[c.first].x, d, nn)) continue;
+        int bf = -1;
+        for (int f = 0; f < 4; ++f)
+            if ((tt.bmask >> f) & 1u)
+                if (bf < 0 || d[f] > d[bf]) bf = f;
+        if (bf < 0) continue;
+        best_t& b = best[c.first];
+        const uint32_t slot = sim.slot_of_tet[c.second];
+        if (d[bf] > b.d || (d[bf] == b.d && slot < b.slot)) b = best_t{d[bf], slot, c.second, bf};
+    }
+    uint32_t nb = 0;
+    for (uint32_t v = 0; v < n; ++v) {
+        if (best[v].face < 0) continue;
+        const tet_topo_t& tt = sim.topo[best[v].tet];
+        double d[4]; vec3 nn[4];
+        inside_faces(sim, tt, sim.particles[v].x, d, nn);
+        const vec3 nf = nn[best[v].face];
+        const vec3 q = sim.particles[v].x - nf * d[best[v].face];
+        sim.collision_constraints.push_back(
+            std::make_unique<collision_constraint_t>(sim.prm.collision_alpha, 0.0, v, q, nf));
+        ++nb;
+    }
+    sim.st.n_body_contacts = nb;
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -560,10 +697,32 @@ int orc_add_body(void* h, const double* x0, const double* xinit, uint32_t nv, co
     std::sort(surf.begin(), surf.end());
     surf.erase(std::unique(surf.begin(), surf.end()), surf.end());
     std::sort(b.surface_tris.begin(), b.surface_tris.end());
+    // per-tet boundary faces and body ids for the spatial hash
+    const uint32_t body_id = (uint32_t)s.bodies.size();
+    s.vbody.resize(s.particles.size(), body_id);
+    s.vsurf.resize(s.particles.size(), 0);
+    for (uint32_t v : surf) s.vsurf[v] = 1;
+    for (uint32_t t = 0; t < nt; ++t) {
+        const uint32_t* q = tets + 4 * t;
+        const uint32_t fl[4][3] = {{q[0], q[1], q[3]}, {q[1], q[2], q[3]}, {q[2], q[0], q[3]}, {q[0], q[2], q[1]}};
+        tet_topo_t tt;
+        for (int k = 0; k < 4; ++k) tt.v[k] = b.v0 + q[k];
+        tt.body = body_id;
+        tt.bmask = 0;
+        for (int f = 0; f < 4; ++f) {
+            uint32_t srt[3] = {fl[f][0], fl[f][1], fl[f][2]};
+            std::sort(srt, srt + 3);
+            uint64_t key = ((uint64_t)srt[0] * nv + srt[1]) * (uint64_t)nv + srt[2];
+            if (faces[key].first == 1) tt.bmask |= (uint8_t)(1u << f);
+        }
+        s.topo.push_back(tt);
+    }
     b.surface = std::move(surf);
     s.bodies.push_back(std::move(b));
     s.sweep.clear();
     for (auto& c : s.constraints) s.sweep.push_back(c.get());
+    s.slot_of_tet.resize(s.constraints.size());
+    for (uint32_t k = 0; k < s.slot_of_tet.size(); ++k) s.slot_of_tet[k] = k;
     s.colour_offsets.clear();
     return (int)s.bodies.size() - 1;
 }
@@ -614,6 +773,7 @@ int orc_set_tet_order(void* h, const uint32_t* order, uint32_t n, const uint32_t
     for (uint32_t k = 0; k < n; ++k) {
         if (order[k] >= n) return 1;
         s.sweep[k] = s.constraints[order[k]].get();
+        s.slot_of_tet[order[k]] = k;
     }
     s.colour_offsets.clear();
     if (offsets) s.colour_offsets.assign(offsets, offsets + n_colours + 1);
@@ -704,7 +864,31 @@ void orc_detect_contacts(void* h) {
     s.ground_end.clear();
     detect_ground(s);
     s.st.n_contacts = (uint32_t)s.collision_constraints.size();
+    s.st.n_body_contacts = 0;
+    detect_bodies(s);   // after the ground contacts: collision list = [ground..., bodies...]
 }
+
+// mode 0 off, 1 between bodies, 2 also within a body; cell size h (metres).
+void orc_set_body_contacts(void* h, int mode, double cell) {
+    sim_t& s = *(sim_t*)h;
+    s.prm.body_contacts = mode;
+    s.prm.hash_cell = cell;
+}
+
+// Candidate (vertex, tet) pairs of the spatial hash for float positions
+// xf [3 * n] (add order), sorted as (vertex << 32 | tet).  Returns the count.
+uint64_t orc_hash_candidates(void* h, const float* xf, double cell, int self, uint64_t* out, uint64_t cap) {
+    sim_t& s = *(sim_t*)h;
+    std::vector<std::pair<uint32_t, uint32_t>> c;
+    hash_candidates(s, xf, (float)(1.0 / cell), self, c);
+    std::vector<uint64_t> k(c.size());
+    for (size_t i = 0; i < c.size(); ++i) k[i] = ((uint64_t)c[i].first << 32) | c[i].second;
+    std::sort(k.begin(), k.end());
+    for (size_t i = 0; i < k.size() && i < cap; ++i) out[i] = k[i];
+    return k.size();
+}
+
+uint32_t orc_n_body_contacts(void* h) { return ((sim_t*)h)->st.n_body_contacts; }
 
 // timestep_t::step (timestep.cpp:20-70): contacts once per frame from x, then
 // per substep predict -> solve -> set x, v.

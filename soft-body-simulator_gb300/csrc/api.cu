@@ -19,6 +19,8 @@
 
 #include "../../include/sbs_gpu.h"
 #include "xpbd_internal.cuh"
+#include "cluster_internal.cuh"
+#include "hash_internal.cuh"
 
 using namespace sbs;
 
@@ -83,6 +85,19 @@ struct sbs_gpu {
     std::map<GraphKey, cudaGraphExec_t> graphs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<void*> allocations;
+    // cluster-resident mode
+    bool cl_feasible = false, global_modes = true;
+    int cl_size = 1, cl_block = 256, cl_grid = 1;
+    size_t cl_smem = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> cl_groups;  // body ranges
+    ClusterDev cd{};
+    // body-body contacts
+    bool body_on = false;
+    HashDev hd{};
+    double hash_cell = 0.0;
+    std::vector<uint8_t> bmask;        // boundary faces per tet slot
+    double sim_time = 0.0;   // host mirror of the simulation time
+    std::vector<uint32_t> seg_split;  // first SNH slot of each colour segment
 
     // stats
     uint64_t frames = 0, projections = 0;
@@ -319,7 +334,7 @@ sbs_status sbs_gpu_params_default(sbs_gpu_params* p) {
     p->tail_threshold = -1;
     p->body_contacts = 0;
     p->hash_cell = 0.0f;
-    p->max_body_contacts = 0;
+    p->candidate_capacity = 0;
     p->check_finite = 1;
     return SBS_OK;
 }
@@ -331,7 +346,7 @@ sbs_status sbs_gpu_create(const sbs_gpu_params* p, sbs_gpu** out) {
     if (p) prm = *p;
     else sbs_gpu_params_default(&prm);
     if (prm.gravity_mode != 0 && prm.gravity_mode != 1) return fail(nullptr, SBS_EINVAL, "gravity_mode");
-    if (prm.exec_mode < 0 || prm.exec_mode > 2) return fail(nullptr, SBS_EINVAL, "exec_mode");
+    if (prm.exec_mode < 0 || prm.exec_mode > 3) return fail(nullptr, SBS_EINVAL, "exec_mode");
     if (prm.block_size != 0 && (prm.block_size < 32 || prm.block_size > 512 || prm.block_size % 32))
         return fail(nullptr, SBS_EINVAL, "block_size must be a multiple of 32 in [32, 512]");
     int ndev = 0;
@@ -514,17 +529,99 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
             new_to_old[b.v0 + n] = b.v0 + key[n].second;
         }
     }
-    // 2-4. sweep order: colour (size-descending), model, Morton code
+    // 2. groups of consecutive bodies for the cluster-resident mode: every
+    //    group must fit the shared memory of one cluster (<= 16 CTAs)
+    const int P = (int)h->planes.size();
+    int smem_optin = 0;
+    CU(h, cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->prm.device));
+    const size_t per_v = cluster_smem_bytes(1, P, h->prm.body_contacts ? 1 : 0);
+    const uint32_t cap_slice = (uint32_t)((size_t)(smem_optin - 2048) / per_v);
+    uint32_t max_body = 0;
+    for (const BodyHost& b : h->bodies) max_body = std::max(max_body, b.nv);
+    h->cl_size = 1;
+    while (h->cl_size < 16 && (uint64_t)h->cl_size * cap_slice < max_body) h->cl_size *= 2;
+    h->cl_feasible = (uint64_t)h->cl_size * cap_slice >= max_body && h->prm.exec_mode != SBS_EXEC_GRAPH &&
+                     h->prm.exec_mode != SBS_EXEC_PERSISTENT;
+    h->cl_groups.clear();
+    if (h->cl_feasible) {
+        const uint64_t cap = (uint64_t)h->cl_size * cap_slice;
+        uint32_t b0 = 0, nv = 0;
+        for (uint32_t bi = 0; bi < h->bodies.size(); ++bi) {
+            if (nv + h->bodies[bi].nv > cap && bi > b0) {
+                h->cl_groups.push_back({b0, bi});
+                b0 = bi;
+                nv = 0;
+            }
+            nv += h->bodies[bi].nv;
+        }
+        h->cl_groups.push_back({b0, (uint32_t)h->bodies.size()});
+    }
+    // 3. sweep order: per group (several groups) or over the whole scene:
+    //    colour (size-descending), model, Morton code
     std::vector<uint32_t> split;
-    const int K = plan_sweep(h->x0.data(), V, h->tets.data(), T, h->tet_model.data(), h->tet_order,
-                             h->colour_offsets, split);
-    if (K < 0) return fail(h, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
-    h->n_colours = (uint32_t)K;
-    // 5. block size, tail threshold
+    std::vector<uint32_t> gcol_start, gcol_split;
+    std::vector<GroupDesc> gdesc;
+    int K = 0;
+    if (h->cl_feasible && h->cl_groups.size() > 1) {
+        h->tet_order.clear();
+        h->colour_offsets.assign(1, 0);
+        for (auto& gr : h->cl_groups) {
+            const BodyHost& bf = h->bodies[gr.first];
+            const BodyHost& bl = h->bodies[gr.second - 1];
+            const uint32_t ov0 = bf.v0, onv = bl.v0 + bl.nv - bf.v0;
+            const uint32_t t0 = bf.t0, nt = bl.t0 + bl.nt - bf.t0;
+            std::vector<uint32_t> lt(4ull * nt);
+            for (uint64_t i = 0; i < 4ull * nt; ++i) lt[i] = h->tets[4ull * t0 + i] - ov0;
+            std::vector<uint32_t> ord, off, spl;
+            const int Kg = plan_sweep(&h->x0[3ull * ov0], onv, lt.data(), nt, &h->tet_model[t0], ord, off, spl);
+            if (Kg < 0) return fail(h, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
+            const uint32_t base = (uint32_t)h->tet_order.size();
+            GroupDesc g;
+            g.v0 = ov0;  // library ids keep the add order of bodies
+            g.nv = onv;
+            g.col_base = (uint32_t)gcol_start.size();
+            g.n_col = (uint32_t)Kg;
+            gdesc.push_back(g);
+            for (uint32_t k : ord) h->tet_order.push_back(t0 + k);
+            for (int c = 0; c <= Kg; ++c) gcol_start.push_back(base + off[c]);
+            for (int c = 0; c < Kg; ++c) gcol_split.push_back(base + spl[c]);
+            for (int c = 0; c < Kg; ++c) h->seg_split.push_back(base + spl[c]);
+            gcol_split.push_back(base + off[Kg]);
+            for (int c = 1; c <= Kg; ++c) h->colour_offsets.push_back(base + off[c]);
+            K = std::max(K, Kg);
+        }
+        h->global_modes = false;   // tets are group-major: only the cluster mode runs them
+        h->n_colours = (uint32_t)(h->colour_offsets.size() - 1);
+    } else {
+        K = plan_sweep(h->x0.data(), V, h->tets.data(), T, h->tet_model.data(), h->tet_order, h->colour_offsets,
+                       split);
+        if (K < 0) return fail(h, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
+        h->n_colours = (uint32_t)K;
+        h->global_modes = true;
+        h->seg_split = split;
+        if (h->cl_feasible) {
+            GroupDesc g;
+            g.v0 = 0;
+            g.nv = V;
+            g.col_base = 0;
+            g.n_col = (uint32_t)K;
+            gdesc.push_back(g);
+            gcol_start = h->colour_offsets;
+            gcol_split = split;
+            gcol_split.push_back(T);
+        }
+    }
+    // single group: enough CTAs that a colour is about one tet per thread
+    if (h->cl_feasible && gdesc.size() == 1) {
+        uint32_t maxc = 0;
+        for (size_t c = 0; c + 1 < gcol_start.size(); ++c) maxc = std::max(maxc, gcol_start[c + 1] - gcol_start[c]);
+        while (h->cl_size < 16 && (uint64_t)h->cl_size * 256 < maxc) h->cl_size *= 2;
+    }
+    // 4. block size
     h->block = h->prm.block_size ? h->prm.block_size : 256;
     int tail_thr = h->prm.tail_threshold >= 0 ? h->prm.tail_threshold : h->block;
-    h->first_tail = (uint32_t)K;
-    while (h->first_tail > 0 &&
+    h->first_tail = h->global_modes ? (uint32_t)K : 0;
+    while (h->global_modes && h->first_tail > 0 &&
            h->colour_offsets[h->first_tail] - h->colour_offsets[h->first_tail - 1] <= (uint32_t)tail_thr)
         --h->first_tail;
     // 6. per-vertex data in library order
@@ -593,6 +690,17 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
         h->surf.clear();
         for (uint32_t n = 0; n < V; ++n)
             if (on[n]) h->surf.push_back(n);
+        // boundary faces per tet slot (spatial hash queries and contact faces)
+        h->bmask.assign(T, 0);
+        for (uint32_t k = 0; k < T; ++k) {
+            const uint32_t* q = &h->tets[4ull * h->tet_order[k]];
+            const uint32_t fl[4][3] = {{q[0], q[1], q[3]}, {q[1], q[2], q[3]}, {q[2], q[0], q[3]}, {q[0], q[2], q[1]}};
+            for (int f = 0; f < 4; ++f) {
+                uint32_t s3[3] = {fl[f][0], fl[f][1], fl[f][2]};
+                std::sort(s3, s3 + 3);
+                if (fc[((uint64_t)s3[0] * V + s3[1]) * (uint64_t)V + s3[2]] == 1) h->bmask[k] |= (uint8_t)(1u << f);
+            }
+        }
     }
     // 9. device allocations and upload
     SceneDev& d = h->d;
@@ -604,7 +712,7 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
 #define AL(p, n) if ((s = dalloc(h, &(p), (n))) != SBS_OK) return s
     AL(d.xi, V); AL(d.xn, V); AL(d.v, V);
     if (need_acc) { AL(d.acc, V); } else d.acc = nullptr;
-    AL(d.tet, T); AL(d.dm0, T); AL(d.dm1, T); AL(d.dm2, T); AL(d.lam0, T); AL(d.lam1, T);
+    AL(d.model, T); AL(d.tet, T); AL(d.dm0, T); AL(d.dm1, T); AL(d.dm2, T); AL(d.lam0, T); AL(d.lam1, T);
     AL(d.surf, d.n_surf);
     const size_t ncont = (size_t)kMaxPlanes * d.n_surf;
     AL(d.contacts, ncont); AL(d.contact_lam, ncont);
@@ -624,6 +732,11 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     if ((s = upload(h, d.dm0, d0.data(), T * sizeof(float4))) != SBS_OK) return s;
     if ((s = upload(h, d.dm1, d1.data(), T * sizeof(float4))) != SBS_OK) return s;
     if ((s = upload(h, d.dm2, d2.data(), T * sizeof(float4))) != SBS_OK) return s;
+    {
+        std::vector<uint8_t> mdl(T);
+        for (uint32_t k = 0; k < T; ++k) mdl[k] = (uint8_t)h->tet_model[h->tet_order[k]];
+        if ((s = upload(h, d.model, mdl.data(), T)) != SBS_OK) return s;
+    }
     if ((s = upload(h, d.surf, h->surf.data(), d.n_surf * sizeof(uint32_t))) != SBS_OK) return s;
     CU(h, cudaMemsetAsync(d.lam0, 0, T * sizeof(float), h->st));
     CU(h, cudaMemsetAsync(d.lam1, 0, T * sizeof(float), h->st));
@@ -633,6 +746,106 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     CU(h, cudaMemsetAsync(d.bar, 0, 2 * sizeof(unsigned), h->st));
     CU(h, cudaMallocHost((void**)&h->h_stage, V * sizeof(float4)));
     CU(h, cudaMallocHost((void**)&h->h_stage2, V * sizeof(float4)));
+    // spatial hash for body-body contacts
+    if (h->prm.body_contacts && d.n_surf > 0) {
+        HashDev& hd = h->hd;
+        double cell = h->prm.hash_cell;
+        if (!(cell > 0)) {  // 2 x mean edge length of the rest meshes
+            double sum = 0;
+            uint64_t cnt = 0;
+            static const int E[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+            for (uint32_t t = 0; t < T; ++t)
+                for (auto& e : E) {
+                    const uint32_t a = h->tets[4ull * t + e[0]], b = h->tets[4ull * t + e[1]];
+                    double l2 = 0;
+                    for (int k = 0; k < 3; ++k) {
+                        const double dd = h->x0[3ull * a + k] - h->x0[3ull * b + k];
+                        l2 += dd * dd;
+                    }
+                    sum += std::sqrt(l2);
+                    ++cnt;
+                }
+            cell = 2.0 * sum / (double)cnt;
+        }
+        h->hash_cell = cell;
+        hd.inv_h = (float)(1.0 / cell);
+        hd.self = h->prm.body_contacts == 2 ? 1 : 0;
+        uint32_t cap = 1024;
+        while (cap < 2 * d.n_surf) cap *= 2;
+        if (cap > (1u << 22)) return fail(h, SBS_EINVAL, "too many surface vertices for the contact hash");
+        hd.mask = cap - 1;
+        std::vector<uint32_t> vb(V), qlist;
+        for (uint32_t bi = 0; bi < h->bodies.size(); ++bi)
+            for (uint32_t i = 0; i < h->bodies[bi].nv; ++i) vb[h->bodies[bi].v0 + i] = bi;
+        for (uint32_t k = 0; k < T; ++k)
+            if (h->bmask[k]) qlist.push_back(k);
+        hd.n_query = (uint32_t)qlist.size();
+        const uint32_t tiles = (cap + 1023) / 1024;
+        if ((s = dalloc(h, &hd.keys, cap)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.count, cap)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.start, cap)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.fill, cap)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.tile_sums, tiles)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.tile_scan, tiles)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.tile_sums2, 8)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.tile_scan2, 8)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.vslot, d.n_surf)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.entries, d.n_surf)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.vbody, V)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.bmask, T)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.query, qlist.size())) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.best, V)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.bc_q, V)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.bc_n, V)) != SBS_OK) return s;
+        if ((s = dalloc(h, &hd.n_cand, 1)) != SBS_OK) return s;
+        hd.cand = nullptr;
+        hd.cand_cap = h->prm.candidate_capacity;
+        if (hd.cand_cap && (s = dalloc(h, &hd.cand, hd.cand_cap)) != SBS_OK) return s;
+        if ((s = upload(h, hd.vbody, vb.data(), V * 4)) != SBS_OK) return s;
+        if ((s = upload(h, hd.bmask, h->bmask.data(), T)) != SBS_OK) return s;
+        if ((s = upload(h, hd.query, qlist.data(), qlist.size() * 4)) != SBS_OK) return s;
+        CU(h, cudaMemsetAsync(hd.bc_q, 0, V * sizeof(float4), h->st));
+        CU(h, cudaMemsetAsync(hd.bc_n, 0, V * sizeof(float4), h->st));
+        CU(h, cudaMemsetAsync(hd.n_cand, 0, sizeof(unsigned long long), h->st));
+        h->body_on = true;
+    }
+    // cluster-resident mode: packed (rank, slice offset) vertex ids, surface
+    // flags, group descriptors and per-group colour tables
+    if (h->cl_feasible) {
+        ClusterDev& c = h->cd;
+        c.cluster_size = (uint32_t)h->cl_size;
+        uint32_t slice = 1;
+        for (const GroupDesc& g : gdesc) slice = std::max(slice, (g.nv + c.cluster_size - 1) / c.cluster_size);
+        c.slice = slice;
+        c.xn_minus_xi = slice * 16u;
+        c.n_groups = (uint32_t)gdesc.size();
+        h->cl_smem = cluster_smem_bytes(slice, P, h->body_on ? 1 : 0);
+        c.body = h->body_on ? 1 : 0;
+        c.bc_q = h->hd.bc_q;
+        c.bc_n = h->hd.bc_n;
+        std::vector<uint32_t> vgroup(V);
+        for (uint32_t gi = 0; gi < gdesc.size(); ++gi)
+            for (uint32_t n = gdesc[gi].v0; n < gdesc[gi].v0 + gdesc[gi].nv; ++n) vgroup[n] = gi;
+        auto pack = [&](uint32_t n) {
+            const uint32_t local = n - gdesc[vgroup[n]].v0;
+            return ((local / slice) << 24) | (local % slice);
+        };
+        std::vector<uint4> tp(T);
+        for (uint32_t k = 0; k < T; ++k) tp[k] = make_uint4(pack(tid[k].x), pack(tid[k].y), pack(tid[k].z), pack(tid[k].w));
+        std::vector<uint8_t> vf(V, 0);
+        for (uint32_t n : h->surf) vf[n] = 1;
+        if ((s = dalloc(h, &c.tet_packed, T)) != SBS_OK) return s;
+        if ((s = dalloc(h, &c.vflags, V)) != SBS_OK) return s;
+        if ((s = dalloc(h, &c.groups, gdesc.size())) != SBS_OK) return s;
+        if ((s = dalloc(h, &c.col_start, gcol_start.size())) != SBS_OK) return s;
+        if ((s = dalloc(h, &c.col_split, gcol_split.size())) != SBS_OK) return s;
+        if ((s = upload(h, c.tet_packed, tp.data(), T * sizeof(uint4))) != SBS_OK) return s;
+        if ((s = upload(h, c.vflags, vf.data(), V)) != SBS_OK) return s;
+        if ((s = upload(h, c.groups, gdesc.data(), gdesc.size() * sizeof(GroupDesc))) != SBS_OK) return s;
+        if ((s = upload(h, c.col_start, gcol_start.data(), gcol_start.size() * 4)) != SBS_OK) return s;
+        if ((s = upload(h, c.col_split, gcol_split.data(), gcol_split.size() * 4)) != SBS_OK) return s;
+        if ((size_t)smem_optin < h->cl_smem + 2048) h->cl_feasible = false;
+    }
     CU(h, cudaStreamSynchronize(h->st));
     // 10. step constants
     StepParams& p = h->base;
@@ -647,19 +860,45 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     for (size_t i = 0; i < h->planes.size(); ++i) p.planes[i] = h->planes[i];
     p.n_kin_groups = (int)h->groups.size();
     p.has_acc = h->has_acc ? 1 : 0;
+    p.body_contacts = h->body_on ? 1 : 0;
     for (size_t i = 0; i < h->groups.size(); ++i) p.kin[i] = h->groups[i];
-    for (int c = 0; c <= K; ++c) p.colour_start[c] = h->colour_offsets[c];
-    for (int c = 0; c < K; ++c) p.colour_split[c] = split[c];
+    if (h->global_modes) {
+        p.n_colours = K;
+        for (int c = 0; c <= K; ++c) p.colour_start[c] = h->colour_offsets[c];
+        for (int c = 0; c < K; ++c) p.colour_split[c] = split[c];
+    } else {
+        p.n_colours = 0;
+        p.first_tail = 0;
+    }
     // 11. execution mode
     int occ = 0;
     CU(h, persistent_occupancy(h->block, &occ));
     uint32_t maxc = 0;
-    for (int c = 0; c < K; ++c) maxc = std::max(maxc, h->colour_offsets[c + 1] - h->colour_offsets[c]);
+    for (uint32_t c = 0; c + 1 < h->colour_offsets.size(); ++c)
+        maxc = std::max(maxc, h->colour_offsets[c + 1] - h->colour_offsets[c]);
     h->grid = std::max(1, std::min(h->n_sm * 8, (int)((maxc + 31) / 32)));
     int cps = h->prm.ctas_per_sm > 0 ? std::min(h->prm.ctas_per_sm, occ) : occ;
     h->pers_block = h->block;
     h->pers_grid = std::max(1, std::min(cps * h->n_sm, (int)((maxc + 31) / 32)));
-    h->exec_mode = h->prm.exec_mode == SBS_EXEC_AUTO ? SBS_EXEC_PERSISTENT : h->prm.exec_mode;
+    if (h->cl_feasible) {
+        h->cl_block = h->prm.block_size ? std::min(h->prm.block_size, kClusterMaxBlock) : 256;
+        CU(h, cluster_configure(h->cl_block, h->cl_smem));
+        int active = 0;
+        cudaError_t e = cluster_max_active(h->cl_size, h->cl_block, h->cl_smem, &active);
+        if (e != cudaSuccess || active < 1) {
+            cudaGetLastError();
+            h->cl_feasible = false;
+        } else {
+            h->cl_grid = std::max(1, std::min(active, (int)h->cd.n_groups));
+        }
+    }
+    if (!h->global_modes && !h->cl_feasible) return fail(h, SBS_ESTATE, "no execution mode fits this scene");
+    if (h->prm.exec_mode == SBS_EXEC_CLUSTER && !h->cl_feasible)
+        return fail(h, SBS_EINVAL, "scene does not fit the cluster-resident mode");
+    if (h->prm.exec_mode == SBS_EXEC_AUTO)
+        h->exec_mode = h->cl_feasible ? SBS_EXEC_CLUSTER : SBS_EXEC_PERSISTENT;
+    else
+        h->exec_mode = h->prm.exec_mode;
     if (h->exec_mode == SBS_EXEC_PERSISTENT && occ < 1) h->exec_mode = SBS_EXEC_GRAPH;
     h->tuned = h->prm.exec_mode != SBS_EXEC_AUTO;
     h->finalized = true;
@@ -687,10 +926,12 @@ static sbs_status enqueue_frame_kernels(sbs_gpu* h, const StepParams& p) {
     cudaStream_t st = h->st;
     CU(h, cudaMemsetAsync(d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), st));
     CU(h, launch_detect_ground(d, p, st));
+    if (h->body_on) CU(h, launch_body_detect(d, h->hd, st));
     for (int sub = 0; sub < p.substeps; ++sub) {
         CU(h, launch_predict(d, p, sub, st));
         for (int it = 0; it < p.iterations; ++it) {
             CU(h, launch_contacts(d, p, it == 0, st));
+            CU(h, launch_body_contacts(d, p, it == 0, st));
             for (int c = 0; c < p.first_tail; ++c) CU(h, launch_colour(d, p, c, it == 0, h->block, h->grid, st));
             CU(h, launch_tail(d, p, it == 0, h->block, st));
         }
@@ -703,11 +944,21 @@ static sbs_status enqueue_frame_kernels(sbs_gpu* h, const StepParams& p) {
 static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations) {
     StepParams p;
     fill_params(h, p, dt, substeps, iterations);
-    if (h->exec_mode == SBS_EXEC_PERSISTENT) {
+    double t_end = h->sim_time;
+    for (uint32_t k = 0; k < substeps; ++k) t_end += dt;   // same double sequence as the CPU loop
+    if (h->exec_mode == SBS_EXEC_CLUSTER) {
+        // the kernel publishes the frame's contacts into the last-frame slots
+        CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+        if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
+        CU(h, launch_cluster_frame(h->d, h->cd, p, h->sim_time, h->cl_grid, h->cl_block, h->cl_smem, h->st));
+        CU(h, launch_end_frame(h->d, h->st));
+        CU(h, launch_store_time(h->d.time, t_end, h->st));
+    } else if (h->exec_mode == SBS_EXEC_PERSISTENT) {
         // the frame kernel expects zero live contact counters (it zeroes them
         // itself at frame end); a standalone detect may have left them set
         if (h->contacts_live)
             CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+        if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
         CU(h, launch_persistent_frame(h->d, p, h->pers_block, h->pers_grid, h->st));
     } else {
         GraphKey key{dt, substeps, iterations};
@@ -730,6 +981,7 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
     h->frames++;
     h->projections += (uint64_t)substeps * iterations * h->n_tets;
     h->contacts_live = false;
+    h->sim_time = t_end;
     return SBS_OK;
 }
 
@@ -754,7 +1006,10 @@ static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t it
     for (uint32_t c = 0; c < h->n_colours; ++c)
         maxc = std::max(maxc, h->colour_offsets[c + 1] - h->colour_offsets[c]);
     const int need = std::max(1, (int)((maxc + 31) / 32));
+    if (h->cl_feasible)
+        for (int blk : {256, 512}) cands.push_back({SBS_EXEC_CLUSTER, blk, 0});
     for (int blk : {128, 256}) {
+        if (!h->global_modes) break;
         int occ = 0;
         if (persistent_occupancy(blk, &occ) != cudaSuccess || occ < 1) continue;
         for (int g : {h->n_sm / 2, h->n_sm, 2 * h->n_sm, occ * h->n_sm}) {
@@ -764,14 +1019,25 @@ static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t it
             if (!dup) cands.push_back({SBS_EXEC_PERSISTENT, blk, gg});
         }
     }
-    cands.push_back({SBS_EXEC_GRAPH, 256, h->grid});
+    if (h->global_modes) cands.push_back({SBS_EXEC_GRAPH, 256, h->grid});
     const int saved_mode = h->exec_mode, saved_pb = h->pers_block, saved_pg = h->pers_grid;
     const uint64_t saved_frames = h->frames, saved_proj = h->projections;
+    const double saved_time = h->sim_time;
     float best = 1e30f;
-    Cand bestc{saved_mode, saved_pb, saved_pg};
+    Cand bestc{saved_mode, h->exec_mode == SBS_EXEC_CLUSTER ? h->cl_block : saved_pb, saved_pg};
     for (const Cand& c : cands) {
         h->exec_mode = c.mode;
         if (c.mode == SBS_EXEC_PERSISTENT) { h->pers_block = c.block; h->pers_grid = c.grid; }
+        if (c.mode == SBS_EXEC_CLUSTER) {
+            int active = 0;
+            if (cluster_configure(c.block, h->cl_smem) != cudaSuccess ||
+                cluster_max_active(h->cl_size, c.block, h->cl_smem, &active) != cudaSuccess || active < 1) {
+                cudaGetLastError();
+                continue;
+            }
+            h->cl_block = c.block;
+            h->cl_grid = std::max(1, std::min(active, (int)h->cd.n_groups));
+        }
         sbs_status s = run_frame(h, dt, substeps, iterations);  // warm-up (and graph capture)
         if (s != SBS_OK) continue;
         CU(h, cudaEventRecord(h->ev0, h->st));
@@ -786,8 +1052,16 @@ static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t it
     }
     h->exec_mode = bestc.mode;
     if (bestc.mode == SBS_EXEC_PERSISTENT) { h->pers_block = bestc.block; h->pers_grid = bestc.grid; }
+    if (bestc.mode == SBS_EXEC_CLUSTER) {
+        int active = 0;
+        h->cl_block = bestc.block;
+        CU(h, cluster_configure(h->cl_block, h->cl_smem));
+        CU(h, cluster_max_active(h->cl_size, h->cl_block, h->cl_smem, &active));
+        h->cl_grid = std::max(1, std::min(active, (int)h->cd.n_groups));
+    }
     h->frames = saved_frames;
     h->projections = saved_proj;
+    h->sim_time = saved_time;
     CU(h, cudaMemcpyAsync(d.xi, bxi, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
     CU(h, cudaMemcpyAsync(d.xn, bxn, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
     CU(h, cudaMemcpyAsync(d.v, bv, V * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
@@ -840,6 +1114,7 @@ sbs_status sbs_gpu_detect_contacts(sbs_gpu* h) {
     fill_params(h, p, 1.0, 1, 1);
     CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
     CU(h, launch_detect_ground(h->d, p, h->st));
+    if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
     h->contacts_live = true;
     return SBS_OK;
 }
@@ -861,6 +1136,7 @@ sbs_status sbs_gpu_update_velocities(sbs_gpu* h, double dt) {
     StepParams p;
     fill_params(h, p, dt, 1, 1);
     CU(h, launch_finalize(h->d, p, h->st));
+    h->sim_time += dt;
     return SBS_OK;
 }
 
@@ -871,10 +1147,20 @@ sbs_status sbs_gpu_solve(sbs_gpu* h, double dt, uint32_t iterations) {
     StepParams p;
     fill_params(h, p, dt, 1, iterations);
     if (!h->contacts_live) CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+    // one launch per vertex-disjoint colour segment (all groups' colours in
+    // sweep order), whatever the execution mode of sbs_gpu_step
     for (uint32_t it = 0; it < iterations; ++it) {
         CU(h, launch_contacts(h->d, p, it == 0, h->st));
-        for (uint32_t c = 0; c < h->first_tail; ++c) CU(h, launch_colour(h->d, p, c, it == 0, h->block, h->grid, h->st));
-        CU(h, launch_tail(h->d, p, it == 0, h->block, h->st));
+        CU(h, launch_body_contacts(h->d, p, it == 0, h->st));
+        for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c) {
+            StepParams q = p;
+            q.n_colours = 1;
+            q.first_tail = 1;
+            q.colour_start[0] = h->colour_offsets[c];
+            q.colour_start[1] = h->colour_offsets[c + 1];
+            q.colour_split[0] = h->seg_split[c];
+            CU(h, launch_colour(h->d, q, 0, it == 0, h->block, h->grid, h->st));
+        }
     }
     h->projections += (uint64_t)iterations * h->n_tets;
     return SBS_OK;
@@ -1034,16 +1320,21 @@ sbs_status sbs_gpu_get_contacts(sbs_gpu* h, uint32_t* verts, float* qn, uint32_t
     CU(h, cudaStreamSynchronize(h->st));
     const uint32_t* c = h->contacts_live ? cnt : cnt + kMaxPlanes + 1;
     std::vector<std::pair<std::pair<uint32_t, uint32_t>, std::array<float, 6>>> all;
-    for (size_t pl = 0; pl < h->planes.size(); ++pl) {
-        std::vector<Contact> buf(c[pl]);
-        if (c[pl])
-            CU(h, cudaMemcpyAsync(buf.data(), h->d.contacts + pl * h->d.n_surf, c[pl] * sizeof(Contact),
+    // ground planes in order, then the body-body segment (ordered after them)
+    const size_t P = h->planes.size();
+    for (size_t seg = 0; seg <= P; ++seg) {
+        const size_t src = seg < P ? seg : (size_t)kMaxPlanes;
+        if (seg == P && !h->body_on) break;
+        const uint32_t m = std::min(c[src], h->d.n_surf);
+        std::vector<Contact> buf(m);
+        if (m)
+            CU(h, cudaMemcpyAsync(buf.data(), h->d.contacts + src * h->d.n_surf, m * sizeof(Contact),
                                   cudaMemcpyDeviceToHost, h->st));
         CU(h, cudaStreamSynchronize(h->st));
         for (const Contact& k : buf) {
             uint32_t vid;
             std::memcpy(&vid, &k.q.w, 4);
-            all.push_back({{(uint32_t)pl, to_global(h, vid)}, {k.q.x, k.q.y, k.q.z, k.n.x, k.n.y, k.n.z}});
+            all.push_back({{(uint32_t)seg, to_global(h, vid)}, {k.q.x, k.q.y, k.q.z, k.n.x, k.n.y, k.n.z}});
         }
     }
     std::sort(all.begin(), all.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
@@ -1052,6 +1343,29 @@ sbs_status sbs_gpu_get_contacts(sbs_gpu* h, uint32_t* verts, float* qn, uint32_t
         if (verts) verts[i] = all[i].first.second;
         if (qn) std::copy(all[i].second.begin(), all[i].second.end(), qn + 6ull * i);
     }
+    return check_err(h);
+}
+
+sbs_status sbs_gpu_get_candidates(sbs_gpu* h, uint64_t* pairs, uint64_t cap, uint64_t* n) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!h->body_on) return fail(h, SBS_ESTATE, "body contacts are off");
+    if (!h->hd.cand) return fail(h, SBS_ESTATE, "candidate recording is off (params.candidate_capacity = 0)");
+    unsigned long long total = 0;
+    CU(h, cudaMemcpyAsync(&total, h->hd.n_cand, sizeof(total), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    const uint64_t m = std::min<uint64_t>(total, h->hd.cand_cap);
+    std::vector<unsigned long long> buf(m);
+    if (m) CU(h, cudaMemcpyAsync(buf.data(), h->hd.cand, m * 8, cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    for (auto& k : buf) {
+        const uint32_t v = (uint32_t)(k >> 32), slot = (uint32_t)(k & 0xFFFFFFFFull);
+        k = ((unsigned long long)to_global(h, v) << 32) | h->tet_order[slot];
+    }
+    std::sort(buf.begin(), buf.end());
+    if (n) *n = total;
+    if (pairs)
+        for (uint64_t i = 0; i < m && i < cap; ++i) pairs[i] = buf[i];
     return check_err(h);
 }
 
@@ -1093,8 +1407,12 @@ sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st) {
     for (size_t pl = 0; pl < h->planes.size(); ++pl) st->n_contacts += c[pl];
     st->n_body_contacts = c[kMaxPlanes];
     st->exec_mode = h->exec_mode;
-    st->grid_ctas = h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_grid : h->grid;
-    st->block_size = h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_block : h->block;
+    st->grid_ctas = h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_grid
+                    : h->exec_mode == SBS_EXEC_CLUSTER  ? h->cl_grid * h->cl_size
+                                                        : h->grid;
+    st->block_size = h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_block
+                     : h->exec_mode == SBS_EXEC_CLUSTER  ? h->cl_block
+                                                         : h->block;
     st->residual = h->residual;
     st->energy = h->energy;
     st->last_frame_ms = h->last_frame_ms;

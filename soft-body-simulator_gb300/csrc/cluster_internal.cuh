@@ -1,0 +1,49 @@
+// Layout of the cluster-resident execution mode (cluster_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "xpbd_internal.cuh"
+
+namespace sbs {
+
+constexpr int kClusterMaxBlock = 512;
+
+// One group of whole bodies run by one thread-block cluster: vertices
+// [v0, v0 + nv) in library order, colour table entries
+// [col_base, col_base + n_col] of ClusterDev::col_start / col_split.
+struct GroupDesc {
+    uint32_t v0, nv, col_base, n_col;
+};
+
+struct ClusterDev {
+    GroupDesc* groups;
+    uint32_t n_groups;
+    uint32_t* col_start;   // per group: n_col + 1 tet offsets (global tet slots)
+    uint32_t* col_split;   // per group: first SNH slot of each colour
+    uint4* tet_packed;     // per tet slot: vertex as (cluster rank << 24) | slice offset
+    uint8_t* vflags;       // per vertex: bit 0 = surface vertex
+    uint32_t cluster_size;
+    uint32_t slice;        // vertices per CTA slice
+    uint32_t xn_minus_xi;  // byte offset from the xi slice to the xn slice
+    int body;              // 1: body-body contacts (records below)
+    const float4* bc_q;    // [V] body contact point, w != 0 when present
+    const float4* bc_n;    // [V] body contact normal, w = slot in the global list (bits)
+};
+
+// Dynamic shared memory of one CTA for `slice` vertices, `planes` planes and
+// an optional body-contact slot: xi, xn, v, contact records and body normals
+// (float4), global contact slots and the contact vertex list (uint32).
+inline size_t cluster_smem_bytes(uint32_t slice, int planes, int body) {
+    const size_t S = (size_t)planes + (body ? 1 : 0);
+    return (size_t)slice * (3 * 16 + S * 16 + (body ? 16 : 0) + S * 4 + 4);
+}
+
+cudaError_t cluster_configure(int block, size_t smem);
+cudaError_t cluster_max_active(int cluster_size, int block, size_t smem, int* n);
+cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const StepParams& p, double t0,
+                                 int n_clusters, int block, size_t smem, cudaStream_t st);
+cudaError_t launch_store_time(double* t, double v, cudaStream_t st);
+
+}  // namespace sbs

@@ -1,0 +1,355 @@
+// Cluster-resident XPBD frame kernel for sm_103a.
+//
+// A thread-block cluster of C CTAs (C <= 16) owns a group of whole bodies.
+// The group's vertex state (xi, xn, v) is split into C contiguous slices,
+// one per CTA, and kept in shared memory for the whole frame; tets gather
+// and scatter their four vertices through distributed shared memory
+// (mapa + ld/st.shared::cluster).  Colour phases are separated by the
+// hardware cluster barrier (barrier.cluster.arrive.release / wait.acquire),
+// so a frame needs no grid-wide synchronisation at all and clusters working
+// on different groups never wait for one another.
+//
+// The sweep is the same Gauss-Seidel order as the global kernels: per
+// iteration the group's contacts (each touches one vertex; a vertex's planes
+// in plane order), then the colours one after another (timestep.cpp:20-70,
+// gauss_seidel_solver.cpp:8-37).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cluster_internal.cuh"
+#include "xpbd_internal.cuh"
+#include "xpbd_math.cuh"
+
+namespace sbs {
+
+__device__ __forceinline__ uint32_t cl_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cl_id() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cl_count() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint32_t map_rank(uint32_t addr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ float4 ld_dsmem(uint32_t addr) {
+    float4 v;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_dsmem(uint32_t addr, float4 v) {
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};"
+                 :: "r"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w) : "memory");
+}
+
+// Address of packed vertex (rank << 24 | local) in the cluster's xi slices.
+__device__ __forceinline__ uint32_t vaddr(uint32_t packed, uint32_t xi_base) {
+    return map_rank(xi_base + ((packed & 0xFFFFFFu) << 4), packed >> 24);
+}
+
+__device__ __forceinline__ void project_tet_dsmem(const SceneDev& s, const ClusterDev& c, const StepParams& p,
+                                                  uint32_t t, bool snh, bool first, uint32_t xi_base) {
+    const uint4 id = __ldg(&c.tet_packed[t]);
+    const float4 a = __ldg(&s.dm0[t]);
+    const float4 b = __ldg(&s.dm1[t]);
+    const float4 cc = __ldg(&s.dm2[t]);
+    const uint32_t a0 = vaddr(id.x, xi_base), a1 = vaddr(id.y, xi_base), a2 = vaddr(id.z, xi_base),
+                   a3 = vaddr(id.w, xi_base);
+    float4 q0 = ld_dsmem(a0), q1 = ld_dsmem(a1), q2 = ld_dsmem(a2), q3 = ld_dsmem(a3);
+    const float w[4] = {q0.w, q1.w, q2.w, q3.w};
+    const f3 x0 = mk(q0), x1 = mk(q1), x2 = mk(q2), x3 = mk(q3);
+    const f3 r0 = mk(a), r1 = mk(b), r2 = mk(cc);
+    f3 dx[4];
+    bool moved = false;
+    if (!snh) {
+        TetEval e;
+        stvk_eval(x0, x1, x2, x3, r0, r1, r2, a.w, b.w, cc.w, e);
+        const float lacc = first ? 0.0f : s.lam0[t];
+        float gd = 0.0f;
+        if (p.stvk_damping) {
+            // xn of the tet's vertices: the global copy holds the frame-start
+            // state only, so damping uses the per-slice xn (same packed ids)
+            const float4 n0 = ld_dsmem(a0 + c.xn_minus_xi), n1 = ld_dsmem(a1 + c.xn_minus_xi),
+                         n2 = ld_dsmem(a2 + c.xn_minus_xi), n3 = ld_dsmem(a3 + c.xn_minus_xi);
+            gd = -(dot(e.g[0], x0 - mk(n0)) + dot(e.g[1], x1 - mk(n1)) + dot(e.g[2], x2 - mk(n2)) +
+                   dot(e.g[3], x3 - mk(n3)));
+        }
+        const float dl = stvk_dlambda(e, w, lacc, p.stvk_alpha_tilde, p.stvk_gamma, gd);
+        s.lam0[t] = lacc + dl;
+        if (dl != 0.0f) {
+            moved = true;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dx[i] = e.g[i] * (w[i] * dl);
+        }
+    } else {
+        float lD = first ? 0.0f : s.lam0[t];
+        float lH = first ? 0.0f : s.lam1[t];
+        float dlD, dlH;
+        if (snh_step(x0, x1, x2, x3, r0, r1, r2, fabsf(a.w), b.w, cc.w, p.inv_dt2, w, lD, lH, dx, dlD, dlH)) {
+            lD += dlD;
+            lH += dlH;
+            moved = true;
+        }
+        s.lam0[t] = lD;
+        s.lam1[t] = lH;
+    }
+    if (moved) {
+        q0.x += dx[0].x; q0.y += dx[0].y; q0.z += dx[0].z;
+        q1.x += dx[1].x; q1.y += dx[1].y; q1.z += dx[1].z;
+        q2.x += dx[2].x; q2.y += dx[2].y; q2.z += dx[2].z;
+        q3.x += dx[3].x; q3.y += dx[3].y; q3.z += dx[3].z;
+        st_dsmem(a0, q0);
+        st_dsmem(a1, q1);
+        st_dsmem(a2, q2);
+        st_dsmem(a3, q3);
+    }
+}
+
+// Shared memory per CTA: xi[slice], xn[slice], v[slice] (float4 each),
+// contact records rec[slice * n_planes] (q.xyz, lambda; q.x = NaN when the
+// vertex has no contact with that plane), their slots in the global contact
+// list gidx[slice * n_planes], and the CTA's contact vertex list clist[slice].
+__global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, ClusterDev c, StepParams p,
+                                                                     double t0) {
+    extern __shared__ float4 sm[];
+    const uint32_t rank = cl_rank();
+    const uint32_t C = c.cluster_size;
+    const uint32_t slice = c.slice;
+    float4* xi = sm;
+    float4* xn = sm + slice;
+    float4* vv = sm + 2 * slice;
+    const int S = p.n_planes + (c.body ? 1 : 0);   // contact slots per vertex: planes, then body
+    float4* rec = sm + 3 * slice;
+    float4* bn = rec + (size_t)slice * S;          // body contact normals (when c.body)
+    uint32_t* gidx = reinterpret_cast<uint32_t*>(bn + (c.body ? slice : 0));
+    uint32_t* clist = gidx + (size_t)slice * S;
+    __shared__ uint32_t s_ncont;
+    const uint32_t xi_base = smem_addr(xi);
+    const uint32_t ctid = rank * blockDim.x + threadIdx.x, nct = C * blockDim.x;
+
+    for (uint32_t g = cl_id(); g < c.n_groups; g += cl_count()) {
+        const GroupDesc gd = c.groups[g];
+        const uint32_t own0 = gd.v0 + rank * slice;
+        const uint32_t own1 = min(gd.v0 + (rank + 1) * slice, gd.v0 + gd.nv);
+        const uint32_t nown = own1 > own0 ? own1 - own0 : 0;
+        if (threadIdx.x == 0) s_ncont = 0;
+        __syncthreads();
+        // load own slice; ground contacts of own surface vertices from the
+        // frame-start positions (bvh_model.cpp:72-94 with the plane SDF)
+        for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+            const uint32_t gv = own0 + i;
+            const float4 x = s.xn[gv];
+            xn[i] = x;
+            xi[i] = x;
+            vv[i] = s.v[gv];
+            bool any = false;
+            const bool surf = (c.vflags[gv] & 1u) != 0;
+            for (int pl = 0; pl < p.n_planes; ++pl) {
+                const Plane P = p.planes[pl];
+                const float sd = P.nx * x.x + P.ny * x.y + P.nz * x.z + P.d;
+                float4 r = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+                if (surf && sd < 0.0f) {
+                    const float ad = fabsf(sd);
+                    r = make_float4(x.x + P.nx * ad, x.y + P.ny * ad, x.z + P.nz * ad, 0.0f);
+                    any = true;
+                    // publish in the frame's global contact list (introspection, residual)
+                    const uint32_t slot = atomicAdd(&s.counters[pl], 1u);
+                    gidx[(size_t)i * S + pl] = slot;
+                    if (slot < s.n_surf) {
+                        Contact ct;
+                        ct.q = make_float4(r.x, r.y, r.z, __uint_as_float(gv));
+                        ct.n = make_float4(P.nx, P.ny, P.nz, 0.0f);
+                        s.contacts[(size_t)pl * s.n_surf + slot] = ct;
+                    }
+                }
+                rec[(size_t)i * S + pl] = r;
+            }
+            if (c.body) {
+                // body-body contact found by the spatial hash for this vertex
+                const float4 bq = c.bc_q[gv];
+                float4 r = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+                if (bq.w != 0.0f) {
+                    const float4 nn = c.bc_n[gv];
+                    r = make_float4(bq.x, bq.y, bq.z, 0.0f);
+                    bn[i] = nn;
+                    gidx[(size_t)i * S + p.n_planes] = __float_as_uint(nn.w);
+                    any = true;
+                }
+                rec[(size_t)i * S + p.n_planes] = r;
+            }
+            if (any) clist[atomicAdd(&s_ncont, 1u)] = i;
+        }
+        cluster_sync();
+        const uint32_t ncont = s_ncont;
+        double t = t0;
+        for (int sub = 0; sub < p.substeps; ++sub) {
+            const double t_next = t + p.dt_d;
+            // prediction of own vertices (timestep.cpp:35-43) + prescribed motion
+            for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+                float4 v = vv[i];
+                const float4 x = xn[i];
+                if (v.w != 0.0f) {
+                    const KinGroup k = p.kin[(int)v.w - 1];
+                    const float4 rel = s.acc[own0 + i];
+                    float sn, cs;
+                    sincosf((float)(k.omega * t_next), &sn, &cs);
+                    const f3 ax = mk(k.ax, k.ay, k.az), r = mk(rel.x, rel.y, rel.z);
+                    const f3 rr = r * cs + cross(ax, r) * sn + ax * (dot(ax, r) * (1.0f - cs));
+                    xi[i] = make_float4(k.cx + rr.x, k.cy + rr.y, k.cz + rr.z, x.w);
+                    continue;
+                }
+                const float w = x.w;
+                float ax = 0.f, ay = 0.f, az = 0.f;
+                if (w > 0.0f) {
+                    if (p.gravity_mode == 1) { ax = p.gx * w; ay = p.gy * w; az = p.gz * w; }
+                    else { ax = p.gx; ay = p.gy; az = p.gz; }
+                    if (p.has_acc) {
+                        const float4 e = s.acc[own0 + i];
+                        ax += e.x; ay += e.y; az += e.z;
+                    }
+                }
+                v.x += ax * p.dt;
+                v.y += ay * p.dt;
+                v.z += az * p.dt;
+                vv[i] = v;
+                xi[i] = make_float4(x.x + v.x * p.dt, x.y + v.y * p.dt, x.z + v.z * p.dt, w);
+            }
+            cluster_sync();
+            for (int it = 0; it < p.iterations; ++it) {
+                const bool first = it == 0;
+                // contacts: own vertices only (collision_constraint.cpp:21-41)
+                for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
+                    const uint32_t i = clist[k];
+                    float4 x = xi[i];
+                    for (int sl = 0; sl < S; ++sl) {
+                        float4 r = rec[(size_t)i * S + sl];
+                        if (isnan(r.x)) continue;
+                        if (first) r.w = 0.0f;
+                        float nx, ny, nz;
+                        if (sl < p.n_planes) {
+                            nx = p.planes[sl].nx; ny = p.planes[sl].ny; nz = p.planes[sl].nz;
+                        } else {
+                            const float4 nn = bn[i];
+                            nx = nn.x; ny = nn.y; nz = nn.z;
+                        }
+                        const float C_ = (x.x - r.x) * nx + (x.y - r.y) * ny + (x.z - r.z) * nz;
+                        if (C_ < 0.0f) {
+                            const float w = x.w;
+                            const float dl = -(C_ + p.contact_alpha_tilde * r.w) / (w + p.contact_alpha_tilde);
+                            r.w += dl;
+                            x.x += w * nx * dl;
+                            x.y += w * ny * dl;
+                            x.z += w * nz * dl;
+                        }
+                        rec[(size_t)i * S + sl] = r;
+                    }
+                    xi[i] = x;
+                }
+                if (S > 0) cluster_sync();  // cluster-uniform condition
+                for (uint32_t col = 0; col < gd.n_col; ++col) {
+                    const uint32_t b = c.col_start[gd.col_base + col], e = c.col_start[gd.col_base + col + 1];
+                    const uint32_t m = c.col_split[gd.col_base + col];
+                    for (uint32_t tt = b + ctid; tt < e; tt += nct)
+                        project_tet_dsmem(s, c, p, tt, tt >= m, first, xi_base);
+                    cluster_sync();
+                }
+            }
+            // velocity update of own vertices (timestep.cpp:48-57)
+            for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+                const float4 a = xi[i];
+                const float4 b = xn[i];
+                float4 v = vv[i];
+                v.x = (a.x - b.x) * p.inv_dt;
+                v.y = (a.y - b.y) * p.inv_dt;
+                v.z = (a.z - b.z) * p.inv_dt;
+                vv[i] = v;
+                xn[i] = a;
+            }
+            t = t_next;
+            __syncthreads();
+        }
+        // write back the slice and the contact multipliers of the last substep
+        for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+            const uint32_t gv = own0 + i;
+            s.xi[gv] = xi[i];
+            s.xn[gv] = xn[i];
+            s.v[gv] = vv[i];
+        }
+        for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
+            const uint32_t i = clist[k];
+            for (int sl = 0; sl < S; ++sl) {
+                const float4 r = rec[(size_t)i * S + sl];
+                const uint32_t slot = gidx[(size_t)i * S + sl];
+                const size_t seg = sl < p.n_planes ? (size_t)sl : (size_t)kMaxPlanes;
+                if (!isnan(r.x) && slot < s.n_surf) s.contact_lam[seg * s.n_surf + slot] = r.w;
+            }
+        }
+        __syncthreads();
+    }
+    // no CTA may leave while a peer could still read its shared memory
+    cluster_sync();
+}
+
+cudaError_t cluster_configure(int block, size_t smem) {
+    cudaError_t e = cudaFuncSetAttribute(k_cluster_frame, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_cluster_frame, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t cluster_max_active(int cluster_size, int block, size_t smem, int* n) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cluster_size);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster_size;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaOccupancyMaxActiveClusters(n, (void*)k_cluster_frame, &cfg);
+}
+
+cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const StepParams& p, double t0,
+                                 int n_clusters, int block, size_t smem, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(n_clusters * c.cluster_size);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = c.cluster_size;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_cluster_frame, s, c, p, t0);
+}
+
+__global__ void k_store_time(double* t, double v) { *t = v; }
+
+cudaError_t launch_store_time(double* t, double v, cudaStream_t st) {
+    k_store_time<<<1, 1, 0, st>>>(t, v);
+    return cudaGetLastError();
+}
+
+}  // namespace sbs

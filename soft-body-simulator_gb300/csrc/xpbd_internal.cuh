@@ -38,6 +38,7 @@ struct SceneDev {
     float4* dm2;   // DmInv row 2, w = Lame lambda
     float* lam0;   // StVK multiplier / SNH deviatoric multiplier
     float* lam1;   // SNH hydrostatic multiplier
+    uint8_t* model; // per slot: 0 StVK, 1 SNH (residual kernel)
     uint32_t n_tets;
     // surface and contacts
     uint32_t* surf;
@@ -92,6 +93,7 @@ struct StepParams {
 cudaError_t launch_detect_ground(const SceneDev& s, const StepParams& p, cudaStream_t st);
 cudaError_t launch_predict(const SceneDev& s, const StepParams& p, int substep, cudaStream_t st);
 cudaError_t launch_contacts(const SceneDev& s, const StepParams& p, int first_iter, cudaStream_t st);
+cudaError_t launch_body_contacts(const SceneDev& s, const StepParams& p, int first_iter, cudaStream_t st);
 cudaError_t launch_colour(const SceneDev& s, const StepParams& p, int colour, int first_iter, int block,
                           int grid, cudaStream_t st);
 cudaError_t launch_tail(const SceneDev& s, const StepParams& p, int first_iter, int block, cudaStream_t st);

@@ -300,6 +300,13 @@ __global__ void k_contacts(SceneDev s, StepParams p, int first) {
     }
 }
 
+// Body-body contacts of the frame (after the ground contacts, as they follow
+// them in the collision constraint list).
+__global__ void k_contacts_body(SceneDev s, StepParams p, int first) {
+    const uint32_t cnt = min(s.counters[kMaxPlanes], s.n_surf);
+    contact_phase(s, (uint32_t)kMaxPlanes * s.n_surf, cnt, p, first != 0);
+}
+
 __global__ void k_colour(SceneDev s, StepParams p, int col, int first) { colour_phase(s, p, col, first != 0); }
 
 __global__ void k_tail(SceneDev s, StepParams p, int first) { tail_phase(s, p, first != 0); }
@@ -337,6 +344,7 @@ __global__ void __launch_bounds__(512) k_frame(SceneDev s, StepParams p, int has
     if (!grid_barrier(s.bar, s.err)) return;
     uint32_t cnt[kMaxPlanes];
     for (int pl = 0; pl < kMaxPlanes; ++pl) cnt[pl] = pl < p.n_planes ? min(__ldcg(&s.counters[pl]), s.n_surf) : 0u;
+    const uint32_t cnt_body = p.body_contacts ? min(__ldcg(&s.counters[kMaxPlanes]), s.n_surf) : 0u;
     for (int sub = 0; sub < p.substeps; ++sub) {
         const double t_next = t + p.dt_d;
         for_each_vertex(s.n_verts, [&](uint32_t i) { predict_vertex(s, p, i, t_next, has_acc); });
@@ -346,6 +354,10 @@ __global__ void __launch_bounds__(512) k_frame(SceneDev s, StepParams p, int has
             for (int pl = 0; pl < p.n_planes; ++pl) {
                 if (cnt[pl] == 0) continue;
                 contact_phase(s, (uint32_t)pl * s.n_surf, cnt[pl], p, first);
+                if (!grid_barrier(s.bar, s.err)) return;
+            }
+            if (cnt_body) {
+                contact_phase(s, (uint32_t)kMaxPlanes * s.n_surf, cnt_body, p, first);
                 if (!grid_barrier(s.bar, s.err)) return;
             }
             for (int col = 0; col < p.first_tail; ++col) {
@@ -415,10 +427,7 @@ __global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
         const uint4 id = s.tet[t];
         const float4 a = s.dm0[t], b = s.dm1[t], c = s.dm2[t];
         const f3 x0 = mk(s.xi[id.x]), x1 = mk(s.xi[id.y]), x2 = mk(s.xi[id.z]), x3 = mk(s.xi[id.w]);
-        // tets at or past the split of their colour are SNH; find the colour by scan
-        int col = 0;
-        while (col + 1 < p.n_colours && t >= p.colour_start[col + 1]) ++col;
-        const bool snh = t >= p.colour_split[col];
+        const bool snh = s.model[t] != 0;
         if (!snh) {
             TetEval e;
             stvk_eval(x0, x1, x2, x3, mk(a), mk(b), mk(c), a.w, b.w, c.w, e);
@@ -433,7 +442,9 @@ __global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
             en.add(E);
         }
     }
-    for (int pl = 0; pl < p.n_planes; ++pl) {
+    for (int pl = 0; pl <= kMaxPlanes; ++pl) {
+        // planes, then the body-contact segment (index kMaxPlanes)
+        if (pl < kMaxPlanes && pl >= p.n_planes) continue;
         const uint32_t cnt = min(s.counters[cnt_base + pl], s.n_surf);
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += stride) {
             const uint32_t ci = (uint32_t)pl * s.n_surf + k;
@@ -495,6 +506,12 @@ cudaError_t launch_contacts(const SceneDev& s, const StepParams& p, int first_it
     if (p.n_planes == 0 || s.n_surf == 0) return cudaSuccess;
     const int grid = p.n_planes > 1 ? 1 : grid_for(s.n_surf, 256, 1024);
     k_contacts<<<grid, 256, 0, st>>>(s, p, first_iter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_body_contacts(const SceneDev& s, const StepParams& p, int first_iter, cudaStream_t st) {
+    if (!p.body_contacts || s.n_surf == 0) return cudaSuccess;
+    k_contacts_body<<<grid_for(s.n_surf, 256, 1024), 256, 0, st>>>(s, p, first_iter);
     return cudaGetLastError();
 }
 

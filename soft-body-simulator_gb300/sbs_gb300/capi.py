@@ -14,7 +14,7 @@ import numpy as np
 from . import build as _build
 
 SBS_OK, SBS_EINVAL, SBS_ECUDA, SBS_ETIMEOUT, SBS_ENAN, SBS_ESTATE, SBS_ENOMEM, SBS_ECOLOUR = range(8)
-EXEC_AUTO, EXEC_GRAPH, EXEC_PERSISTENT = 0, 1, 2
+EXEC_AUTO, EXEC_GRAPH, EXEC_PERSISTENT, EXEC_CLUSTER = 0, 1, 2, 3
 GRAVITY_ACCELERATION, GRAVITY_FORCE = 0, 1
 
 HEADER = _build.INCLUDE / "sbs_gpu.h"
@@ -32,7 +32,7 @@ class Params(C.Structure):
                 ("gravity_mode", C.c_int32), ("device", C.c_int32), ("exec_mode", C.c_int32),
                 ("block_size", C.c_int32), ("ctas_per_sm", C.c_int32),
                 ("tail_threshold", C.c_int32), ("body_contacts", C.c_int32),
-                ("hash_cell", C.c_float), ("max_body_contacts", C.c_uint32),
+                ("hash_cell", C.c_float), ("candidate_capacity", C.c_uint32),
                 ("check_finite", C.c_int32)]
 
 
@@ -100,6 +100,7 @@ def load(build: bool = True):
         "sbs_gpu_destroy": [P],
         "sbs_gpu_plan_sweep": [f64, C.c_uint32, u32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_get_candidates": [P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -161,7 +162,8 @@ class Solver:
         self.scene = scene
         kw = dict(compliance=scene.compliance, damping=scene.damping,
                   collision_compliance=scene.collision_compliance, gravity=scene.gravity,
-                  gravity_mode=scene.gravity_mode)
+                  gravity_mode=scene.gravity_mode, body_contacts=int(scene.body_contacts),
+                  hash_cell=float(scene.hash_cell))
         kw.update(param_overrides)
         prm = default_params(**kw)
         h = C.c_void_p()
@@ -174,8 +176,9 @@ class Solver:
             tets = np.ascontiguousarray(b.tets, np.uint32).ravel()
             mat = Material(b.model, b.young, b.poisson, b.density)
             bid = C.c_int32()
+            mass = None if b.mass is None else np.ascontiguousarray(b.mass, np.float64)
             self._check(L.sbs_gpu_add_body(h, x0, _ptr(xi), len(b.x0), tets, len(b.tets),
-                                           C.byref(mat), None, C.byref(bid)))
+                                           C.byref(mat), _ptr(mass), C.byref(bid)))
             if len(b.pinned):
                 self._check(L.sbs_gpu_pin_vertices(h, bid, np.ascontiguousarray(b.pinned, np.uint32),
                                                    len(b.pinned)))
@@ -297,6 +300,14 @@ class Solver:
         self._check(self.L.sbs_gpu_get_contacts(self.h, v.ctypes.data, qn.ctypes.data, n.value,
                                                 C.byref(n)))
         return v, qn.reshape(-1, 6)
+
+    def candidates(self) -> np.ndarray:
+        """Broad-phase (vertex << 32 | tet) pairs of the last detection, sorted."""
+        n = C.c_uint64()
+        self._check(self.L.sbs_gpu_get_candidates(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.uint64)
+        self._check(self.L.sbs_gpu_get_candidates(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out
 
     def inv_masses(self) -> np.ndarray:
         out = np.zeros(self.scene.n_verts, np.float32)

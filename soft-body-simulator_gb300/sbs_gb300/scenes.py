@@ -178,6 +178,7 @@ class Body:
     kin_axis: tuple = (1.0, 0.0, 0.0)
     kin_omega: float = 0.0
     ext_acc: np.ndarray | None = None  # [V,3] external acceleration field
+    mass: np.ndarray | None = None     # [V] per-vertex masses (None: lumped from density)
 
 
 @dataclass

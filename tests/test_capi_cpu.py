@@ -1,0 +1,86 @@
+"""C-ABI library without a GPU: it builds, loads, exports every declared
+symbol, plans sweeps on the host, and fails loudly instead of falling back."""
+import ctypes as C
+import subprocess
+
+import numpy as np
+import pytest
+
+from sbs_gb300 import capi, scenes
+
+
+def test_exports_every_declared_symbol():
+    L = capi.load()
+    names = capi.declared_symbols()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing
+
+
+def test_nm_lists_declared_symbols():
+    from sbs_gb300 import build
+    out = subprocess.run(["nm", "-D", "--defined-only", str(build.LIB)], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    assert set(capi.declared_symbols()) <= exported
+
+
+def test_params_default_follow_reference_parameters():
+    p = capi.default_params()
+    # simulation_parameters.h:12-27
+    assert p.compliance == 1e-4 and p.damping == 0.0 and p.collision_compliance == 1e-8
+    assert tuple(p.gravity) == (0.0, -9.81, 0.0)
+
+
+def test_create_without_gpu_fails_loudly():
+    pytest.importorskip("torch")
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    L = capi.load()
+    h = C.c_void_p()
+    p = capi.default_params()
+    assert L.sbs_gpu_create(C.byref(p), C.byref(h)) == capi.SBS_ECUDA
+    with pytest.raises(capi.SbsError):
+        capi.Solver(scenes.beam_c1())
+
+
+def test_plan_sweep_is_a_valid_colouring():
+    for sc in (scenes.beam_c1(), scenes.beam_twist(16, 8, 8, 0.05)):
+        order, off = capi.plan_sweep(sc)
+        t = sc.bodies[0].tets
+        assert np.array_equal(np.sort(order), np.arange(len(t)))
+        sizes = np.diff(off)
+        assert np.all(sizes[:-1] >= sizes[1:])          # colours by decreasing size
+        for c in range(len(off) - 1):
+            v = t[order[off[c]:off[c + 1]]].ravel()
+            assert len(np.unique(v)) == len(v)
+
+
+def test_plan_sweep_colour_count_98k_beam():
+    order, off = capi.plan_sweep(scenes.beam_twist())
+    # interior vertices of the 6-tet split touch 24 tets: at least 24 colours
+    assert 24 <= len(off) - 1 <= 40
+
+
+def test_plan_sweep_rejects_bad_indices():
+    L = capi.load()
+    x0 = np.zeros(12)
+    tets = np.array([0, 1, 2, 7], np.uint32)
+    n = C.c_uint32()
+    assert L.sbs_gpu_plan_sweep(x0, 4, tets, 1, None, None, None, 0, C.byref(n)) == capi.SBS_EINVAL
+
+
+def test_golden_fixtures_reproduce(oracle_mod):
+    from pathlib import Path
+    from golden.make_golden import golden_scene, NAMES
+    d = np.load(Path(__file__).parent / "golden" / "ref_meshes.npz")
+    for name in NAMES:
+        sc = golden_scene(d[f"{name}_x0"], d[f"{name}_tets"])
+        order, off = capi.plan_sweep(sc)
+        o = oracle_mod.Oracle(sc)
+        o.set_order(order, off)
+        o.step(1)
+        assert np.array_equal(o.get(), d[f"{name}_x1"])
+        o.step(9)
+        assert np.array_equal(o.get(), d[f"{name}_x10"])

@@ -1,0 +1,314 @@
+"""GPU kernels (through the C ABI) against the FP64 oracle running the same
+Gauss-Seidel sweep order.
+
+Tolerances.  One sweep from an identical state must agree to 2e-5 of the
+bounding-box diagonal (FP32 arithmetic: measured 1.6e-6 .. 3.9e-6).  Over
+whole frames the sequential loop amplifies rounding differences (a 1e-12 m
+perturbation grows to 1e-4 m within a frame of the 450-tet beam, see
+test_oracle.py), so multi-frame positions are compared against the oracle's
+own noise floor: the spread between the oracle and the oracle restarted from
+FP32-rounded initial positions.
+"""
+import numpy as np
+import pytest
+
+from conftest import make_pair
+from sbs_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+SWEEP_TOL = 2e-5
+
+
+def sync_from_oracle(g, o, oracle):
+    """Copy the oracle's state, rounded to FP32, into both solvers."""
+    x = o.get().astype(np.float32).astype(np.float64)
+    v = o.get(oracle.FIELD_V).astype(np.float32).astype(np.float64)
+    o.set(oracle.FIELD_X, x)
+    o.set(oracle.FIELD_V, v)
+    off = 0
+    for b, n in enumerate(g.body_sizes):
+        g.set_state(b, x[off:off + n], v[off:off + n])
+        off += n
+
+
+def sweeps(g, o, oracle, dt, k):
+    o.L.orc_detect_contacts(o.h)
+    o.L.orc_predict(o.h, dt)
+    o.L.orc_solve(o.h, dt, k)
+    g.detect_contacts()
+    g.predict(dt)
+    g.solve(dt, k)
+    return g.get_predicted(0).astype(np.float64), o.get(oracle.FIELD_XI)
+
+
+def noise_floor(scene, oracle, frames, seed=0):
+    from sbs_gb300 import capi
+    order, off = capi.plan_sweep(scene)
+    return oracle.noise_floor(scene, frames, order, off, seed)
+
+
+@pytest.mark.parametrize("pre", [0, 5])
+def test_one_sweep_stvk(capi_mod, oracle_mod, pre):
+    sc = scenes.beam_c1()
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    g.step(pre)
+    o.step(pre)
+    sync_from_oracle(g, o, oracle_mod)
+    xg, xo = sweeps(g, o, oracle_mod, sc.frame_dt, 1)
+    assert np.abs(xg - xo).max() / sc.bbox_diag() < SWEEP_TOL
+    lg, lo = g.lambdas()[:, 0], o.lambdas()[:, 0]
+    assert np.abs(lg - lo).max() <= 1e-2 * np.abs(lo).max()
+
+
+def test_one_sweep_snh_twist(capi_mod, oracle_mod):
+    sc = scenes.beam_twist(16, 4, 4, 0.05)
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    g.step(2)
+    o.step(2)
+    sync_from_oracle(g, o, oracle_mod)
+    xg, xo = sweeps(g, o, oracle_mod, sc.frame_dt / sc.substeps, 1)
+    assert np.abs(xg - xo).max() / sc.bbox_diag() < SWEEP_TOL
+    lg, lo = g.lambdas(), o.lambdas()
+    assert np.abs(lg - lo).max() <= 1e-2 * np.abs(lo).max()
+
+
+def test_one_sweep_with_contacts(capi_mod, oracle_mod):
+    sc = scenes.beam_c1()
+    sc.ground = ((0.0, 1.0, 0.0), -0.15)   # plane y = 0.15 cuts the beam
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    xg, xo = sweeps(g, o, oracle_mod, sc.frame_dt, 1)
+    assert np.abs(xg - xo).max() / sc.bbox_diag() < SWEEP_TOL
+
+
+def test_contact_set_is_identical(capi_mod, oracle_mod):
+    sc = scenes.beam_c1()
+    sc.ground = ((0.0, 1.0, 0.0), -0.15)
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    g.detect_contacts()
+    vg, qg = g.contacts()
+    vo, qo = o.detect_contacts()
+    assert len(vo) > 0
+    assert np.array_equal(vg, vo)          # both sorted by (plane, vertex)
+    assert np.abs(qg - qo).max() < 1e-6
+
+
+def test_contact_sets_after_frames(capi_mod, oracle_mod):
+    # the beam sags onto a raised ground: compare the frame's contact set on
+    # identical (synchronised) states
+    sc = scenes.beam_c1()
+    sc.ground = ((0.0, 1.0, 0.0), 0.02)
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    for _ in range(6):
+        g.step(1)
+        o.step(1)
+        sync_from_oracle(g, o, oracle_mod)
+        g.detect_contacts()
+        vg, _ = g.contacts()
+        vo, _ = o.detect_contacts()
+        assert np.array_equal(vg, vo)
+
+
+@pytest.mark.parametrize("name", ["tetrahedron", "2tets", "3tets", "cube_tet", "tet_bar_5x2x2",
+                                  "bar_tet"])
+def test_reference_meshes_first_frame(capi_mod, oracle_mod, name):
+    from golden.make_golden import golden_scene
+    d = np.load(__import__("pathlib").Path(__file__).parent / "golden" / "ref_meshes.npz")
+    sc = golden_scene(d[f"{name}_x0"], d[f"{name}_tets"])
+    g = capi_mod.Solver(sc)
+    g.step(1)
+    err = np.abs(g.positions() - d[f"{name}_x1"]).max() / sc.bbox_diag()
+    floor = noise_floor(sc, oracle_mod, 1) / sc.bbox_diag()
+    assert err < max(20 * floor, SWEEP_TOL)
+
+
+def test_beam450_frames_within_noise_floor(capi_mod, oracle_mod):
+    sc = scenes.beam_c1()
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    g.step(1)
+    o.step(1)
+    err = float(np.abs(g.positions() - o.get()).max())
+    floor = noise_floor(sc, oracle_mod, 1)
+    assert err < 20 * floor + 1e-7
+
+
+def test_beam98k_first_frame(capi_mod, oracle_mod):
+    sc = scenes.beam_twist()
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    g.step(1)
+    o.step(1)
+    x = g.positions()
+    assert np.all(np.isfinite(x))
+    err = float(np.abs(x - o.get()).max()) / sc.bbox_diag()
+    assert err < 1e-3
+    b = sc.bodies[0]
+    assert np.array_equal(x[b.pinned], b.x0[b.pinned].astype(np.float32))
+
+
+def test_kinematic_face_follows_rotation(capi_mod):
+    sc = scenes.beam_twist(16, 4, 4, 0.05)
+    g = capi_mod.Solver(sc)
+    g.step(10)
+    b = sc.bodies[0]
+    ang = b.kin_omega * 10 * sc.frame_dt
+    R = np.array([[1, 0, 0], [0, np.cos(ang), -np.sin(ang)], [0, np.sin(ang), np.cos(ang)]])
+    c = np.array(b.kin_center)
+    want = (b.x0[b.kin_verts] - c) @ R.T + c
+    assert np.abs(g.positions()[b.kin_verts] - want).max() < 1e-6
+
+
+def test_masses_and_surface(capi_mod, oracle_mod):
+    sc = scenes.beam_twist(8, 3, 3, 0.05)
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    m = o.masses()
+    w = np.where(m > 0, 1.0 / np.where(m > 0, m, 1), 0.0)
+    assert np.allclose(g.inv_masses(), w, rtol=1e-6)
+    assert np.array_equal(g.surface(), o.surface())
+
+
+def test_colouring_is_a_valid_sweep(capi_mod):
+    sc = scenes.beam_twist()
+    g = capi_mod.Solver(sc)
+    order, off = g.tet_order()
+    assert np.array_equal(np.sort(order), np.arange(sc.n_tets))
+    t = sc.bodies[0].tets
+    for c in range(len(off) - 1):
+        v = t[order[off[c]:off[c + 1]]].ravel()
+        assert len(np.unique(v)) == len(v)
+    po, poff = capi_mod.plan_sweep(sc)
+    assert np.array_equal(po, order) and np.array_equal(poff, off)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_deterministic(capi_mod, mode):
+    sc = scenes.beam_twist(16, 4, 4, 0.05)
+    a = capi_mod.Solver(sc, exec_mode=mode)
+    b = capi_mod.Solver(sc, exec_mode=mode)
+    a.step(5)
+    b.step(5)
+    assert np.array_equal(a.positions(), b.positions())
+
+
+def test_graph_and_persistent_agree(capi_mod, oracle_mod):
+    sc = scenes.beam_c1()
+    a = capi_mod.Solver(sc, exec_mode=1)
+    b = capi_mod.Solver(sc, exec_mode=2)
+    a.step(1)
+    b.step(1)
+    floor = noise_floor(sc, oracle_mod, 1)
+    assert np.abs(a.positions() - b.positions()).max() < 20 * floor + 1e-7
+
+
+def test_residual_matches_oracle(capi_mod, oracle_mod):
+    for sc in (scenes.beam_c1(), scenes.beam_twist(16, 4, 4, 0.05)):
+        g, o = make_pair(sc, capi_mod, oracle_mod)
+        g.step(2)
+        o.step(2)
+        sync_from_oracle(g, o, oracle_mod)
+        dt = sc.frame_dt / sc.substeps
+        sweeps(g, o, oracle_mod, dt, 1)
+        r, e = g.residual(dt)
+        ro = np.zeros(3)
+        o.L.orc_residual(o.h, dt, ro)
+        assert r == pytest.approx(ro[0], rel=1e-3)
+        assert e == pytest.approx(ro[1], rel=1e-3)
+
+
+def test_residual_kahan_on_large_mesh(capi_mod, oracle_mod):
+    # 98k tets: the compensated FP32 sums agree with the FP64 oracle
+    sc = scenes.beam_twist()
+    g, o = make_pair(sc, capi_mod, oracle_mod)
+    dt = sc.frame_dt / sc.substeps
+    xg, xo = sweeps(g, o, oracle_mod, dt, 1)
+    g.set_predicted(0, xo)
+    r, e = g.residual(dt)
+    ro = np.zeros(3)
+    o.L.orc_residual(o.h, dt, ro)
+    assert r == pytest.approx(ro[0], rel=1e-3)
+    assert e == pytest.approx(ro[1], rel=1e-3)
+
+
+def test_invalid_arguments(capi_mod):
+    import ctypes as C
+    L = capi_mod.load()
+    h = C.c_void_p()
+    p = capi_mod.default_params()
+    assert L.sbs_gpu_create(C.byref(p), C.byref(h)) == capi_mod.SBS_OK
+    x0 = np.zeros(12)
+    x0[3], x0[7], x0[11] = 1, 1, 1
+    tets_bad = np.array([0, 1, 2, 9], np.uint32)
+    mat = capi_mod.Material(0, 1e5, 0.3, 1000)
+    bid = C.c_int32()
+    assert L.sbs_gpu_add_body(h, x0, None, 4, tets_bad, 1, C.byref(mat), None,
+                              C.byref(bid)) == capi_mod.SBS_EINVAL
+    assert L.sbs_gpu_step(h, 1 / 60, 1, 1) == capi_mod.SBS_ESTATE
+    assert L.sbs_gpu_finalize(h) == capi_mod.SBS_ESTATE   # no bodies
+    tets = np.array([0, 1, 2, 3], np.uint32)
+    assert L.sbs_gpu_add_body(h, x0, None, 4, tets, 1, C.byref(mat), None,
+                              C.byref(bid)) == capi_mod.SBS_OK
+    assert L.sbs_gpu_pin_vertices(h, 5, tets, 1) == capi_mod.SBS_EINVAL
+    assert L.sbs_gpu_finalize(h) == capi_mod.SBS_OK
+    assert L.sbs_gpu_step(h, -1.0, 1, 1) == capi_mod.SBS_EINVAL
+    xbad = np.full(12, np.nan, np.float32)
+    assert L.sbs_gpu_set_state(h, 0, xbad.ctypes.data, None) == capi_mod.SBS_EINVAL
+    assert L.sbs_gpu_destroy(h) == capi_mod.SBS_OK
+
+
+# --- cluster-resident mode -------------------------------------------------
+
+@pytest.mark.parametrize("make", [lambda: scenes.beam_c1(),
+                                  lambda: scenes.beam_twist(16, 4, 4, 0.05)])
+def test_cluster_mode_one_frame(capi_mod, oracle_mod, make):
+    sc = make()
+    g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=capi_mod.EXEC_CLUSTER)
+    assert g.stats().exec_mode == capi_mod.EXEC_CLUSTER
+    g.step(1)
+    o.step(1)
+    err = float(np.abs(g.positions() - o.get()).max())
+    assert err < 20 * noise_floor(sc, oracle_mod, 1) + 1e-7
+
+
+def test_cluster_mode_contacts_and_residual(capi_mod, oracle_mod):
+    sc = scenes.beam_c1()
+    sc.ground = ((0.0, 1.0, 0.0), -0.15)
+    g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=capi_mod.EXEC_CLUSTER)
+    g.step(1)
+    o.step(1)
+    vg, _ = g.contacts()
+    # the frame's contacts come from the identical initial state
+    o2 = oracle_mod.Oracle(sc)
+    vo, _ = o2.detect_contacts()
+    assert np.array_equal(vg, vo)
+    r, e = g.residual(sc.frame_dt)
+    assert np.isfinite(r) and np.isfinite(e) and r > 0
+
+
+def _batch(n=40, seed=5):
+    sc = scenes.box_drop(n_bodies=n, seed=seed, min_cells=5, max_cells=11, arena=12.0,
+                         body_contacts=False, iterations=6, substeps=1)
+    return sc
+
+
+def test_cluster_mode_batch_of_bodies(capi_mod, oracle_mod):
+    sc = _batch()
+    g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=capi_mod.EXEC_CLUSTER)
+    order, off = g.tet_order()
+    # colour segments are vertex-disjoint, whatever the grouping
+    tets = np.concatenate([b.tets.astype(np.int64) + sum(len(bb.x0) for bb in sc.bodies[:i])
+                           for i, b in enumerate(sc.bodies)])
+    for c in range(len(off) - 1):
+        v = tets[order[off[c]:off[c + 1]]].ravel()
+        assert len(np.unique(v)) == len(v)
+    g.step(1)
+    o.step(1)
+    err = float(np.abs(g.positions() - o.get()).max())
+    assert err < 20 * oracle_mod.noise_floor(sc, 1, order, off) + 1e-7
+
+
+def test_cluster_mode_deterministic(capi_mod):
+    sc = scenes.beam_twist(16, 4, 4, 0.05)
+    a = capi_mod.Solver(sc, exec_mode=3)
+    b = capi_mod.Solver(sc, exec_mode=3)
+    a.step(4)
+    b.step(4)
+    assert np.array_equal(a.positions(), b.positions())
