@@ -214,6 +214,50 @@ sbs_status sbs_gpu_plan_sweep(const double* x0, uint32_t n_verts, const uint32_t
                               const int32_t* models, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
                               uint32_t* n_colours);
 
+/* ---- Learned warm start: per-vertex MLP 16 -> 128 -> 128 -> 128 -> 3 (SiLU),
+ * BF16 tensor-core GEMMs with FP32 accumulate, FP32 master weights, Adam.
+ * No reference counterpart (the reference always starts its sweeps from the
+ * predicted positions, timestep.cpp:35-45).  Parameters are laid out
+ * W1[128][16] b1 W2[128][128] b2 W3[128][128] b3 W4[3][128] b4 (35,587 floats).
+ * Features per vertex (16): inertial displacement xi - x (3), mean deformation
+ * gradient of incident tets, row-major (9), external acceleration (3), pin flag
+ * (1); output: displacement correction (3).  Inputs are normalised as
+ * (x - mean) / std and outputs multiplied by out_scale inside the network. */
+typedef struct sbs_mlp sbs_mlp;
+uint32_t sbs_mlp_param_count(void);
+sbs_status sbs_mlp_create(int32_t device, uint64_t seed, sbs_mlp** out);
+sbs_status sbs_mlp_destroy(sbs_mlp* m);
+const char* sbs_mlp_last_error(const sbs_mlp* m);
+sbs_status sbs_mlp_get_params(sbs_mlp* m, float* params);
+sbs_status sbs_mlp_set_params(sbs_mlp* m, const float* params);
+sbs_status sbs_mlp_set_normalization(sbs_mlp* m, const float* in_mean, const float* in_std, const float* out_scale);
+/* Host buffers: x [n*16] raw features -> y [n*3] raw outputs. */
+sbs_status sbs_mlp_forward(sbs_mlp* m, const float* x, uint32_t n, float* y);
+/* Host buffers: loss = mean over rows of ||(y - t) / out_scale||^2 and its
+ * gradient w.r.t. all parameters (for gradient checks). */
+sbs_status sbs_mlp_loss_grad(sbs_mlp* m, const float* x, const float* t, uint32_t n, float* loss, float* grad);
+/* Training set upload (host buffers x [n*16], t [n*3]) and `steps` Adam steps
+ * on random batches of `batch` rows; *loss = loss of the last batch. */
+sbs_status sbs_mlp_set_dataset(sbs_mlp* m, const float* x, const float* t, uint32_t n);
+sbs_status sbs_mlp_train(sbs_mlp* m, uint32_t steps, uint32_t batch, float lr, uint64_t seed, float* loss);
+
+/* Attaches (m != NULL) or detaches the warm-start network.  While attached,
+ * every substep of sbs_gpu_step runs predict -> features -> MLP -> one fit
+ * sweep that turns the predicted displacement into multipliers (colour order,
+ * each constraint's increment best matching the displacement still missing at
+ * its vertices) -> `iterations` sweeps continuing from those multipliers.
+ * Do not train the same network while it is attached. */
+sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m);
+/* The warm-start half of a substep on its own, after sbs_gpu_predict. */
+sbs_status sbs_gpu_warm_start_init(sbs_gpu* h, double dt);
+/* As sbs_gpu_solve; with reset_lambda = 0 the sweeps continue from the
+ * current multipliers (after sbs_gpu_warm_start_init) instead of resetting
+ * them as constraint_t::prepare_for_projection does (constraint.cpp:12-16). */
+sbs_status sbs_gpu_solve_ex(sbs_gpu* h, double dt, uint32_t iterations, int32_t reset_lambda);
+/* Features of every vertex at the current predicted state, host [16 * n_vertices]
+ * in global vertex order (training data). */
+sbs_status sbs_gpu_get_features(sbs_gpu* h, float* feat);
+
 /* Frees every device resource of the handle. */
 sbs_status sbs_gpu_destroy(sbs_gpu* h);
 

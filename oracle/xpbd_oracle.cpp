@@ -492,11 +492,11 @@ static void detect_ground(sim_t& sim) {
 // visits the cells of its AABB.  A candidate is a (surface vertex, tet) pair
 // with the vertex's cell inside the tet's cell range, the vertex not a vertex
 // of the tet, and the two from different bodies (or, with self contacts, from
-// any body).  Narrow phase: the vertex lies inside the tet (barycentric
-// coordinates >= 0); the contact is the half-space of the tet's boundary face
-// with the largest signed distance d <= 0 (the shallowest exit), frozen for
-// the frame like the reference's collision constraint: q = x - d n, outward n.
-// One contact per vertex: the largest d, ties to the lower sweep slot.
+// any body).  Narrow phase (vertex-triangle): the vertex is behind one of
+// the tet's boundary triangles by less than the cell size and projects inside
+// it; the contact is that triangle's half-space, frozen for the frame like
+// the reference's collision constraint: q = x - d n, outward n.  One contact
+// per vertex: the largest d, ties to the lower (sweep slot, face).
 
 static inline int32_t hash_cell_coord(float x, float inv_h) { return (int32_t)std::floor(x * inv_h); }
 
@@ -547,29 +547,36 @@ static void hash_candidates(const sim_t& s, const float* xf, float inv_h, int se
     }
 }
 
-// Signed distances of p to the four face planes of tet t (outward normals,
-// faces in faces_copy order); returns false if p is outside.
-static bool inside_faces(const sim_t& s, const tet_topo_t& tt, vec3 p, double d[4], vec3 n[4]) {
+// Boundary face f of tet tt as a contact plane for point p: outward unit
+// normal (oriented away from the tet's opposite vertex), signed distance d of
+// p to the plane, and whether the projection of p onto the plane falls
+// inside the triangle.
+static bool face_plane(const sim_t& s, const tet_topo_t& tt, int f, vec3 p, double& d, vec3& n) {
     static const int F[4][4] = {{0, 1, 3, 2}, {1, 2, 3, 0}, {2, 0, 3, 1}, {0, 2, 1, 3}};  // a b c opposite
-    bool inside = true;
-    for (int f = 0; f < 4; ++f) {
-        vec3 a = s.particles[tt.v[F[f][0]]].x, b = s.particles[tt.v[F[f][1]]].x, c = s.particles[tt.v[F[f][2]]].x,
-             o = s.particles[tt.v[F[f][3]]].x;
-        vec3 nn = cross(b - a, c - a);
-        double l = norm(nn);
-        if (!(l > 0)) return false;
-        nn = nn / l;
-        if (dot(nn, o - a) > 0) nn = -nn;
-        n[f] = nn;
-        d[f] = dot(p - a, nn);
-        if (d[f] > 0) inside = false;
-    }
-    return inside;
+    const vec3 a = s.particles[tt.v[F[f][0]]].x, b = s.particles[tt.v[F[f][1]]].x,
+               c = s.particles[tt.v[F[f][2]]].x, o = s.particles[tt.v[F[f][3]]].x;
+    vec3 nn = cross(b - a, c - a);
+    const double l = norm(nn);
+    if (!(l > 0)) return false;
+    nn = nn / l;
+    if (dot(nn, o - a) > 0) nn = -nn;
+    n = nn;
+    d = dot(p - a, nn);
+    const vec3 q = p - nn * d;
+    // barycentric signs of q in (a, b, c) measured along n
+    const double ua = dot(nn, cross(b - q, c - q)), ub = dot(nn, cross(c - q, a - q)),
+                 uc = dot(nn, cross(a - q, b - q));
+    return (ua >= 0 && ub >= 0 && uc >= 0) || (ua <= 0 && ub <= 0 && uc <= 0);
 }
 
+// Narrow phase of a candidate (vertex, tet): the vertex is behind a boundary
+// triangle of the tet (-h < d < 0) and projects inside it.  One contact per
+// vertex: the shallowest such triangle (largest d), ties to the lower
+// (sweep slot, face).  Contact: q = x - d n, normal n (frozen for the frame).
 static void detect_bodies(sim_t& sim) {
     if (!sim.prm.body_contacts || !(sim.prm.hash_cell > 0)) return;
     const float inv_h = (float)(1.0 / sim.prm.hash_cell);
+    const double depth = sim.prm.hash_cell;
     const uint32_t n = (uint32_t)sim.particles.size();
     std::vector<float> xf(3 * (size_t)n);
     for (uint32_t v = 0; v < n; ++v) {
@@ -579,31 +586,27 @@ static void detect_bodies(sim_t& sim) {
     }
     std::vector<std::pair<uint32_t, uint32_t>> cand;
     hash_candidates(sim, xf.data(), inv_h, sim.prm.body_contacts == 2, cand);
-    struct best_t { double d; uint32_t slot, tet; int face; };
-    std::vector<best_t> best(n, best_t{-1e300, 0xFFFFFFFFu, 0, -1});
+    struct best_t { double d; uint64_t key; vec3 n; };
+    std::vector<best_t> best(n, best_t{-1e300, ~0ull, vec3{}});
     for (auto& c : cand) {
         const tet_topo_t& tt = sim.topo[c.second];
-        double d[4]; vec3 nn[4];
-        if (!inside_faces(sim, tt, sim.particles[c.first].x, d, nn)) continue;
-        int bf = -1;
-        for (int f = 0; f < 4; ++f)
-            if ((tt.bmask >> f) & 1u)
-                if (bf < 0 || d[f] > d[bf]) bf = f;
-        if (bf < 0) continue;
-        best_t& b = best[c.first];
-        const uint32_t slot = sim.slot_of_tet[c.second];
-        if (d[bf] > b.d || (d[bf] == b.d && slot < b.slot)) b = best_t{d[bf], slot, c.second, bf};
+        const vec3 p = sim.particles[c.first].x;
+        for (int f = 0; f < 4; ++f) {
+            if (!((tt.bmask >> f) & 1u)) continue;
+            double d; vec3 nn;
+            if (!face_plane(sim, tt, f, p, d, nn)) continue;
+            if (!(d < 0.0 && d > -depth)) continue;
+            best_t& b = best[c.first];
+            const uint64_t key = ((uint64_t)sim.slot_of_tet[c.second] << 2) | (uint64_t)f;
+            if (d > b.d || (d == b.d && key < b.key)) b = best_t{d, key, nn};
+        }
     }
     uint32_t nb = 0;
     for (uint32_t v = 0; v < n; ++v) {
-        if (best[v].face < 0) continue;
-        const tet_topo_t& tt = sim.topo[best[v].tet];
-        double d[4]; vec3 nn[4];
-        inside_faces(sim, tt, sim.particles[v].x, d, nn);
-        const vec3 nf = nn[best[v].face];
-        const vec3 q = sim.particles[v].x - nf * d[best[v].face];
+        if (best[v].key == ~0ull) continue;
+        const vec3 q = sim.particles[v].x - best[v].n * best[v].d;
         sim.collision_constraints.push_back(
-            std::make_unique<collision_constraint_t>(sim.prm.collision_alpha, 0.0, v, q, nf));
+            std::make_unique<collision_constraint_t>(sim.prm.collision_alpha, 0.0, v, q, best[v].n));
         ++nb;
     }
     sim.st.n_body_contacts = nb;

@@ -21,6 +21,8 @@
 #include "xpbd_internal.cuh"
 #include "cluster_internal.cuh"
 #include "hash_internal.cuh"
+#include "mlp_internal.cuh"
+#include "warmstart_internal.cuh"
 
 using namespace sbs;
 
@@ -89,6 +91,7 @@ struct sbs_gpu {
     bool cl_feasible = false, global_modes = true;
     int cl_size = 1, cl_block = 256, cl_grid = 1;
     size_t cl_smem = 0;
+    uint32_t cl_slice = 1, cl_lcap = 1;
     std::vector<std::pair<uint32_t, uint32_t>> cl_groups;  // body ranges
     ClusterDev cd{};
     // body-body contacts
@@ -96,6 +99,10 @@ struct sbs_gpu {
     HashDev hd{};
     double hash_cell = 0.0;
     std::vector<uint8_t> bmask;        // boundary faces per tet slot
+    // learned warm start
+    sbs_mlp* mlp = nullptr;
+    WarmDev wd{};
+    bool warm_buffers = false;
     double sim_time = 0.0;   // host mirror of the simulation time
     std::vector<uint32_t> seg_split;  // first SNH slot of each colour segment
 
@@ -534,8 +541,11 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     const int P = (int)h->planes.size();
     int smem_optin = 0;
     CU(h, cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->prm.device));
-    const size_t per_v = cluster_smem_bytes(1, P, h->prm.body_contacts ? 1 : 0);
-    const uint32_t cap_slice = (uint32_t)((size_t)(smem_optin - 2048) / per_v);
+    // per vertex: its state and contact records, plus the multipliers of the
+    // tets it brings (T/V + 1 tets per vertex, 8 bytes each)
+    const size_t per_v = cluster_smem_bytes(1, P, h->prm.body_contacts ? 1 : 0, 0) +
+                         8 * ((size_t)T / std::max<uint32_t>(V, 1) + 1);
+    const uint32_t cap_slice = (uint32_t)((size_t)(smem_optin - 4096) / per_v);
     uint32_t max_body = 0;
     for (const BodyHost& b : h->bodies) max_body = std::max(max_body, b.nv);
     h->cl_size = 1;
@@ -616,6 +626,49 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
         uint32_t maxc = 0;
         for (size_t c = 0; c + 1 < gcol_start.size(); ++c) maxc = std::max(maxc, gcol_start[c + 1] - gcol_start[c]);
         while (h->cl_size < 16 && (uint64_t)h->cl_size * 256 < maxc) h->cl_size *= 2;
+    }
+    // cluster mode: give every tet to the CTA whose vertex slice holds most
+    // of its vertices (gathers then mostly hit the CTA's own shared memory);
+    // within a colour tets are reordered by owner, which leaves each
+    // colour's tet set - and so the sweep - unchanged
+    std::vector<uint32_t> crs, lbs;
+    if (h->cl_feasible) {
+        const uint32_t C = (uint32_t)h->cl_size;
+        uint32_t slice = 1;
+        for (const GroupDesc& g : gdesc) slice = std::max(slice, (g.nv + C - 1) / C);
+        h->cl_slice = slice;
+        h->cl_lcap = 1;
+        std::vector<uint32_t> tmp;
+        for (GroupDesc& g : gdesc) {
+            const uint32_t crs_base = (uint32_t)crs.size(), lb_base = (uint32_t)lbs.size();
+            std::vector<uint32_t> owned(C, 0);
+            for (uint32_t col = 0; col < g.n_col; ++col) {
+                const uint32_t b = gcol_start[g.col_base + col], e = gcol_start[g.col_base + col + 1];
+                std::vector<std::vector<uint32_t>> by(C);
+                for (uint32_t k = b; k < e; ++k) {
+                    const uint32_t* q = &h->tets[4ull * h->tet_order[k]];
+                    uint32_t r[4], best = 0, bestn = 0;
+                    for (int i = 0; i < 4; ++i) r[i] = (old_to_new[q[i]] - g.v0) / slice;
+                    for (int i = 0; i < 4; ++i) {
+                        uint32_t n = 0;
+                        for (int j = 0; j < 4; ++j) n += r[j] == r[i];
+                        if (n > bestn || (n == bestn && r[i] < best)) { best = r[i]; bestn = n; }
+                    }
+                    by[best].push_back(h->tet_order[k]);
+                }
+                uint32_t k = b;
+                for (uint32_t rr = 0; rr < C; ++rr) {
+                    crs.push_back(k);
+                    lbs.push_back(owned[rr]);
+                    owned[rr] += (uint32_t)by[rr].size();
+                    for (uint32_t t : by[rr]) h->tet_order[k++] = t;
+                }
+            }
+            crs.push_back(g.n_col ? gcol_start[g.col_base + g.n_col] : 0);
+            for (uint32_t rr = 0; rr < C; ++rr) h->cl_lcap = std::max(h->cl_lcap, owned[rr]);
+            g.col_base = crs_base;
+            g.lb_base = lb_base;
+        }
     }
     // 4. block size
     h->block = h->prm.block_size ? h->prm.block_size : 256;
@@ -769,6 +822,7 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
         }
         h->hash_cell = cell;
         hd.inv_h = (float)(1.0 / cell);
+        hd.depth = (float)cell;
         hd.self = h->prm.body_contacts == 2 ? 1 : 0;
         uint32_t cap = 1024;
         while (cap < 2 * d.n_surf) cap *= 2;
@@ -815,11 +869,12 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
         ClusterDev& c = h->cd;
         c.cluster_size = (uint32_t)h->cl_size;
         uint32_t slice = 1;
-        for (const GroupDesc& g : gdesc) slice = std::max(slice, (g.nv + c.cluster_size - 1) / c.cluster_size);
+        slice = h->cl_slice;
         c.slice = slice;
         c.xn_minus_xi = slice * 16u;
         c.n_groups = (uint32_t)gdesc.size();
-        h->cl_smem = cluster_smem_bytes(slice, P, h->body_on ? 1 : 0);
+        h->cl_smem = cluster_smem_bytes(slice, P, h->body_on ? 1 : 0, h->cl_lcap);
+        c.lcap = h->cl_lcap;
         c.body = h->body_on ? 1 : 0;
         c.bc_q = h->hd.bc_q;
         c.bc_n = h->hd.bc_n;
@@ -837,13 +892,13 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
         if ((s = dalloc(h, &c.tet_packed, T)) != SBS_OK) return s;
         if ((s = dalloc(h, &c.vflags, V)) != SBS_OK) return s;
         if ((s = dalloc(h, &c.groups, gdesc.size())) != SBS_OK) return s;
-        if ((s = dalloc(h, &c.col_start, gcol_start.size())) != SBS_OK) return s;
-        if ((s = dalloc(h, &c.col_split, gcol_split.size())) != SBS_OK) return s;
+        if ((s = dalloc(h, &c.col_start, crs.size())) != SBS_OK) return s;
+        if ((s = dalloc(h, &c.lam_base, lbs.size())) != SBS_OK) return s;
         if ((s = upload(h, c.tet_packed, tp.data(), T * sizeof(uint4))) != SBS_OK) return s;
         if ((s = upload(h, c.vflags, vf.data(), V)) != SBS_OK) return s;
         if ((s = upload(h, c.groups, gdesc.data(), gdesc.size() * sizeof(GroupDesc))) != SBS_OK) return s;
-        if ((s = upload(h, c.col_start, gcol_start.data(), gcol_start.size() * 4)) != SBS_OK) return s;
-        if ((s = upload(h, c.col_split, gcol_split.data(), gcol_split.size() * 4)) != SBS_OK) return s;
+        if ((s = upload(h, c.col_start, crs.data(), crs.size() * 4)) != SBS_OK) return s;
+        if ((s = upload(h, c.lam_base, lbs.data(), lbs.size() * 4)) != SBS_OK) return s;
         if ((size_t)smem_optin < h->cl_smem + 2048) h->cl_feasible = false;
     }
     CU(h, cudaStreamSynchronize(h->st));
@@ -941,12 +996,29 @@ static sbs_status enqueue_frame_kernels(sbs_gpu* h, const StepParams& p) {
     return SBS_OK;
 }
 
+static sbs_status enqueue_warm_init(sbs_gpu* h, const StepParams& p);
+static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t iterations, bool reset);
+
 static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations) {
     StepParams p;
     fill_params(h, p, dt, substeps, iterations);
     double t_end = h->sim_time;
     for (uint32_t k = 0; k < substeps; ++k) t_end += dt;   // same double sequence as the CPU loop
-    if (h->exec_mode == SBS_EXEC_CLUSTER) {
+    if (h->mlp) {
+        // learned warm start: per substep predict -> features -> MLP -> fit
+        // sweep, then the sweeps continue from the fitted multipliers
+        CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+        CU(h, launch_detect_ground(h->d, p, h->st));
+        if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
+        for (uint32_t sub = 0; sub < substeps; ++sub) {
+            CU(h, launch_predict(h->d, p, (int)sub, h->st));
+            sbs_status s = enqueue_warm_init(h, p);
+            if (s) return s;
+            if ((s = enqueue_segments(h, p, iterations, false)) != SBS_OK) return s;
+            CU(h, launch_finalize(h->d, p, h->st));
+        }
+        CU(h, launch_end_frame(h->d, h->st));
+    } else if (h->exec_mode == SBS_EXEC_CLUSTER) {
         // the kernel publishes the frame's contacts into the last-frame slots
         CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
         if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
@@ -1366,6 +1438,111 @@ sbs_status sbs_gpu_get_candidates(sbs_gpu* h, uint64_t* pairs, uint64_t cap, uin
     if (n) *n = total;
     if (pairs)
         for (uint64_t i = 0; i < m && i < cap; ++i) pairs[i] = buf[i];
+    return check_err(h);
+}
+
+static sbs_status warm_prepare(sbs_gpu* h) {
+    if (h->warm_buffers) return SBS_OK;
+    const uint32_t V = h->n_verts, T = h->n_tets;
+    std::vector<uint32_t> cnt(V + 1, 0), inc(4ull * T);
+    std::vector<uint4> tid(T);
+    CU(h, cudaMemcpyAsync(tid.data(), h->d.tet, T * sizeof(uint4), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    for (uint32_t t = 0; t < T; ++t) {
+        cnt[tid[t].x + 1]++; cnt[tid[t].y + 1]++; cnt[tid[t].z + 1]++; cnt[tid[t].w + 1]++;
+    }
+    for (uint32_t v = 0; v < V; ++v) cnt[v + 1] += cnt[v];
+    std::vector<uint32_t> fill(cnt.begin(), cnt.end() - 1);
+    for (uint32_t t = 0; t < T; ++t) {
+        inc[fill[tid[t].x]++] = t; inc[fill[tid[t].y]++] = t; inc[fill[tid[t].z]++] = t; inc[fill[tid[t].w]++] = t;
+    }
+    sbs_status s;
+    if ((s = dalloc(h, &h->wd.feat, 16ull * V)) != SBS_OK) return s;
+    if ((s = dalloc(h, &h->wd.delta, 3ull * V)) != SBS_OK) return s;
+    if ((s = dalloc(h, &h->wd.xpred, V)) != SBS_OK) return s;
+    if ((s = dalloc(h, &h->wd.inc_start, V + 1)) != SBS_OK) return s;
+    if ((s = dalloc(h, &h->wd.inc, 4ull * T)) != SBS_OK) return s;
+    if ((s = upload(h, h->wd.inc_start, cnt.data(), (V + 1) * 4)) != SBS_OK) return s;
+    if ((s = upload(h, h->wd.inc, inc.data(), 4ull * T * 4)) != SBS_OK) return s;
+    CU(h, cudaStreamSynchronize(h->st));
+    h->warm_buffers = true;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (m && m->d.device != h->prm.device) return fail(h, SBS_EINVAL, "MLP lives on another device");
+    if (m && (s = warm_prepare(h)) != SBS_OK) return s;
+    if (m) CU(h, mlp_reserve(m->d, (int)h->n_verts));
+    h->mlp = m;
+    h->graphs.clear();
+    return SBS_OK;
+}
+
+// features -> MLP -> fit sweep (multipliers initialised), on the predicted state
+static sbs_status enqueue_warm_init(sbs_gpu* h, const StepParams& p) {
+    CU(h, launch_features(h->d, h->wd, p, h->st));
+    CU(h, mlp_forward_dev(h->mlp->d, h->wd.feat, (int)h->n_verts, h->wd.delta, h->st));
+    for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c)
+        CU(h, launch_fit_segment(h->d, h->wd, p, h->colour_offsets[c], h->colour_offsets[c + 1], h->st));
+    CU(h, cudaMemsetAsync(h->d.contact_lam, 0, (size_t)(kMaxPlanes + 1) * h->d.n_surf * sizeof(float), h->st));
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_warm_start_init(sbs_gpu* h, double dt) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!h->mlp) return fail(h, SBS_ESTATE, "no warm-start network attached");
+    if (!(dt > 0)) return fail(h, SBS_EINVAL, "dt");
+    StepParams p;
+    fill_params(h, p, dt, 1, 1);
+    return enqueue_warm_init(h, p);
+}
+
+static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t iterations, bool reset) {
+    for (uint32_t it = 0; it < iterations; ++it) {
+        const int first = (reset && it == 0) ? 1 : 0;
+        CU(h, launch_contacts(h->d, p, first, h->st));
+        CU(h, launch_body_contacts(h->d, p, first, h->st));
+        for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c) {
+            StepParams q = p;
+            q.n_colours = 1;
+            q.first_tail = 1;
+            q.colour_start[0] = h->colour_offsets[c];
+            q.colour_start[1] = h->colour_offsets[c + 1];
+            q.colour_split[0] = h->seg_split[c];
+            CU(h, launch_colour(h->d, q, 0, first, h->block, h->grid, h->st));
+        }
+    }
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_solve_ex(sbs_gpu* h, double dt, uint32_t iterations, int32_t reset_lambda) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!(dt > 0)) return fail(h, SBS_EINVAL, "dt");
+    StepParams p;
+    fill_params(h, p, dt, 1, iterations);
+    if (!h->contacts_live) CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+    if ((s = enqueue_segments(h, p, iterations, reset_lambda != 0)) != SBS_OK) return s;
+    h->projections += (uint64_t)iterations * h->n_tets;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_features(sbs_gpu* h, float* feat) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!feat) return fail(h, SBS_EINVAL, "null");
+    if ((s = warm_prepare(h)) != SBS_OK) return s;
+    StepParams p;
+    fill_params(h, p, 1.0, 1, 1);
+    CU(h, launch_features(h->d, h->wd, p, h->st));
+    std::vector<float> buf(16ull * h->n_verts);
+    CU(h, cudaMemcpyAsync(buf.data(), h->wd.feat, buf.size() * 4, cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    for (uint32_t n = 0; n < h->n_verts; ++n)
+        std::copy(&buf[16ull * n], &buf[16ull * n + 16], feat + 16ull * to_global(h, n));
     return check_err(h);
 }
 

@@ -14,14 +14,18 @@ constexpr int kClusterMaxBlock = 512;
 // [v0, v0 + nv) in library order, colour table entries
 // [col_base, col_base + n_col] of ClusterDev::col_start / col_split.
 struct GroupDesc {
-    uint32_t v0, nv, col_base, n_col;
+    uint32_t v0, nv, col_base, n_col, lb_base;
 };
 
 struct ClusterDev {
     GroupDesc* groups;
     uint32_t n_groups;
-    uint32_t* col_start;   // per group: n_col + 1 tet offsets (global tet slots)
-    uint32_t* col_split;   // per group: first SNH slot of each colour
+    // per group, colour-major then rank: n_col * C + 1 tet-slot offsets; the
+    // tets of (colour c, rank r) are those of colour c owning most of their
+    // vertices in rank r's slice
+    uint32_t* col_start;
+    uint32_t* lam_base;    // per group: n_col * C offsets into the CTA's multiplier array
+    uint32_t lcap;         // multipliers per CTA (max tets owned by one CTA)
     uint4* tet_packed;     // per tet slot: vertex as (cluster rank << 24) | slice offset
     uint8_t* vflags;       // per vertex: bit 0 = surface vertex
     uint32_t cluster_size;
@@ -35,9 +39,9 @@ struct ClusterDev {
 // Dynamic shared memory of one CTA for `slice` vertices, `planes` planes and
 // an optional body-contact slot: xi, xn, v, contact records and body normals
 // (float4), global contact slots and the contact vertex list (uint32).
-inline size_t cluster_smem_bytes(uint32_t slice, int planes, int body) {
+inline size_t cluster_smem_bytes(uint32_t slice, int planes, int body, uint32_t lcap) {
     const size_t S = (size_t)planes + (body ? 1 : 0);
-    return (size_t)slice * (3 * 16 + S * 16 + (body ? 16 : 0) + S * 4 + 4);
+    return (size_t)slice * (3 * 16 + S * 16 + (body ? 16 : 0) + S * 4 + 4) + 2 * sizeof(float) * (size_t)lcap;
 }
 
 cudaError_t cluster_configure(int block, size_t smem);

@@ -64,8 +64,11 @@ __device__ __forceinline__ uint32_t vaddr(uint32_t packed, uint32_t xi_base) {
     return map_rank(xi_base + ((packed & 0xFFFFFFu) << 4), packed >> 24);
 }
 
+// lam: this tet's multipliers in the CTA's shared memory (lam[0]; SNH's
+// hydrostatic one at lam[lstride]).
 __device__ __forceinline__ void project_tet_dsmem(const SceneDev& s, const ClusterDev& c, const StepParams& p,
-                                                  uint32_t t, bool snh, bool first, uint32_t xi_base) {
+                                                  uint32_t t, bool snh, bool first, uint32_t xi_base, float* lam,
+                                                  uint32_t lstride) {
     const uint4 id = __ldg(&c.tet_packed[t]);
     const float4 a = __ldg(&s.dm0[t]);
     const float4 b = __ldg(&s.dm1[t]);
@@ -81,7 +84,7 @@ __device__ __forceinline__ void project_tet_dsmem(const SceneDev& s, const Clust
     if (!snh) {
         TetEval e;
         stvk_eval(x0, x1, x2, x3, r0, r1, r2, a.w, b.w, cc.w, e);
-        const float lacc = first ? 0.0f : s.lam0[t];
+        const float lacc = first ? 0.0f : lam[0];
         float gd = 0.0f;
         if (p.stvk_damping) {
             // xn of the tet's vertices: the global copy holds the frame-start
@@ -92,23 +95,23 @@ __device__ __forceinline__ void project_tet_dsmem(const SceneDev& s, const Clust
                    dot(e.g[3], x3 - mk(n3)));
         }
         const float dl = stvk_dlambda(e, w, lacc, p.stvk_alpha_tilde, p.stvk_gamma, gd);
-        s.lam0[t] = lacc + dl;
+        lam[0] = lacc + dl;
         if (dl != 0.0f) {
             moved = true;
 #pragma unroll
             for (int i = 0; i < 4; ++i) dx[i] = e.g[i] * (w[i] * dl);
         }
     } else {
-        float lD = first ? 0.0f : s.lam0[t];
-        float lH = first ? 0.0f : s.lam1[t];
+        float lD = first ? 0.0f : lam[0];
+        float lH = first ? 0.0f : lam[lstride];
         float dlD, dlH;
         if (snh_step(x0, x1, x2, x3, r0, r1, r2, fabsf(a.w), b.w, cc.w, p.inv_dt2, w, lD, lH, dx, dlD, dlH)) {
             lD += dlD;
             lH += dlH;
             moved = true;
         }
-        s.lam0[t] = lD;
-        s.lam1[t] = lH;
+        lam[0] = lD;
+        lam[lstride] = lH;
     }
     if (moved) {
         q0.x += dx[0].x; q0.y += dx[0].y; q0.z += dx[0].z;
@@ -140,9 +143,9 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
     float4* bn = rec + (size_t)slice * S;          // body contact normals (when c.body)
     uint32_t* gidx = reinterpret_cast<uint32_t*>(bn + (c.body ? slice : 0));
     uint32_t* clist = gidx + (size_t)slice * S;
+    float* lam_s = reinterpret_cast<float*>(clist + slice);   // [2 * lcap] multipliers of this CTA's tets
     __shared__ uint32_t s_ncont;
     const uint32_t xi_base = smem_addr(xi);
-    const uint32_t ctid = rank * blockDim.x + threadIdx.x, nct = C * blockDim.x;
 
     for (uint32_t g = cl_id(); g < c.n_groups; g += cl_count()) {
         const GroupDesc gd = c.groups[g];
@@ -264,10 +267,12 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                 }
                 if (S > 0) cluster_sync();  // cluster-uniform condition
                 for (uint32_t col = 0; col < gd.n_col; ++col) {
-                    const uint32_t b = c.col_start[gd.col_base + col], e = c.col_start[gd.col_base + col + 1];
-                    const uint32_t m = c.col_split[gd.col_base + col];
-                    for (uint32_t tt = b + ctid; tt < e; tt += nct)
-                        project_tet_dsmem(s, c, p, tt, tt >= m, first, xi_base);
+                    // this CTA's tets of the colour: those owning most of their vertices here
+                    const uint32_t k = gd.col_base + col * C + rank;
+                    const uint32_t b = c.col_start[k], e = c.col_start[k + 1];
+                    float* lb = lam_s + c.lam_base[gd.lb_base + col * C + rank] - b;
+                    for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
+                        project_tet_dsmem(s, c, p, tt, s.model[tt] != 0, first, xi_base, lb + tt, c.lcap);
                     cluster_sync();
                 }
             }
@@ -285,12 +290,21 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
             t = t_next;
             __syncthreads();
         }
-        // write back the slice and the contact multipliers of the last substep
+        // write back the slice and the multipliers of the last substep
         for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
             const uint32_t gv = own0 + i;
             s.xi[gv] = xi[i];
             s.xn[gv] = xn[i];
             s.v[gv] = vv[i];
+        }
+        for (uint32_t col = 0; col < gd.n_col; ++col) {
+            const uint32_t k = gd.col_base + col * C + rank;
+            const uint32_t b = c.col_start[k], e = c.col_start[k + 1];
+            const float* lb = lam_s + c.lam_base[gd.lb_base + col * C + rank] - b;
+            for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x) {
+                s.lam0[tt] = lb[tt];
+                s.lam1[tt] = lb[tt + c.lcap];
+            }
         }
         for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
             const uint32_t i = clist[k];

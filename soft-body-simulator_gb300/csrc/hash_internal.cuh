@@ -10,6 +10,7 @@ namespace sbs {
 
 struct HashDev {
     float inv_h;                  // 1 / cell size, rounded to float
+    float depth;                  // contact depth limit (the cell size)
     int self;                     // 1: contacts within a body too
     uint32_t mask;                // table capacity - 1 (power of two, >= 2 x surface vertices)
     unsigned long long* keys;     // [cap] cell keys, ~0 = empty

@@ -10,12 +10,13 @@
 // tet with at least one boundary face visits the cells of its AABB; a
 // (surface vertex, tet) pair is a candidate when the vertex is not one of the
 // tet's vertices and belongs to another body (or self contacts are on).
-// Narrow phase: the vertex lies inside the tet; the contact is the boundary
-// face with the largest signed distance d <= 0, frozen for the frame:
-// q = x - d n, outward unit normal n (collision_constraint_t form,
+// Narrow phase (vertex-triangle): the vertex lies behind one of the tet's
+// boundary triangles by less than the cell size and projects inside it; the
+// contact is that triangle's half-space, frozen for the frame: q = x - d n,
+// outward unit normal n (collision_constraint_t form,
 // src/physics/xpbd/collision_constraint.cpp:11-19).  One contact per vertex:
-// largest d, ties to the lower sweep slot, selected with a 64-bit atomicMax
-// (order independent, hence deterministic).
+// largest d, ties to the lower (sweep slot, face), selected with a 64-bit
+// atomicMax (order independent, hence deterministic).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -121,26 +122,24 @@ __global__ void k_hash_fill(SceneDev s, HashDev hd) {
     }
 }
 
-// Signed distances of p to the four face planes of a tet (faces in
-// tetrahedron_t::faces_copy order, src/physics/topology.cpp:335-342, outward
-// normals).  Returns false when p is outside or the tet is degenerate.
-__device__ __forceinline__ bool inside_faces(const float4* x, uint4 id, f3 p, float (&d)[4], f3 (&n)[4]) {
-    const f3 v[4] = {mk(x[id.x]), mk(x[id.y]), mk(x[id.z]), mk(x[id.w])};
+// Boundary face f of a tet as a contact plane for point p (faces in
+// tetrahedron_t::faces_copy order, src/physics/topology.cpp:335-342): outward
+// unit normal n (away from the opposite vertex), signed distance d, and
+// whether the projection of p onto the plane falls inside the triangle.
+__device__ __forceinline__ bool face_plane(const float4* x, uint4 id, int f, f3 p, float& d, f3& n) {
+    const uint32_t v[4] = {id.x, id.y, id.z, id.w};
     const int F[4][4] = {{0, 1, 3, 2}, {1, 2, 3, 0}, {2, 0, 3, 1}, {0, 2, 1, 3}};
-    bool inside = true;
-#pragma unroll
-    for (int f = 0; f < 4; ++f) {
-        const f3 a = v[F[f][0]], b = v[F[f][1]], c = v[F[f][2]], o = v[F[f][3]];
-        f3 nn = cross(b - a, c - a);
-        const float l = sqrtf(dot(nn, nn));
-        if (!(l > 0.0f)) return false;
-        nn = nn * (1.0f / l);
-        if (dot(nn, o - a) > 0.0f) nn = -nn;
-        n[f] = nn;
-        d[f] = dot(p - a, nn);
-        if (d[f] > 0.0f) inside = false;
-    }
-    return inside;
+    const f3 a = mk(x[v[F[f][0]]]), b = mk(x[v[F[f][1]]]), c = mk(x[v[F[f][2]]]), o = mk(x[v[F[f][3]]]);
+    f3 nn = cross(b - a, c - a);
+    const float l = sqrtf(dot(nn, nn));
+    if (!(l > 0.0f)) return false;
+    nn = nn * (1.0f / l);
+    if (dot(nn, o - a) > 0.0f) nn = -nn;
+    n = nn;
+    d = dot(p - a, nn);
+    const f3 q = p - nn * d;
+    const float ua = dot(nn, cross(b - q, c - q)), ub = dot(nn, cross(c - q, a - q)), uc = dot(nn, cross(a - q, b - q));
+    return (ua >= 0.0f && ub >= 0.0f && uc >= 0.0f) || (ua <= 0.0f && ub <= 0.0f && uc <= 0.0f);
 }
 
 __device__ __forceinline__ uint32_t orderable(float f) {
@@ -148,6 +147,10 @@ __device__ __forceinline__ uint32_t orderable(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
+// Narrow phase per candidate: the vertex is behind a boundary triangle of the
+// tet by less than the cell size (-h < d < 0) and projects inside it.  Best
+// per vertex: largest d, ties to the lower (slot, face), by a 64-bit max of
+// (orderable(d) << 32 | ~(slot << 2 | face)).
 __global__ void k_hash_query(SceneDev s, HashDev hd) {
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < hd.n_query; q += gridDim.x * blockDim.x) {
         const uint32_t t = hd.query[q];
@@ -180,17 +183,17 @@ __global__ void k_hash_query(SceneDev s, HashDev hd) {
                         } else {
                             atomicAdd(hd.n_cand, 1ull);
                         }
-                        float d[4];
-                        f3 n[4];
-                        const float4 xv = s.xn[v];
-                        if (!inside_faces(s.xn, id, mk(xv), d, n)) continue;
-                        int bf = -1;
-                        for (int f = 0; f < 4; ++f)
-                            if ((bm >> f) & 1u)
-                                if (bf < 0 || d[f] > d[bf]) bf = f;
-                        if (bf < 0) continue;
-                        const unsigned long long packed = ((unsigned long long)orderable(d[bf]) << 32) | (uint32_t)(~t);
-                        atomicMax(hd.best + v, packed);
+                        const f3 xv = mk(s.xn[v]);
+                        for (int f = 0; f < 4; ++f) {
+                            if (!((bm >> f) & 1u)) continue;
+                            float d;
+                            f3 n;
+                            if (!face_plane(s.xn, id, f, xv, d, n)) continue;
+                            if (!(d < 0.0f && d > -hd.depth)) continue;
+                            const unsigned long long packed =
+                                ((unsigned long long)orderable(d) << 32) | (uint32_t)(~((t << 2) | (uint32_t)f));
+                            atomicMax(hd.best + v, packed);
+                        }
                     }
                 }
     }
@@ -205,28 +208,22 @@ __global__ void k_body_contacts(SceneDev s, HashDev hd) {
         const unsigned long long b = hd.best[v];
         float4 rq = make_float4(0.f, 0.f, 0.f, 0.f), rn = make_float4(0.f, 0.f, 0.f, 0.f);
         if (b != 0ull) {
-            const uint32_t t = ~(uint32_t)(b & 0xFFFFFFFFull);
-            const uint4 id = s.tet[t];
-            const float4 xv = s.xn[v];
-            float d[4];
-            f3 n[4];
-            inside_faces(s.xn, id, mk(xv), d, n);
-            const uint8_t bm = hd.bmask[t];
-            int bf = -1;
-            for (int f = 0; f < 4; ++f)
-                if ((bm >> f) & 1u)
-                    if (bf < 0 || d[f] > d[bf]) bf = f;
-            if (bf >= 0) {
-                const f3 q = mk(xv) - n[bf] * d[bf];
-                rq = make_float4(q.x, q.y, q.z, 1.0f);
-                const uint32_t slot = atomicAdd(&s.counters[kMaxPlanes], 1u);
-                rn = make_float4(n[bf].x, n[bf].y, n[bf].z, __uint_as_float(slot));
-                if (slot < s.n_surf) {
-                    Contact c;
-                    c.q = make_float4(q.x, q.y, q.z, __uint_as_float(v));
-                    c.n = rn;
-                    s.contacts[(size_t)kMaxPlanes * s.n_surf + slot] = c;
-                }
+            const uint32_t key = ~(uint32_t)(b & 0xFFFFFFFFull);
+            const uint32_t t = key >> 2;
+            const int f = (int)(key & 3u);
+            const f3 xv = mk(s.xn[v]);
+            float d;
+            f3 n;
+            face_plane(s.xn, s.tet[t], f, xv, d, n);
+            const f3 q = xv - n * d;
+            rq = make_float4(q.x, q.y, q.z, 1.0f);
+            const uint32_t slot = atomicAdd(&s.counters[kMaxPlanes], 1u);
+            rn = make_float4(n.x, n.y, n.z, __uint_as_float(slot));
+            if (slot < s.n_surf) {
+                Contact c;
+                c.q = make_float4(q.x, q.y, q.z, __uint_as_float(v));
+                c.n = rn;
+                s.contacts[(size_t)kMaxPlanes * s.n_surf + slot] = c;
             }
         }
         hd.bc_q[v] = rq;

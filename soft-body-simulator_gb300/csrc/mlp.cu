@@ -1,0 +1,332 @@
+// Per-vertex warm-start MLP: 16 -> 128 -> 128 -> 128 -> 3, SiLU after the
+// three hidden layers.  BF16 tensor-core GEMMs (mma.sync m16n8k16, FP32
+// accumulate), FP32 master weights, Adam.  Forward, backward and the
+// optimiser are written here; nothing calls a library GEMM.
+//
+// Layout: activations row-major [n][features]; weights [out][in] row-major
+// (FP32 master + BF16 copy); inputs are normalised inside the network
+// ((x - mean) / std) and outputs scaled by out_scale, so callers pass raw
+// features and receive raw displacements.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sbs_gpu.h"
+#include "mlp_internal.cuh"
+
+namespace sbs {
+
+// --------------------------------------------------------------------------
+// Generic BF16 GEMM on tensor cores:
+//   C[m, n] (f32) = beta * C[m, n] + sum_k A(m, k) * B(k, n) (+ bias[n])
+// with A(m, k) = A[m * sam + k * sak] and B(k, n) = B[k * sbk + n * sbn]
+// (BF16, arbitrary strides, so transposes are free).  Epilogue: optional
+// bias, optional SiLU into a BF16 copy, optional BF16 copy of C.
+// CTA tile 64 x 64, k-step 32, 4 warps of 32 x 32.
+constexpr int GM = 64, GN = 64, GK = 32, GPAD = 8;
+
+struct GemmArgs {
+    const __nv_bfloat16* A;
+    long long sam, sak;
+    const __nv_bfloat16* B;
+    long long sbk, sbn;
+    float* C;             // [M x N] row-major, ldc
+    long long ldc;
+    float beta;
+    const float* bias;    // [N] or null
+    __nv_bfloat16* Cb;    // optional BF16 copy of C (pre-activation), ld = ldc
+    __nv_bfloat16* Act;   // optional BF16 SiLU(C), ld = ldc
+    int M, N, K;
+    int splitk;           // > 1: blockIdx.z takes a K slice and atomically adds into C (pre-zeroed)
+};
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+
+__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
+    __shared__ __align__(16) __nv_bfloat16 As[GM][GK + GPAD];
+    __shared__ __align__(16) __nv_bfloat16 Bs[GN][GK + GPAD];  // n-major, k contiguous
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int gid = lane >> 2, tig = lane & 3;
+    const int m0 = blockIdx.y * GM, n0 = blockIdx.x * GN;
+    const int kper = g.splitk > 1 ? ((g.K + g.splitk * GK - 1) / (g.splitk * GK)) * GK : g.K;
+    const int kbeg = g.splitk > 1 ? blockIdx.z * kper : 0;
+    const int kend = g.splitk > 1 ? min(g.K, kbeg + kper) : g.K;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.0f;
+    const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+    for (int k0 = kbeg; k0 < kend; k0 += GK) {
+        for (int e = tid; e < GM * GK; e += 128) {
+            const int mm = e / GK, kk = e % GK;
+            const int m = m0 + mm, k = k0 + kk;
+            As[mm][kk] = (m < g.M && k < kend) ? g.A[m * g.sam + k * g.sak] : zero;
+        }
+        for (int e = tid; e < GN * GK; e += 128) {
+            const int nn = e / GK, kk = e % GK;
+            const int n = n0 + nn, k = k0 + kk;
+            Bs[nn][kk] = (n < g.N && k < kend) ? g.B[k * g.sbk + n * g.sbn] : zero;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < GK; ks += 16) {
+            uint32_t a[2][4], b[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = wm + i * 16 + gid;
+                a[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + tig * 2]);
+                a[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + tig * 2]);
+                a[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + tig * 2 + 8]);
+                a[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + tig * 2 + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = wn + j * 8 + gid;
+                b[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + tig * 2]);
+                b[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + tig * 2 + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], a[i], b[j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int m = m0 + wm + i * 16 + gid + (r >= 2 ? 8 : 0);
+                const int n = n0 + wn + j * 8 + tig * 2 + (r & 1);
+                if (m >= g.M || n >= g.N) continue;
+                float v = acc[i][j][r];
+                float* cp = g.C + m * g.ldc + n;
+                if (g.splitk > 1) {
+                    atomicAdd(cp, v);
+                    continue;
+                }
+                if (g.beta != 0.0f) v += g.beta * *cp;
+                if (g.bias) v += g.bias[n];
+                *cp = v;
+                if (g.Cb) g.Cb[m * g.ldc + n] = __float2bfloat16(v);
+                if (g.Act) g.Act[m * g.ldc + n] = __float2bfloat16(silu(v));
+            }
+}
+
+static cudaError_t gemm(const GemmArgs& g, cudaStream_t st) {
+    dim3 grid((g.N + GN - 1) / GN, (g.M + GM - 1) / GM, g.splitk > 1 ? g.splitk : 1);
+    k_gemm<<<grid, 128, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+// --------------------------------------------------------------------------
+// Elementwise kernels
+
+// xn = bf16((x - mean) / std), x [n][16]
+__global__ void k_norm_in(const float* x, const float* mean, const float* inv_std, __nv_bfloat16* xn, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * kIn) return;
+    const int f = i % kIn;
+    xn[i] = __float2bfloat16((x[i] - mean[f]) * inv_std[f]);
+}
+
+// y = z4 * out_scale (raw output), z4 [n][3]
+__global__ void k_scale_out(const float* z4, const float* scale, float* y, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * kOut) return;
+    y[i] = z4[i] * scale[i % kOut];
+}
+
+// loss = mean_i sum_o (z4 - t / scale)^2 ; dz4 = 2 (z4 - t/scale) / n  (bf16 and f32)
+__global__ void k_loss(const float* z4, const float* t, const float* scale, float* dz4, __nv_bfloat16* dz4b,
+                       float* loss_acc, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float e2 = 0.0f;
+    if (i < n * kOut) {
+        const float d = z4[i] - t[i] / scale[i % kOut];
+        dz4[i] = 2.0f * d / (float)n;
+        dz4b[i] = __float2bfloat16(2.0f * d / (float)n);
+        e2 = d * d;
+    }
+    for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss_acc, e2 / (float)n);
+}
+
+// dz = da * silu'(z), z kept in f32: silu'(z) = s (1 + z (1 - s)), s = sigmoid(z)
+__global__ void k_silu_back(const float* da, const float* z, __nv_bfloat16* dzb, float* dz, int count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float s = 1.0f / (1.0f + __expf(-z[i]));
+    const float v = da[i] * s * (1.0f + z[i] * (1.0f - s));
+    dz[i] = v;
+    dzb[i] = __float2bfloat16(v);
+}
+
+// db[j] = sum_rows dz[r][j]
+__global__ void k_colsum(const float* dz, float* db, int n, int cols) {
+    const int j = blockIdx.x;
+    float s = 0.0f;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) s += dz[(long long)r * cols + j];
+    __shared__ float sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[j] = sh[0];
+}
+
+// Adam on the FP32 masters, then refresh the BF16 copies.
+__global__ void k_adam(float* w, const float* gr, float* m1, float* m2, __nv_bfloat16* wb, int count, float lr,
+                       float b1, float b2, float eps, float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float g = gr[i];
+    const float a = b1 * m1[i] + (1.0f - b1) * g;
+    const float b = b2 * m2[i] + (1.0f - b2) * g * g;
+    m1[i] = a;
+    m2[i] = b;
+    const float v = w[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+    w[i] = v;
+    wb[i] = __float2bfloat16(v);
+}
+
+__global__ void k_to_bf16(const float* w, __nv_bfloat16* wb, int count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) wb[i] = __float2bfloat16(w[i]);
+}
+
+// gather rows idx[0..n) of (x, t) into contiguous batch buffers
+__global__ void k_gather(const float* x, const float* t, const uint32_t* idx, float* xb, float* tb, int n) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const uint32_t s = idx[r];
+    for (int f = 0; f < kIn; ++f) xb[r * kIn + f] = x[(size_t)s * kIn + f];
+    for (int o = 0; o < kOut; ++o) tb[r * kOut + o] = t[(size_t)s * kOut + o];
+}
+
+// idx[r] = hash(seed, step, r) mod n_data (sampling with replacement)
+__global__ void k_sample(uint32_t* idx, int n, uint32_t n_data, unsigned long long seed) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    unsigned long long z = seed + 0x9e3779b97f4a7c15ull * (unsigned long long)(r + 1);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    idx[r] = (uint32_t)(z % n_data);
+}
+
+static inline int nb(long long n, int b = 256) { return (int)((n + b - 1) / b); }
+
+// --------------------------------------------------------------------------
+// Network passes on device buffers (MlpDev holds weights and workspace).
+
+cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = mlp_reserve(d, n)) != cudaSuccess) return e;
+    k_norm_in<<<nb((long long)n * kIn), 256, 0, st>>>(x, d.mean, d.inv_std, d.xn, n);
+    const __nv_bfloat16* in = d.xn;
+    int kin = kIn;
+    for (int l = 0; l < 3; ++l) {
+        GemmArgs g{};
+        g.A = in; g.sam = kin; g.sak = 1;
+        g.B = d.wb[l]; g.sbk = 1; g.sbn = kin;        // B(k, n) = W[n][k]
+        g.C = d.z[l]; g.ldc = kHid; g.beta = 0.0f; g.bias = d.b[l];
+        g.Act = d.a[l];
+        g.M = n; g.N = kHid; g.K = kin;
+        if ((e = gemm(g, st)) != cudaSuccess) return e;
+        in = d.a[l];
+        kin = kHid;
+    }
+    GemmArgs g{};
+    g.A = d.a[2]; g.sam = kHid; g.sak = 1;
+    g.B = d.wb[3]; g.sbk = 1; g.sbn = kHid;
+    g.C = d.z[3]; g.ldc = kOut; g.beta = 0.0f; g.bias = d.b[3];
+    g.M = n; g.N = kOut; g.K = kHid;
+    if ((e = gemm(g, st)) != cudaSuccess) return e;
+    if (y_raw) k_scale_out<<<nb((long long)n * kOut), 256, 0, st>>>(d.z[3], d.out_scale, y_raw, n);
+    return cudaGetLastError();
+}
+
+// Loss and gradient w.r.t. all parameters (into d.grad) for n rows.
+cudaError_t mlp_backward_dev(MlpDev& d, const float* x, const float* t, int n, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = mlp_forward_dev(d, x, n, nullptr, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(d.loss, 0, sizeof(float), st)) != cudaSuccess) return e;
+    k_loss<<<nb((long long)n * kOut), 256, 0, st>>>(d.z[3], t, d.out_scale, d.dz[3], d.dzb[3], d.loss, n);
+    const int fin[4] = {kIn, kHid, kHid, kHid};
+    const int fout[4] = {kHid, kHid, kHid, kOut};
+    for (int l = 3; l >= 0; --l) {
+        // dW_l[o][i] = sum_r dz_l[r][o] * act_{l-1}[r][i]
+        const __nv_bfloat16* act = l == 0 ? d.xn : d.a[l - 1];
+        GemmArgs g{};
+        g.A = d.dzb[l]; g.sam = 1; g.sak = fout[l];    // A(m=o, k=r) = dz[r][o]
+        g.B = act; g.sbk = fin[l]; g.sbn = 1;           // B(k=r, n=i) = act[r][i]
+        g.C = d.grad + d.woff[l]; g.ldc = fin[l]; g.beta = 0.0f;
+        g.M = fout[l]; g.N = fin[l]; g.K = n;
+        g.splitk = std::max(1, std::min(256, n / 1024));
+        if (g.splitk > 1 &&
+            (e = cudaMemsetAsync(g.C, 0, sizeof(float) * (size_t)fout[l] * fin[l], st)) != cudaSuccess)
+            return e;
+        if ((e = gemm(g, st)) != cudaSuccess) return e;
+        k_colsum<<<fout[l], 256, 0, st>>>(d.dz[l], d.grad + d.boff[l], n, fout[l]);
+        if (l == 0) break;
+        // da_{l-1}[r][i] = sum_o dz_l[r][o] * W_l[o][i]
+        GemmArgs h{};
+        h.A = d.dzb[l]; h.sam = fout[l]; h.sak = 1;
+        h.B = d.wb[l]; h.sbk = fin[l]; h.sbn = 1;       // B(k=o, n=i) = W[o][i]
+        h.C = d.da; h.ldc = fin[l]; h.beta = 0.0f;
+        h.M = n; h.N = fin[l]; h.K = fout[l];
+        if ((e = gemm(h, st)) != cudaSuccess) return e;
+        k_silu_back<<<nb((long long)n * kHid), 256, 0, st>>>(d.da, d.z[l - 1], d.dzb[l - 1], d.dz[l - 1], n * kHid);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_adam_dev(MlpDev& d, float lr, cudaStream_t st) {
+    d.step += 1;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float c1 = 1.0f - powf(b1, (float)d.step), c2 = 1.0f - powf(b2, (float)d.step);
+    k_adam<<<nb(kParams), 256, 0, st>>>(d.w, d.grad, d.m1, d.m2, d.wball, kParams, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_sync_bf16(MlpDev& d, cudaStream_t st) {
+    k_to_bf16<<<nb(kParams), 256, 0, st>>>(d.w, d.wball, kParams);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_train_steps(MlpDev& d, int steps, int batch, float lr, unsigned long long seed, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = mlp_reserve(d, batch)) != cudaSuccess) return e;
+    for (int s = 0; s < steps; ++s) {
+        k_sample<<<nb(batch), 256, 0, st>>>(d.idx, batch, d.n_data, seed + 1000003ull * (unsigned long long)d.step);
+        k_gather<<<nb(batch), 256, 0, st>>>(d.data_x, d.data_t, d.idx, d.bx, d.bt, batch);
+        if ((e = mlp_backward_dev(d, d.bx, d.bt, batch, st)) != cudaSuccess) return e;
+        if ((e = mlp_adam_dev(d, lr, st)) != cudaSuccess) return e;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace sbs

@@ -1,0 +1,164 @@
+// Learned warm start of a substep's Gauss-Seidel sweeps.
+//
+// After the prediction (timestep.cpp:35-43) the per-vertex MLP maps 16
+// features to a displacement guess d_i for the substep's solution.  Moving
+// the positions alone would break XPBD's bookkeeping (x - x_pred must stay
+// sum_j M^-1 grad C_j^T lambda_j, with lambda starting at 0), so the guess is
+// turned into multipliers by one "fit" sweep in the solver's colour order:
+// each constraint takes the multiplier increment whose position update best
+// matches the displacement still missing at its vertices,
+//     dl = argmin sum_i m_i |w_i grad_i C dl - r_i|^2,  r_i = x_pred_i + d_i - x_i,
+// (2x2 normal equations with the XPBD compliance terms for SNH), and moves
+// its vertices accordingly.  The ordinary sweeps then continue from those
+// multipliers.  Features (per vertex): x_pred - x (3), mean deformation
+// gradient of the incident tets at x_pred (9, row-major), external
+// acceleration (3), pin flag (1).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "warmstart_internal.cuh"
+#include "xpbd_internal.cuh"
+#include "xpbd_math.cuh"
+
+namespace sbs {
+
+__global__ void k_features(SceneDev s, WarmDev w, StepParams p) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < s.n_verts; v += gridDim.x * blockDim.x) {
+        const float4 xp = s.xi[v], x = s.xn[v];
+        float* f = w.feat + (size_t)v * 16;
+        f[0] = xp.x - x.x;
+        f[1] = xp.y - x.y;
+        f[2] = xp.z - x.z;
+        float F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const uint32_t b = w.inc_start[v], e = w.inc_start[v + 1];
+        for (uint32_t k = b; k < e; ++k) {
+            const uint32_t t = w.inc[k];
+            const uint4 id = s.tet[t];
+            const f3 x3 = mk(s.xi[id.w]);
+            const f3 d1 = mk(s.xi[id.x]) - x3, d2 = mk(s.xi[id.y]) - x3, d3 = mk(s.xi[id.z]) - x3;
+            const m3 Fm = deformation(d1, d2, d3, mk(s.dm0[t]), mk(s.dm1[t]), mk(s.dm2[t]));
+            F[0] += Fm.c0.x; F[1] += Fm.c1.x; F[2] += Fm.c2.x;
+            F[3] += Fm.c0.y; F[4] += Fm.c1.y; F[5] += Fm.c2.y;
+            F[6] += Fm.c0.z; F[7] += Fm.c1.z; F[8] += Fm.c2.z;
+        }
+        const float inv = e > b ? 1.0f / (float)(e - b) : 0.0f;
+        for (int i = 0; i < 9; ++i) f[3 + i] = F[i] * inv;
+        const bool pinned = !(xp.w > 0.0f);
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        if (!pinned) {
+            if (p.gravity_mode == 1) { ax = p.gx * xp.w; ay = p.gy * xp.w; az = p.gz * xp.w; }
+            else { ax = p.gx; ay = p.gy; az = p.gz; }
+            if (p.has_acc && s.v[v].w == 0.0f) {
+                const float4 a = s.acc[v];
+                ax += a.x; ay += a.y; az += a.z;
+            }
+        }
+        f[12] = ax;
+        f[13] = ay;
+        f[14] = az;
+        f[15] = pinned ? 1.0f : 0.0f;
+        w.xpred[v] = xp;
+    }
+}
+
+// One tet of the fit sweep; lambda starts from 0 (first sweep of the substep).
+__device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, const StepParams& p, uint32_t t) {
+    const uint4 id = s.tet[t];
+    const float4 a = s.dm0[t], b = s.dm1[t], c = s.dm2[t];
+    float4 q[4] = {__ldcg(&s.xi[id.x]), __ldcg(&s.xi[id.y]), __ldcg(&s.xi[id.z]), __ldcg(&s.xi[id.w])};
+    const uint32_t vid[4] = {id.x, id.y, id.z, id.w};
+    f3 r[4];
+    float wgt[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float4 xp = w.xpred[vid[i]];
+        const float* d = w.delta + (size_t)vid[i] * 3;
+        r[i] = mk(xp.x + d[0] - q[i].x, xp.y + d[1] - q[i].y, xp.z + d[2] - q[i].z);
+        wgt[i] = q[i].w;
+    }
+    const f3 x0 = mk(q[0]), x1 = mk(q[1]), x2 = mk(q[2]), x3 = mk(q[3]);
+    const f3 r0 = mk(a), r1 = mk(b), r2 = mk(c);
+    f3 dx[4];
+    if (s.model[t] == 0) {
+        TetEval e;
+        stvk_eval(x0, x1, x2, x3, r0, r1, r2, a.w, b.w, c.w, e);
+        float num = 0.f, den = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            num += wgt[i] > 0.0f ? dot(e.g[i], r[i]) : 0.0f;
+            den += wgt[i] * dot(e.g[i], e.g[i]);
+        }
+        const float dl = den > 1e-20f ? num / (den + p.stvk_alpha_tilde) : 0.0f;
+        s.lam0[t] = dl;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dx[i] = e.g[i] * (wgt[i] * dl);
+    } else {
+        const float aV0 = fabsf(a.w), mu = b.w, lam = c.w;
+        const m3 F = deformation(x0 - x3, x1 - x3, x2 - x3, r0, r1, r2);
+        const float cD = sqrtf(dot(F.c0, F.c0) + dot(F.c1, F.c1) + dot(F.c2, F.c2));
+        float dlD = 0.f, dlH = 0.f;
+        f3 gD[4], gH[4];
+        if (cD > 1e-12f) {
+            const float icD = 1.0f / cD;
+            const f3 h0 = cross(F.c1, F.c2), h1 = cross(F.c2, F.c0), h2 = cross(F.c0, F.c1);
+            gD[0] = (F.c0 * r0.x + F.c1 * r0.y + F.c2 * r0.z) * icD;
+            gD[1] = (F.c0 * r1.x + F.c1 * r1.y + F.c2 * r1.z) * icD;
+            gD[2] = (F.c0 * r2.x + F.c1 * r2.y + F.c2 * r2.z) * icD;
+            gD[3] = -(gD[0] + gD[1] + gD[2]);
+            gH[0] = h0 * r0.x + h1 * r0.y + h2 * r0.z;
+            gH[1] = h0 * r1.x + h1 * r1.y + h2 * r1.z;
+            gH[2] = h0 * r2.x + h1 * r2.y + h2 * r2.z;
+            gH[3] = -(gH[0] + gH[1] + gH[2]);
+            float a11 = p.inv_dt2 / (mu * aV0), a22 = p.inv_dt2 / (lam * aV0), a12 = 0.f, b1 = 0.f, b2 = 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                a11 += wgt[i] * dot(gD[i], gD[i]);
+                a22 += wgt[i] * dot(gH[i], gH[i]);
+                a12 += wgt[i] * dot(gD[i], gH[i]);
+                if (wgt[i] > 0.0f) {
+                    b1 += dot(gD[i], r[i]);
+                    b2 += dot(gH[i], r[i]);
+                }
+            }
+            const float det = a11 * a22 - a12 * a12;
+            if (det > 1e-30f * a11 * a22) {
+                dlD = (b1 * a22 - b2 * a12) / det;
+                dlH = (b2 * a11 - b1 * a12) / det;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) gD[i] = gH[i] = mk(0.f, 0.f, 0.f);
+        }
+        s.lam0[t] = dlD;
+        s.lam1[t] = dlH;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dx[i] = (gD[i] * dlD + gH[i] * dlH) * wgt[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        q[i].x += dx[i].x;
+        q[i].y += dx[i].y;
+        q[i].z += dx[i].z;
+        s.xi[vid[i]] = q[i];
+    }
+}
+
+__global__ void k_fit_segment(SceneDev s, WarmDev w, StepParams p, uint32_t b, uint32_t e) {
+    for (uint32_t t = b + blockIdx.x * blockDim.x + threadIdx.x; t < e; t += gridDim.x * blockDim.x) fit_tet(s, w, p, t);
+}
+
+cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParams& p, cudaStream_t st) {
+    const int grid = (int)std::min<uint32_t>(4096, (s.n_verts + 255) / 256);
+    k_features<<<grid > 0 ? grid : 1, 256, 0, st>>>(s, w, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fit_segment(const SceneDev& s, const WarmDev& w, const StepParams& p, uint32_t b, uint32_t e,
+                               cudaStream_t st) {
+    if (e <= b) return cudaSuccess;
+    const int grid = (int)std::min<uint32_t>(2048, (e - b + 127) / 128);
+    k_fit_segment<<<grid, 128, 0, st>>>(s, w, p, b, e);
+    return cudaGetLastError();
+}
+
+}  // namespace sbs

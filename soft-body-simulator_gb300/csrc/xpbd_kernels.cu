@@ -254,14 +254,16 @@ __device__ __forceinline__ void project_tet(const SceneDev& s, const StepParams&
 
 __device__ __forceinline__ void colour_phase(const SceneDev& s, const StepParams& p, int col, bool first) {
     const uint32_t b = p.colour_start[col], e = p.colour_start[col + 1], m = p.colour_split[col];
-    for_each_spread(b, e, [&](uint32_t t) { project_tet(s, p, t, t >= m, first); });
+    (void)m;
+    for_each_spread(b, e, [&](uint32_t t) { project_tet(s, p, t, s.model[t] != 0, first); });
 }
 
 // Tail colours in one CTA, separated by CTA barriers.
 __device__ __forceinline__ void tail_phase(const SceneDev& s, const StepParams& p, bool first) {
     for (int col = p.first_tail; col < p.n_colours; ++col) {
         const uint32_t b = p.colour_start[col], e = p.colour_start[col + 1], m = p.colour_split[col];
-        for (uint32_t t = b + threadIdx.x; t < e; t += blockDim.x) project_tet(s, p, t, t >= m, first);
+        (void)m;
+        for (uint32_t t = b + threadIdx.x; t < e; t += blockDim.x) project_tet(s, p, t, s.model[t] != 0, first);
         __syncthreads();
     }
 }

@@ -101,11 +101,34 @@ def load(build: bool = True):
         "sbs_gpu_plan_sweep": [f64, C.c_uint32, u32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_uint32, C.POINTER(C.c_uint32)],
         "sbs_gpu_get_candidates": [P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)],
+        "sbs_gpu_set_warm_start": [P, C.c_void_p],
+        "sbs_gpu_warm_start_init": [P, C.c_double],
+        "sbs_gpu_solve_ex": [P, C.c_double, C.c_uint32, C.c_int32],
+        "sbs_gpu_get_features": [P, f32],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = C.c_int
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C")
+    msig = {
+        "sbs_mlp_create": [C.c_int32, C.c_uint64, C.POINTER(P)],
+        "sbs_mlp_destroy": [P],
+        "sbs_mlp_get_params": [P, f32p],
+        "sbs_mlp_set_params": [P, f32p],
+        "sbs_mlp_set_normalization": [P, f32p, f32p, f32p],
+        "sbs_mlp_forward": [P, f32p, C.c_uint32, f32p],
+        "sbs_mlp_loss_grad": [P, f32p, f32p, C.c_uint32, C.POINTER(C.c_float), C.c_void_p],
+        "sbs_mlp_set_dataset": [P, f32p, f32p, C.c_uint32],
+        "sbs_mlp_train": [P, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64, C.POINTER(C.c_float)],
+    }
+    for name, args in msig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    L.sbs_mlp_param_count.restype = C.c_uint32
+    L.sbs_mlp_last_error.argtypes = [P]
+    L.sbs_mlp_last_error.restype = C.c_char_p
     L.sbs_gpu_status_string.argtypes = [C.c_int]
     L.sbs_gpu_status_string.restype = C.c_char_p
     L.sbs_gpu_last_error.argtypes = [P]
@@ -301,6 +324,25 @@ class Solver:
                                                 C.byref(n)))
         return v, qn.reshape(-1, 6)
 
+    # -- learned warm start -------------------------------------------------
+    def set_warm_start(self, mlp):
+        self._warm = mlp
+        self._check(self.L.sbs_gpu_set_warm_start(self.h, None if mlp is None else mlp.h))
+
+    def warm_start_init(self, dt: float):
+        self._check(self.L.sbs_gpu_warm_start_init(self.h, dt))
+
+    def solve_ex(self, dt: float, iterations: int, reset: bool):
+        self._check(self.L.sbs_gpu_solve_ex(self.h, dt, iterations, 1 if reset else 0))
+
+    def features(self) -> np.ndarray:
+        out = np.zeros(16 * self.scene.n_verts, np.float32)
+        self._check(self.L.sbs_gpu_get_features(self.h, out))
+        return out.reshape(-1, 16)
+
+    def predicted_all(self) -> np.ndarray:
+        return np.concatenate([self.get_predicted(b) for b in range(len(self.body_sizes))])
+
     def candidates(self) -> np.ndarray:
         """Broad-phase (vertex << 32 | tet) pairs of the last detection, sorted."""
         n = C.c_uint64()
@@ -325,3 +367,70 @@ class Solver:
         st = Stats()
         self._check(self.L.sbs_gpu_get_stats(self.h, C.byref(st)))
         return st
+
+
+class Mlp:
+    """The warm-start MLP (sbs_mlp handle)."""
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        L = load()
+        self.L = L
+        h = C.c_void_p()
+        st = L.sbs_mlp_create(device, seed, C.byref(h))
+        if st != SBS_OK:
+            raise SbsError(st, "sbs_mlp_create failed")
+        self.h = h
+        self.n_params = int(L.sbs_mlp_param_count())
+
+    def _check(self, st):
+        if st != SBS_OK:
+            raise SbsError(st, self.L.sbs_mlp_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sbs_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, np.float32)
+        self._check(self.L.sbs_mlp_get_params(self.h, out))
+        return out
+
+    def set_params(self, p):
+        self._check(self.L.sbs_mlp_set_params(self.h, np.ascontiguousarray(p, np.float32)))
+
+    def set_normalization(self, mean, std, scale):
+        self._check(self.L.sbs_mlp_set_normalization(
+            self.h, np.ascontiguousarray(mean, np.float32), np.ascontiguousarray(std, np.float32),
+            np.ascontiguousarray(scale, np.float32)))
+
+    def forward(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros((len(x), 3), np.float32)
+        self._check(self.L.sbs_mlp_forward(self.h, x.ravel(), len(x), y.ravel()))
+        return y
+
+    def loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = C.c_float()
+        g = np.zeros(self.n_params, np.float32)
+        self._check(self.L.sbs_mlp_loss_grad(self.h, x.ravel(), t.ravel(), len(x), C.byref(loss),
+                                             g.ctypes.data))
+        return loss.value, g
+
+    def set_dataset(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        self._check(self.L.sbs_mlp_set_dataset(self.h, x.ravel(), t.ravel(), len(x)))
+
+    def train(self, steps: int, batch: int, lr: float = 1e-3, seed: int = 0) -> float:
+        loss = C.c_float()
+        self._check(self.L.sbs_mlp_train(self.h, steps, batch, lr, seed, C.byref(loss)))
+        return loss.value

@@ -10,7 +10,10 @@ from sbs_gb300 import scenes
 CELL = 0.2
 
 
-def overlapping_boxes(shift=(0.25, 0.3, 0.05), model=scenes.MODEL_STVK, n=4, body_contacts=1):
+# generic offsets (no vertex of one box exactly on a face plane of the other,
+# where FP32 and FP64 inside tests may legitimately disagree) and a shallow
+# overlap, so penetrating vertices sit in tets with a boundary face
+def overlapping_boxes(shift=(0.353, 0.121, 0.047), model=scenes.MODEL_STVK, n=4, body_contacts=1):
     xa, ta = scenes.bar_5tet(n + 1, n + 1, n + 1, 0.1)
     xb = xa + np.asarray(shift)
     bodies = [scenes.Body(x0=x, tets=ta, model=model, young=1e5, poisson=0.3, density=1000.0,
@@ -109,7 +112,7 @@ def test_body_contact_set_and_sweep(capi_mod, oracle_mod):
     g.detect_contacts()
     vg, qg = g.contacts()
     vo, qo = o.detect_contacts()
-    assert len(vo) > 10
+    assert len(vo) > 3
     assert np.array_equal(vg, vo)
     assert np.abs(qg - qo).max() < 1e-5
     dt = sc.frame_dt

@@ -175,8 +175,12 @@ def test_colouring_is_a_valid_sweep(capi_mod):
     for c in range(len(off) - 1):
         v = t[order[off[c]:off[c + 1]]].ravel()
         assert len(np.unique(v)) == len(v)
+    # the host planner gives the same colours; the solver may order tets within
+    # a colour differently (by owning CTA), which leaves the sweep unchanged
     po, poff = capi_mod.plan_sweep(sc)
-    assert np.array_equal(po, order) and np.array_equal(poff, off)
+    assert np.array_equal(poff, off)
+    for c in range(len(off) - 1):
+        assert np.array_equal(np.sort(po[off[c]:off[c + 1]]), np.sort(order[off[c]:off[c + 1]]))
 
 
 @pytest.mark.parametrize("mode", [1, 2])
