@@ -214,6 +214,27 @@ sbs_status sbs_gpu_plan_sweep(const double* x0, uint32_t n_verts, const uint32_t
                               const int32_t* models, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
                               uint32_t* n_colours);
 
+/* Plane-contact detection for callers that cannot allocate device memory.
+ * No counterpart in the reference (which has no GPU code); it is the ground
+ * contact rule of the solver (surface vertex with n.x + d < 0 becomes a
+ * contact at q = x + |n.x + d| n) offered as one call on buffers the caller
+ * already owns, for hosts that hand out every device byte through their own
+ * allocator or budget, code running inside CUDA stream capture, and real-time
+ * loops that cannot take an allocation's implicit synchronisation.
+ * All pointers are DEVICE pointers: x [3*n_verts] float positions,
+ * surface [n_surface] vertex ids, contact_verts [n_surface] and
+ * contact_points [3*n_surface] outputs (contacts in the order of `surface`),
+ * count [1] output.  n_surface <= 1,048,576 (SBS_EINVAL beyond).  Enqueued on
+ * `stream` (a cudaStream_t; NULL for the default stream), asynchronous.
+ * Working memory is a 32 KB static device array shared by every call on a
+ * device: calls that overlap on the GPU race; the first call on a device
+ * looks the array up (cudaGetSymbolAddress), so make that first call outside
+ * any stream capture.  Allocates nothing. */
+sbs_status sbs_gpu_plane_contacts_noalloc(const float* x, uint32_t n_verts, const uint32_t* surface,
+                                          uint32_t n_surface, const double normal[3], double d,
+                                          uint32_t* contact_verts, float* contact_points, uint32_t* count,
+                                          void* stream);
+
 /* ---- Learned warm start: per-vertex MLP 16 -> 128 -> 128 -> 128 -> 3 (SiLU),
  * BF16 tensor-core GEMMs with FP32 accumulate, FP32 master weights, Adam.
  * No reference counterpart (the reference always starts its sweeps from the
