@@ -48,6 +48,14 @@ BYTES_PREDICT = 64   # read xn, v; write xi, v (float4)
 BYTES_FINALIZE = 64  # read xi, xn; write xn, v
 
 
+MATERIALS = {
+    "beam98k": "stable Neo-Hookean E 1e6 nu 0.49",
+    "beam450": "StVK (Green strain energy) E 1e5 nu 0.45",
+    "block2m": "stable Neo-Hookean E 5e5 nu 0.48",
+    "boxes512": "StVK, E log-uniform 1e4..1e6, nu U(0.3, 0.49), per body",
+}
+
+
 def workload(name: str):
     from sbs_gb300 import scenes
     if name == "beam98k":
@@ -56,7 +64,31 @@ def workload(name: str):
         return scenes.beam_c1()
     if name == "block2m":
         return scenes.big_block()
+    if name == "boxes512":
+        return scenes.box_drop()
     raise SystemExit(f"unknown workload {name}")
+
+
+def scene_bytes(scene) -> int:
+    """Device footprint of the solver state: 3 float4 per vertex (xi, xn, v),
+    per tet uint4 indices + 3 float4 (DmInv rows, V0, mu, lambda) + 2 lambdas
+    + model byte."""
+    return scene.n_verts * 48 + scene.n_tets * (16 + 48 + 8 + 1)
+
+
+def bounded_sample(scene, budget: int):
+    """The part of the workload a CPU sample times: whole frames when one
+    frame is within `budget` tet projections, else one substep with as many
+    iterations as fit.  Returns (scene copy, frames, description)."""
+    import dataclasses
+    per_frame = scene.substeps * scene.iterations * scene.n_tets
+    if per_frame <= budget:
+        frames = max(1, min(4, budget // per_frame))
+        return scene, frames, f"{frames} frame(s) of {scene.name}"
+    its = max(1, min(scene.iterations, budget // scene.n_tets))
+    sub = dataclasses.replace(scene, substeps=1, iterations=its)
+    return sub, 1, (f"1 substep ({scene.frame_dt / scene.substeps:.5f} s) with {its} of the "
+                    f"{scene.iterations} iterations of {scene.name}")
 
 
 def frame_bytes(scene, n_contacts: int) -> int:
@@ -124,16 +156,18 @@ def dist_env():
     return world, rank, local
 
 
-def cpu_baseline_sample(scene, frames: int, threads: int):
-    """Times the FP64 oracle on `frames` frames of the workload."""
+def cpu_baseline_sample(scene, budget: int, threads: int):
+    """Times the FP64 oracle on a bounded sample of the workload; returns
+    (projections/s, seconds, projections, description)."""
     from oracle import oracle
     from sbs_gb300 import capi
-    order, offsets = capi.plan_sweep(scene)
-    o = oracle.Oracle(scene, threads=threads)
+    sub, frames, desc = bounded_sample(scene, budget)
+    order, offsets = capi.plan_sweep(sub)
+    o = oracle.Oracle(sub, threads=threads)
     o.set_order(order, offsets)
     secs = o.time_frames(frames)
-    proj = frames * scene.substeps * scene.iterations * scene.n_tets
-    return proj / secs, secs
+    proj = frames * sub.substeps * sub.iterations * sub.n_tets
+    return proj / secs, secs, proj, desc
 
 
 def run_reference(args):
@@ -144,8 +178,11 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     from oracle import oracle
     from sbs_gb300 import capi
-    order, offsets = capi.plan_sweep(scene)
-    o = oracle.Oracle(scene, threads=threads)
+    # each step: one frame, or a bounded part of one for the large workloads
+    sub, _, desc = bounded_sample(scene, 40_000_000)
+    per_step = sub.substeps * sub.iterations * sub.n_tets
+    order, offsets = capi.plan_sweep(sub)
+    o = oracle.Oracle(sub, threads=threads)
     o.set_order(order, offsets)
     for _ in range(args.warmup):
         o.step(1, fast=True)
@@ -153,8 +190,7 @@ def run_reference(args):
     for _ in range(args.steps):
         o.step(1, fast=True)
     secs = time.perf_counter() - t0
-    per_frame = scene.substeps * scene.iterations * scene.n_tets
-    value = per_frame * args.steps / secs
+    value = per_step * args.steps / secs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -163,8 +199,8 @@ def run_reference(args):
         "config": {"workload": scene.name, "tets": scene.n_tets, "vertices": scene.n_verts,
                    "substeps": scene.substeps, "iterations": scene.iterations},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} frames of {scene.name}, colour-parallel sweep "
-                                   f"(bit-identical to the sequential reference order)"},
+                         "sample": f"{args.steps} steps, each {desc.replace('1 frame(s)', 'one frame')}, "
+                                   f"colour-parallel sweep (bit-identical to the sequential reference order)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -178,7 +214,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="beam98k")
     ap.add_argument("--exec-mode", type=int, default=0)
-    ap.add_argument("--cpu-frames", type=int, default=2)
+    ap.add_argument("--cpu-budget", type=int, default=25_000_000,
+                    help="tet projections in the single-thread CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -214,6 +251,7 @@ def main():
         pg.barrier()
     torch.cuda.synchronize()
     frame_ms = []
+    launches0 = solver.stats().kernel_launches
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()
@@ -224,6 +262,7 @@ def main():
         pg.barrier()
     t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
+    timed_launches = solver.stats().kernel_launches - launches0
     total_ms = float(sum(frame_ms))
     if pg:
         t = torch.tensor([total_ms], device=f"cuda:{device}")
@@ -233,7 +272,7 @@ def main():
     value = world * per_frame * args.steps / (total_ms * 1e-3)
 
     # end to end through the C ABI with host buffers
-    x, v = solver.get_state(0)
+    x, v = solver.get_state(-1)   # the whole scene, every body
     hx = torch.empty(x.size, dtype=torch.float32).pin_memory().numpy()
     hv = torch.empty(v.size, dtype=torch.float32).pin_memory().numpy()
     hx[:] = x.ravel()
@@ -243,9 +282,9 @@ def main():
         pg.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        solver.set_state(0, hx, hv)
+        solver.set_state(-1, hx, hv)
         solver.step(1)
-        xo, vo = solver.get_state(0)
+        xo, vo = solver.get_state(-1)
         hx[:] = xo.ravel()
         hv[:] = vo.ravel()
     e2e_s = time.perf_counter() - t0
@@ -281,28 +320,29 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline:
-        cpu_val, cpu_s = cpu_baseline_sample(scene, args.cpu_frames, 1)
+        cpu_val, cpu_s, cpu_proj, cpu_desc = cpu_baseline_sample(scene, args.cpu_budget, 1)
         cpu = {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{args.cpu_frames} frames ({args.cpu_frames * per_frame} tet projections) of "
-                         f"{scene.name} on the FP64 oracle, single thread, {cpu_s:.1f} s"}
+               "sample": f"{cpu_desc} ({cpu_proj} tet projections) on the FP64 oracle, single thread, "
+                         f"{cpu_s:.1f} s"}
 
     st = solver.stats()
-    launches_per_frame = 1 if st.exec_mode == capi.EXEC_PERSISTENT else None
-    if launches_per_frame is None:
-        tail = 1 if st.n_tail_colours else 0
-        launches_per_frame = 2 + scene.substeps * (2 + scene.iterations * (
-            1 + (st.n_colours - st.n_tail_colours) + tail))
+    footprint = scene_bytes(scene)
+    resident = footprint < 100 * 1024 * 1024
+    kernel = {capi.EXEC_PERSISTENT: "k_frame_t<false>", capi.EXEC_CLUSTER: "k_cluster_frame",
+              capi.EXEC_WAVEFRONT: "k_frame_t<true>"}.get(st.exec_mode, "k_colour")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_frame, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": scene.name, "tets": scene.n_tets, "vertices": scene.n_verts,
                    "substeps": scene.substeps, "iterations": scene.iterations,
-                   "frame_dt": scene.frame_dt, "material": "stable Neo-Hookean E 1e6 nu 0.49",
-                   "exec_mode": ["auto", "graph", "persistent", "cluster"][st.exec_mode],
+                   "frame_dt": scene.frame_dt, "material": MATERIALS.get(args.workload, scene.name),
+                   "bodies": len(scene.bodies),
+                   "exec_mode": ["auto", "graph", "persistent", "cluster", "wavefront"][st.exec_mode],
                    "grid_ctas": st.grid_ctas, "block": st.block_size, "colours": st.n_colours,
-                   "l2": "flushed (256 MB write) before every timed frame; the 9 MB scene is "
-                         "L2-resident within a frame",
+                   "l2": (f"flushed (256 MB write) before every timed frame; the "
+                          f"{footprint / 2**20:.0f} MB solver state is "
+                          + ("L2-resident within a frame" if resident else "larger than L2")),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "ms_per_frame": ms_per_frame,
         "frame_ms_samples": frame_ms,
@@ -312,12 +352,12 @@ def main():
                 "ms_per_step": 1e3 * e2e_s / e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_frame" if st.exec_mode == capi.EXEC_PERSISTENT else "k_colour",
-                     "bytes_per_launch": fb, "peak_source": peak_src,
-                     "note": "algorithmic bytes counted once per projection; the scene is "
-                             "L2-resident, so the frame is latency/L2-bound"},
+                     "kernel": kernel, "bytes_per_launch": fb, "peak_source": peak_src,
+                     "note": "algorithmic bytes counted once per projection, per frame; "
+                             + ("the state is L2-resident, so the frame is latency/L2-bound"
+                                if resident else "the state exceeds L2, so sweeps stream from HBM")},
         "cpu_baseline": cpu,
-        "gpu_launches": launches_per_frame * args.steps,
+        "gpu_launches": timed_launches,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

@@ -52,8 +52,11 @@ typedef enum sbs_exec_mode {
     SBS_EXEC_AUTO = 0,       /* pick with the built-in autotuner on the first step */
     SBS_EXEC_GRAPH = 1,      /* one kernel per phase, replayed as a CUDA graph */
     SBS_EXEC_PERSISTENT = 2, /* one cooperative kernel per frame, grid barriers */
-    SBS_EXEC_CLUSTER = 3     /* groups of bodies resident in the shared memory of a
+    SBS_EXEC_CLUSTER = 3,    /* groups of bodies resident in the shared memory of a
                                 thread-block cluster, cluster barriers between phases */
+    SBS_EXEC_WAVEFRONT = 4   /* one cooperative kernel per frame; each CTA owns a slice
+                                of every colour and waits only for the CTAs whose tets
+                                share vertices with its own */
 } sbs_exec_mode;
 
 /* Solver parameters.  Defaults (sbs_gpu_params_default) follow
@@ -96,6 +99,8 @@ typedef struct sbs_gpu_stats {
     double residual;          /* XPBD residual after the last substep (if evaluated) */
     double energy;            /* elastic energy after the last substep (if evaluated) */
     double last_frame_ms;     /* device time of the last timed frame (sbs_gpu_step_timed) */
+    uint64_t kernel_launches; /* kernels run by sbs_gpu_step / step_timed since finalize
+                                 (counted by the host as it enqueues them or their graph) */
 } sbs_gpu_stats;
 
 typedef struct sbs_gpu sbs_gpu;
@@ -139,6 +144,18 @@ sbs_status sbs_gpu_set_external_acceleration(sbs_gpu* h, int32_t body, const flo
  * environment_body_t in main.cpp:60-72. */
 sbs_status sbs_gpu_add_ground_plane(sbs_gpu* h, const double n[3], double d);
 
+/* Distance constraints: n rows of ids [4n] = (b1, b2, v1, v2) - body and
+ * body-local vertex of each end, the order of distance_constraint_t's
+ * constructor (src/physics/xpbd/distance_constraint.cpp:8-22) - with
+ * compliance alpha and damping beta; rest length |x0_1 - x0_2|.  Projected by
+ * distance_constraint_t::project_positions (:24-53) in every iteration after
+ * the tet constraints, in their own colours (sbs_gpu_get_distance_order).
+ * Coincident ends, where the reference divides by zero, leave a constraint
+ * unchanged.  Before finalize; not with SBS_EXEC_CLUSTER (the other modes run
+ * them). */
+sbs_status sbs_gpu_add_distance_constraints(sbs_gpu* h, const uint32_t* ids, uint32_t n, double alpha,
+                                            double beta);
+
 /* Colours the constraint graph, orders tets by (colour, Morton code), uploads
  * the scene and selects the execution mode.  After this the scene is fixed.
  * No single reference counterpart: it replaces building the constraint list
@@ -171,13 +188,15 @@ sbs_status sbs_gpu_detect_contacts(sbs_gpu* h);
  * predicted positions with compensated (Kahan) FP32 sums.  Writes both. */
 sbs_status sbs_gpu_residual(sbs_gpu* h, double dt, double* residual, double* energy);
 
-/* State transfer for one body (host buffers; pinned memory is fastest).
+/* State transfer for one body, or with body = -1 for the whole scene in
+ * global vertex order (bodies in add order), as simulation_t::particles()
+ * holds it (host buffers; pinned memory is fastest).
  * x: positions [3*n_verts], v: velocities [3*n_verts]; either may be NULL.
  * set_state writes x into x, xn and xi, as a particle_t's state after a frame.
  * The gpu_timestep_t adapter calls these around sbs_gpu_step. */
 sbs_status sbs_gpu_set_state(sbs_gpu* h, int32_t body, const float* x, const float* v);
 sbs_status sbs_gpu_get_state(sbs_gpu* h, int32_t body, float* x, float* v);
-/* Predicted/iterate positions xi of one body [3*n_verts]. */
+/* Predicted/iterate positions xi of one body (-1: whole scene) [3*n_verts]. */
 sbs_status sbs_gpu_get_predicted(sbs_gpu* h, int32_t body, float* xi);
 sbs_status sbs_gpu_set_predicted(sbs_gpu* h, int32_t body, const float* xi);
 
@@ -190,6 +209,11 @@ sbs_status sbs_gpu_set_predicted(sbs_gpu* h, int32_t body, const float* xi);
 sbs_status sbs_gpu_get_tet_order(sbs_gpu* h, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
                                  uint32_t* n_colours);
 sbs_status sbs_gpu_get_lambdas(sbs_gpu* h, float* lambdas);
+/* Projection order of the distance constraints (input indices, colour-major)
+ * and colour offsets [n_colours + 1]; their multipliers in input order. */
+sbs_status sbs_gpu_get_distance_order(sbs_gpu* h, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
+                                      uint32_t* n_colours);
+sbs_status sbs_gpu_get_distance_lambdas(sbs_gpu* h, float* lambdas);
 sbs_status sbs_gpu_get_contacts(sbs_gpu* h, uint32_t* verts, float* qn, uint32_t cap, uint32_t* n);
 sbs_status sbs_gpu_get_masses(sbs_gpu* h, float* inv_mass);
 /* Broad-phase candidate pairs of the last contact detection (needs
@@ -199,6 +223,33 @@ sbs_status sbs_gpu_get_masses(sbs_gpu* h, float* inv_mass);
  * (contact_handler.cpp:17 handles SDF contacts only). */
 sbs_status sbs_gpu_get_candidates(sbs_gpu* h, uint64_t* pairs, uint64_t cap, uint64_t* n);
 sbs_status sbs_gpu_get_surface(sbs_gpu* h, uint32_t* verts, uint32_t cap, uint32_t* n);
+
+/* Visual model of a body: the boundary triangle mesh tetrahedral_mesh_boundary_t
+ * builds (src/physics/tetrahedral_mesh_boundary.cpp:76-120) - faces with != 2
+ * incident tets, in the order and winding of their first appearance over the
+ * tets (input order) and their faces_copy faces (src/physics/topology.cpp:335-342);
+ * surface vertices numbered by first appearance.  triangles [3 * n_triangles]
+ * holds surface-vertex ids, vertex_map [n_vertices] the body-local vertex of
+ * each surface vertex (tetrahedral_mesh_boundary_t::from_surface_vertex).
+ * Either array may be NULL (counts only). */
+sbs_status sbs_gpu_get_surface_mesh(sbs_gpu* h, int32_t body, uint32_t* triangles, uint32_t cap_triangles,
+                                    uint32_t* n_triangles, uint32_t* vertex_map, uint32_t cap_vertices,
+                                    uint32_t* n_vertices);
+/* tetrahedral_body_t::update_visual_model (src/physics/tetrahedral_body.cpp:157-165)
+ * on the device: each surface vertex takes its vertex's position, and the
+ * vertex normals get compute_normals' update (tetrahedral_mesh_boundary.cpp:122-145):
+ * add (p2 - p1) x (p3 - p1) of every incident boundary triangle, in triangle
+ * order, then normalise.  The reference never clears the normals, so each
+ * update adds to the previous normal: accumulate_normals = 1 keeps that
+ * behaviour (the state starts at zero and finalize runs the constructor's
+ * first update), 0 starts from zero.  When vertex_buffer is not NULL, surface
+ * vertex i's position and normal are written to vertex_buffer[i * stride + 0..5]
+ * (stride >= 6 floats; 9 is the reference's render layout position, normal,
+ * colour, whose colour floats are left untouched).  vertex_buffer may be device
+ * memory of the handle's device (written by the kernel, no host copy) or host
+ * memory.  Returns when the buffer is written. */
+sbs_status sbs_gpu_update_surface(sbs_gpu* h, int32_t body, int32_t accumulate_normals, float* vertex_buffer,
+                                  uint32_t stride);
 sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st);
 
 /* Host-only (no GPU needed): the Gauss-Seidel sweep order the solver uses
@@ -263,12 +314,16 @@ sbs_status sbs_mlp_set_dataset(sbs_mlp* m, const float* x, const float* t, uint3
 sbs_status sbs_mlp_train(sbs_mlp* m, uint32_t steps, uint32_t batch, float lr, uint64_t seed, float* loss);
 
 /* Attaches (m != NULL) or detaches the warm-start network.  While attached,
- * every substep of sbs_gpu_step runs predict -> features -> MLP -> one fit
- * sweep that turns the predicted displacement into multipliers (colour order,
- * each constraint's increment best matching the displacement still missing at
- * its vertices) -> `iterations` sweeps continuing from those multipliers.
+ * every substep of sbs_gpu_step runs predict -> features -> MLP ->
+ * `fit_sweeps` (1..16) fit sweeps that turn the guessed displacement (the
+ * previous substep's solve displacement plus the network's correction) into
+ * multipliers (colour order, each constraint's increment best matching the
+ * displacement still missing at its vertices) -> `iterations` sweeps
+ * continuing from those multipliers.  The previous substep's displacement is
+ * known when its features were computed and the state was not replaced since
+ * (set_state / set_predicted / a frame without the network reset it to 0).
  * Do not train the same network while it is attached. */
-sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m);
+sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps);
 /* The warm-start half of a substep on its own, after sbs_gpu_predict. */
 sbs_status sbs_gpu_warm_start_init(sbs_gpu* h, double dt);
 /* As sbs_gpu_solve; with reset_lambda = 0 the sweeps continue from the
@@ -276,7 +331,9 @@ sbs_status sbs_gpu_warm_start_init(sbs_gpu* h, double dt);
  * them as constraint_t::prepare_for_projection does (constraint.cpp:12-16). */
 sbs_status sbs_gpu_solve_ex(sbs_gpu* h, double dt, uint32_t iterations, int32_t reset_lambda);
 /* Features of every vertex at the current predicted state, host [16 * n_vertices]
- * in global vertex order (training data). */
+ * in global vertex order (training data).  Call it once per substep, after
+ * sbs_gpu_predict: it also records the prediction that the next substep's
+ * previous-displacement features are measured from. */
 sbs_status sbs_gpu_get_features(sbs_gpu* h, float* feat);
 
 /* Frees every device resource of the handle. */

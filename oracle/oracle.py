@@ -67,6 +67,13 @@ def lib():
         L.orc_get_surface.restype = U32
         L.orc_get_surface.argtypes = [P, I, up, U32]
         L.orc_get_lambdas.argtypes = [P, dp]
+        L.orc_add_distance.restype = I
+        L.orc_add_distance.argtypes = [P, up, U32, D, D]
+        L.orc_set_edge_order.restype = I
+        L.orc_set_edge_order.argtypes = [P, up, U32, C.c_void_p, U32]
+        L.orc_get_distance_lambdas.argtypes = [P, dp]
+        L.orc_surface_mesh.argtypes = [P, I, C.c_void_p, U32, C.POINTER(U32), C.c_void_p, U32, C.POINTER(U32)]
+        L.orc_update_surface.argtypes = [P, I, I, dp, dp]
         L.orc_get_contacts.restype = U32
         L.orc_get_contacts.argtypes = [P, up, dp, U32]
         L.orc_tet_eval.argtypes = [P, U32, C.POINTER(D), dp]
@@ -134,6 +141,11 @@ class Oracle:
             self.body_ranges.append((self.n_verts, len(b.x0)))
             self.n_verts += len(b.x0)
             self.n_tets += len(b.tets)
+        dist = getattr(scene, "distance", None)
+        if dist is not None and len(dist):
+            ids = np.ascontiguousarray(dist, np.uint32).ravel()
+            if L.orc_add_distance(self.h, ids, len(dist), scene.distance_compliance, scene.distance_damping):
+                raise ValueError("bad distance constraint ids")
         if scene.ground is not None:
             n, d = scene.ground
             L.orc_add_ground_plane(self.h, np.asarray(n, np.float64), d)
@@ -163,6 +175,25 @@ class Oracle:
         if rc:
             raise ValueError("bad tet order")
 
+    def set_edge_order(self, order: np.ndarray, offsets: np.ndarray | None = None):
+        """Projection order (input indices, colour-major) of the distance
+        constraints, which run after the tets in every sweep."""
+        order = np.ascontiguousarray(order, np.uint32)
+        off = None if offsets is None else np.ascontiguousarray(offsets, np.uint32)
+        self._eoff = off
+        rc = self.L.orc_set_edge_order(self.h, order, len(order), None if off is None else off.ctypes.data,
+                                       0 if off is None else len(off) - 1)
+        if rc:
+            raise ValueError("bad edge order")
+
+    def distance_lambdas(self) -> np.ndarray:
+        dist = getattr(self.scene, "distance", None)
+        n = 0 if dist is None else len(dist)
+        out = np.zeros(n)
+        if n:
+            self.L.orc_get_distance_lambdas(self.h, out)
+        return out
+
     def step(self, frames: int = 1, fast: bool = False):
         s = self.scene
         f = self.L.orc_step_fast if fast else self.L.orc_step
@@ -187,6 +218,25 @@ class Oracle:
         out = np.zeros(n, np.uint32)
         self.L.orc_get_surface(self.h, body, out, n)
         return out
+
+    def surface_mesh(self, body: int = 0):
+        """(triangles [n_tri, 3] of surface-local ids, surface vertex -> body
+        vertex map) of the body's visual model."""
+        nt, nv = C.c_uint32(), C.c_uint32()
+        self.L.orc_surface_mesh(self.h, body, None, 0, C.byref(nt), None, 0, C.byref(nv))
+        tris = np.zeros(3 * nt.value, np.uint32)
+        vmap = np.zeros(nv.value, np.uint32)
+        self.L.orc_surface_mesh(self.h, body, tris.ctypes.data, nt.value, C.byref(nt), vmap.ctypes.data,
+                                nv.value, C.byref(nv))
+        return tris.reshape(-1, 3), vmap
+
+    def update_surface(self, body: int = 0, accumulate: bool = True):
+        """One visual-model update; returns (positions, normals) [n_sv, 3]."""
+        _, vmap = self.surface_mesh(body)
+        pos = np.zeros(3 * len(vmap))
+        nrm = np.zeros(3 * len(vmap))
+        self.L.orc_update_surface(self.h, body, 1 if accumulate else 0, pos, nrm)
+        return pos.reshape(-1, 3), nrm.reshape(-1, 3)
 
     def lambdas(self) -> np.ndarray:
         out = np.zeros(self.n_tets * 2)

@@ -15,6 +15,10 @@
 //   * plane contacts on surface vertices  src/physics/collision/bvh_model.cpp:72-94,
 //                                      sdf_model.cpp:52-64, contact_handler.cpp:14-54
 //   * particle_t::invmass / a()        src/physics/particle.cpp:39-53
+//   * distance_constraint_t            src/physics/xpbd/distance_constraint.cpp:8-53
+//   * the visual model's boundary mesh and normals
+//                                      src/physics/tetrahedral_mesh_boundary.cpp:76-145,
+//                                      src/physics/tetrahedral_body.cpp:157-165
 // with the same data structure the reference uses: an array of particle
 // records (x0, xi, xn, x, v, f, m) and a list of constraint objects projected
 // through a virtual call, one at a time, in list order.
@@ -215,7 +219,37 @@ struct body_t {
     std::vector<uint32_t> surface;   // global vertex ids, ascending
     std::vector<std::array<uint32_t, 3>> surface_tris;  // global ids, outward
     int model;
+    // visual model (tetrahedral_mesh_boundary_t): triangles in surface-local
+    // ids, surface vertex -> global particle, accumulated vertex normals
+    std::vector<std::array<uint32_t, 3>> vis_tris;
+    std::vector<uint32_t> vis_map;
+    std::vector<vec3> vis_normal;
 };
+
+// tetrahedral_body_t::update_visual_model (src/physics/tetrahedral_body.cpp:157-165)
+// followed by compute_normals (src/physics/tetrahedral_mesh_boundary.cpp:122-145):
+// positions from the particles' x; every boundary triangle adds
+// (p2 - p1) x (p3 - p1) to its three vertex normals, in triangle order; then
+// each normal is normalised (left unchanged when its squared norm is 0, as
+// Eigen's normalize() does).  The normals are not cleared first.
+static void update_visual_model(const std::vector<particle_t>& particles, body_t& b, std::vector<vec3>* pos) {
+    if (pos) {
+        pos->resize(b.vis_map.size());
+        for (size_t i = 0; i < b.vis_map.size(); ++i) (*pos)[i] = particles[b.vis_map[i]].x;
+    }
+    for (const auto& t : b.vis_tris) {
+        const vec3 p1 = particles[b.vis_map[t[0]]].x, p2 = particles[b.vis_map[t[1]]].x,
+                   p3 = particles[b.vis_map[t[2]]].x;
+        const vec3 n = cross(p2 - p1, p3 - p1);
+        b.vis_normal[t[0]] += n;
+        b.vis_normal[t[1]] += n;
+        b.vis_normal[t[2]] += n;
+    }
+    for (auto& n : b.vis_normal) {
+        const double z = dot(n, n);
+        if (z > 0.0) n = n / std::sqrt(z);
+    }
+}
 
 struct params_t {
     double alpha = 1e-4, beta = 0.0, collision_alpha = 1e-8;
@@ -253,6 +287,10 @@ struct sim_t {
     std::vector<uint32_t> vbody;           // per particle
     std::vector<uint8_t> vsurf;            // per particle: surface vertex
     std::vector<uint32_t> slot_of_tet;     // sweep slot of each tet (tie-breaks)
+    // distance constraints, input order; projected after the tets in
+    // edge_order (colour-major), with their colour boundaries in edge_offsets
+    std::vector<std::unique_ptr<constraint_t>> edges;
+    std::vector<uint32_t> edge_order, edge_offsets;
     double time = 0.0;
     int threads = 1;
     stats_t st;
@@ -426,6 +464,21 @@ struct snh_constraint_t final : constraint_t {
         r2 += hd * hd + hh * hh;
         energy += aV0 * (0.5 * mu * (cd * cd - 3.0) + 0.5 * lambda * ch * ch);
     }
+};
+
+// ---------------------------------------------------------------------------
+// distance_constraint_t: src/physics/xpbd/distance_constraint.cpp:8-53.  The
+// rest length is |x0_1 - x0_2| (:20); C = |x1 - x2| - d; n = (x1 - x2)/|x1 - x2|;
+// the damping term gamma * n . ((x1 - xn1) - (x2 - xn2)) as in the Green
+// constraint.  One guard the reference lacks: coincident endpoints (length 0,
+// where the reference divides by zero) and a zero denominator (both ends
+// pinned, alpha 0) leave the constraint untouched.
+struct distance_constraint_t final : constraint_t {
+    uint32_t v1, v2;
+    double d;
+    distance_constraint_t(double a, double b, const sim_t& sim, uint32_t g1, uint32_t g2);
+    void project_positions(sim_t& sim, double dt) override;
+    void residual(const sim_t& sim, double dt, double& r2, double& energy) const override;
 };
 
 // ---------------------------------------------------------------------------
@@ -616,6 +669,65 @@ static void detect_bodies(sim_t& sim) {
 
 using namespace orc;
 
+distance_constraint_t::distance_constraint_t(double a, double b, const sim_t& sim, uint32_t g1, uint32_t g2)
+    : constraint_t(a, b), v1(g1), v2(g2) {
+    d = norm(sim.particles[g1].x0 - sim.particles[g2].x0);
+}
+
+void distance_constraint_t::project_positions(sim_t& sim, double dt) {
+    particle_t& p1 = sim.particles[v1];
+    particle_t& p2 = sim.particles[v2];
+    const double w1 = p1.invmass(), w2 = p2.invmass();
+    const vec3 diff = p1.xi - p2.xi;
+    const double length = norm(diff);
+    if (!(length > 0.0)) return;
+    const vec3 n = diff / length;
+    const double C = length - d;
+    const double wsum = w1 + w2;
+    const double dt2 = dt * dt;
+    const double alpha_tilde = alpha / dt2;
+    const double beta_tilde = beta * dt2;
+    const double gradC_dot_disp = dot(n, p1.xi - p1.xn) - dot(n, p2.xi - p2.xn);
+    const double gamma = alpha_tilde * beta_tilde / dt;
+    const double num = -(C + alpha_tilde * lagrange) + gamma * gradC_dot_disp;
+    const double den = (1.0 + gamma) * wsum + alpha_tilde;
+    if (!(den > 0.0)) return;
+    const double dl = num / den;
+    lagrange += dl;
+    p1.xi += n * (w1 * dl);
+    p2.xi += -n * (w2 * dl);
+}
+
+void distance_constraint_t::residual(const sim_t& sim, double dt, double& r2, double& energy) const {
+    const double C = norm(sim.particles[v1].xi - sim.particles[v2].xi) - d;
+    const double h = C + alpha / (dt * dt) * lagrange;
+    r2 += h * h;
+    if (alpha > 0.0) energy += 0.5 * C * C / alpha;
+}
+
+// The elastic sweep: tets in their (colour) order, then the distance
+// constraints in theirs.
+static void rebuild_edge_tail(sim_t& s) {
+    const size_t nt = s.constraints.size();
+    s.sweep.resize(nt);
+    if (s.edge_order.size() != s.edges.size()) {
+        s.edge_order.resize(s.edges.size());
+        for (uint32_t k = 0; k < s.edge_order.size(); ++k) s.edge_order[k] = k;
+        s.edge_offsets.clear();
+    }
+    for (uint32_t k : s.edge_order) s.sweep.push_back(s.edges[k].get());
+    if (!s.colour_offsets.empty()) {
+        // tet colours first (their offsets end at nt), then the edge colours
+        while (s.colour_offsets.size() > 1 && s.colour_offsets.back() > nt) s.colour_offsets.pop_back();
+        if (s.edge_offsets.empty()) {
+            if (!s.edges.empty()) s.colour_offsets.push_back((uint32_t)(nt + s.edges.size()));
+        } else {
+            for (size_t c = 1; c < s.edge_offsets.size(); ++c)
+                s.colour_offsets.push_back((uint32_t)nt + s.edge_offsets[c]);
+        }
+    }
+}
+
 extern "C" {
 
 void* orc_create(double alpha, double beta, double collision_alpha, const double* gravity,
@@ -700,6 +812,38 @@ int orc_add_body(void* h, const double* x0, const double* xinit, uint32_t nv, co
     std::sort(surf.begin(), surf.end());
     surf.erase(std::unique(surf.begin(), surf.end()), surf.end());
     std::sort(b.surface_tris.begin(), b.surface_tris.end());
+    // visual model (tetrahedral_mesh_boundary.cpp:76-120): the tet mesh lists
+    // each distinct face once, at its first appearance over the tets in order
+    // and their faces_copy faces (topology.cpp:335-342, add_tetrahedron
+    // :904-950), keeping that appearance's winding; faces with != 2 incident
+    // tets are boundary triangles; surface vertices are numbered by first
+    // appearance in them
+    {
+        std::unordered_map<uint64_t, uint8_t> seen;
+        std::unordered_map<uint32_t, uint32_t> local;
+        for (uint32_t t = 0; t < nt; ++t) {
+            const uint32_t* q = tets + 4 * t;
+            const uint32_t fl[4][3] = {{q[0], q[1], q[3]}, {q[1], q[2], q[3]}, {q[2], q[0], q[3]}, {q[0], q[2], q[1]}};
+            for (auto& f : fl) {
+                uint32_t srt[3] = {f[0], f[1], f[2]};
+                std::sort(srt, srt + 3);
+                const uint64_t key = ((uint64_t)srt[0] * nv + srt[1]) * (uint64_t)nv + srt[2];
+                if (faces[key].first == 2 || !seen.emplace(key, 1).second) continue;
+                std::array<uint32_t, 3> tri;
+                for (int j = 0; j < 3; ++j) {
+                    auto it = local.find(f[j]);
+                    if (it == local.end()) {
+                        it = local.emplace(f[j], (uint32_t)b.vis_map.size()).first;
+                        b.vis_map.push_back(b.v0 + f[j]);
+                    }
+                    tri[j] = it->second;
+                }
+                b.vis_tris.push_back(tri);
+            }
+        }
+        b.vis_normal.assign(b.vis_map.size(), vec3{0.0, 0.0, 0.0});
+        update_visual_model(s.particles, b, nullptr);   // tetrahedral_body.cpp:25
+    }
     // per-tet boundary faces and body ids for the spatial hash
     const uint32_t body_id = (uint32_t)s.bodies.size();
     s.vbody.resize(s.particles.size(), body_id);
@@ -727,6 +871,7 @@ int orc_add_body(void* h, const double* x0, const double* xinit, uint32_t nv, co
     s.slot_of_tet.resize(s.constraints.size());
     for (uint32_t k = 0; k < s.slot_of_tet.size(); ++k) s.slot_of_tet[k] = k;
     s.colour_offsets.clear();
+    rebuild_edge_tail(s);
     return (int)s.bodies.size() - 1;
 }
 
@@ -780,7 +925,43 @@ int orc_set_tet_order(void* h, const uint32_t* order, uint32_t n, const uint32_t
     }
     s.colour_offsets.clear();
     if (offsets) s.colour_offsets.assign(offsets, offsets + n_colours + 1);
+    rebuild_edge_tail(s);
     return 0;
+}
+
+// distance_constraint_t objects (distance_constraint.cpp:8-22) for n 4-tuples
+// (b1, b2, v1, v2), as the reference's constructor takes them.
+int orc_add_distance(void* h, const uint32_t* ids, uint32_t n, double alpha, double beta) {
+    sim_t& s = *(sim_t*)h;
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t b1 = ids[4 * k], b2 = ids[4 * k + 1], v1 = ids[4 * k + 2], v2 = ids[4 * k + 3];
+        if (b1 >= s.bodies.size() || b2 >= s.bodies.size() || v1 >= s.bodies[b1].nv || v2 >= s.bodies[b2].nv)
+            return 1;
+        s.edges.push_back(std::make_unique<distance_constraint_t>(alpha, beta, s, s.bodies[b1].v0 + v1,
+                                                                  s.bodies[b2].v0 + v2));
+    }
+    s.edge_order.clear();
+    rebuild_edge_tail(s);
+    return 0;
+}
+
+// Projection order of the distance constraints (input indices, colour-major)
+// with n_colours + 1 colour offsets (may be NULL).
+int orc_set_edge_order(void* h, const uint32_t* order, uint32_t n, const uint32_t* offsets, uint32_t n_colours) {
+    sim_t& s = *(sim_t*)h;
+    if (n != s.edges.size()) return 1;
+    for (uint32_t k = 0; k < n; ++k)
+        if (order[k] >= n) return 1;
+    s.edge_order.assign(order, order + n);
+    s.edge_offsets.clear();
+    if (offsets) s.edge_offsets.assign(offsets, offsets + n_colours + 1);
+    rebuild_edge_tail(s);
+    return 0;
+}
+
+void orc_get_distance_lambdas(void* h, double* out) {
+    sim_t& s = *(sim_t*)h;
+    for (size_t k = 0; k < s.edges.size(); ++k) out[k] = s.edges[k]->lagrange;
 }
 
 static void compute_residual(sim_t& s, double dt, double& r2e, double& r2c, double& energy) {
@@ -820,7 +1001,7 @@ void orc_solve(void* h, double dt, uint32_t iterations) {
     for (uint32_t k = 0; k < iterations; ++k) {
         for (auto& c : s.collision_constraints) c->project_positions(s, dt);
         project_sweep(s, dt);
-        s.st.projections += s.sweep.size();
+        s.st.projections += s.constraints.size();
         if (s.record_history) {
             double r2e, r2c, e;
             compute_residual(s, dt, r2e, r2c, e);
@@ -1024,6 +1205,32 @@ void orc_svd3(const double* F9, double* U9, double* s3, double* V9) {
     svd3(F, U, s, V);
     for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) { U9[3 * i + j] = U.m[i][j]; V9[3 * i + j] = V.m[i][j]; }
     s3[0] = s.x; s3[1] = s.y; s3[2] = s.z;
+}
+
+// Visual model of a body: triangles (surface-local ids) and surface vertex ->
+// body-local vertex map; returns counts through n_tri / n_sv.
+void orc_surface_mesh(void* h, int body, uint32_t* tris, uint32_t cap_tri, uint32_t* n_tri, uint32_t* vmap,
+                      uint32_t cap_sv, uint32_t* n_sv) {
+    const body_t& b = ((sim_t*)h)->bodies[body];
+    *n_tri = (uint32_t)b.vis_tris.size();
+    *n_sv = (uint32_t)b.vis_map.size();
+    for (uint32_t i = 0; i < b.vis_tris.size() && i < cap_tri; ++i)
+        for (int j = 0; j < 3; ++j) tris[3 * i + j] = b.vis_tris[i][j];
+    for (uint32_t i = 0; i < b.vis_map.size() && i < cap_sv; ++i) vmap[i] = b.vis_map[i] - b.v0;
+}
+
+// One visual-model update (accumulate = 0 clears the normals first, which the
+// reference never does); pos / nrm receive [3 * n_sv] each.
+void orc_update_surface(void* h, int body, int accumulate, double* pos, double* nrm) {
+    sim_t& s = *(sim_t*)h;
+    body_t& b = s.bodies[body];
+    if (!accumulate) b.vis_normal.assign(b.vis_map.size(), vec3{0.0, 0.0, 0.0});
+    std::vector<vec3> p;
+    update_visual_model(s.particles, b, &p);
+    for (size_t i = 0; i < p.size(); ++i) {
+        pos[3 * i] = p[i].x; pos[3 * i + 1] = p[i].y; pos[3 * i + 2] = p[i].z;
+        nrm[3 * i] = b.vis_normal[i].x; nrm[3 * i + 1] = b.vis_normal[i].y; nrm[3 * i + 2] = b.vis_normal[i].z;
+    }
 }
 
 double orc_time(void* h) { return ((sim_t*)h)->time; }

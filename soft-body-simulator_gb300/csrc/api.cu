@@ -22,6 +22,8 @@
 #include "cluster_internal.cuh"
 #include "hash_internal.cuh"
 #include "mlp_internal.cuh"
+#include "launch_count.cuh"
+#include "surface_internal.cuh"
 #include "warmstart_internal.cuh"
 
 using namespace sbs;
@@ -82,9 +84,18 @@ struct sbs_gpu {
     int exec_mode = SBS_EXEC_GRAPH;
     int block = 256, grid = 0;
     int pers_block = 256, pers_grid = 0;
+    int wave_grid = 0;                 // CTAs of the wavefront mode (0: unavailable)
+    uint32_t wave_max_nb = 0;          // largest neighbour list
     bool tuned = false;
     bool contacts_live = false;
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::map<GraphKey, uint64_t> graph_kernels;   // kernel nodes of each graph
+    uint64_t kernel_launches = 0;                 // kernels run by frames since finalize
+    BodyHost all_bodies;                          // the whole scene as one range (state transfer)
+    // distance constraints: ends as global input vertex ids, parameters
+    std::vector<uint32_t> dist_v;                 // 2 per constraint
+    std::vector<float4> dist_p;                   // rest length, alpha, beta, 0
+    std::vector<uint32_t> edge_order, edge_offsets;   // colour-major projection order
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<void*> allocations;
     // cluster-resident mode
@@ -103,6 +114,13 @@ struct sbs_gpu {
     sbs_mlp* mlp = nullptr;
     WarmDev wd{};
     bool warm_buffers = false;
+    bool xpred_valid = false;   // wd.xpred belongs to the substep that produced the current x
+    // visual models, numbered as tetrahedral_mesh_boundary_t numbers them
+    std::vector<uint32_t> vis_tri0, vis_sv0;   // per body + end: first triangle / surface vertex
+    std::vector<uint32_t> vis_tris;            // 3 per triangle, surface-local vertex ids
+    std::vector<uint32_t> vis_map;             // surface vertex -> body-local vertex id
+    SurfaceDev sd{};
+    uint32_t fit_sweeps = 1;
     double sim_time = 0.0;   // host mirror of the simulation time
     std::vector<uint32_t> seg_split;  // first SNH slot of each colour segment
 
@@ -353,7 +371,7 @@ sbs_status sbs_gpu_create(const sbs_gpu_params* p, sbs_gpu** out) {
     if (p) prm = *p;
     else sbs_gpu_params_default(&prm);
     if (prm.gravity_mode != 0 && prm.gravity_mode != 1) return fail(nullptr, SBS_EINVAL, "gravity_mode");
-    if (prm.exec_mode < 0 || prm.exec_mode > 3) return fail(nullptr, SBS_EINVAL, "exec_mode");
+    if (prm.exec_mode < 0 || prm.exec_mode > 4) return fail(nullptr, SBS_EINVAL, "exec_mode");
     if (prm.block_size != 0 && (prm.block_size < 32 || prm.block_size > 512 || prm.block_size % 32))
         return fail(nullptr, SBS_EINVAL, "block_size must be a multiple of 32 in [32, 512]");
     int ndev = 0;
@@ -486,6 +504,69 @@ sbs_status sbs_gpu_add_ground_plane(sbs_gpu* h, const double n[3], double d) {
     return SBS_OK;
 }
 
+sbs_status sbs_gpu_add_distance_constraints(sbs_gpu* h, const uint32_t* ids, uint32_t n, double alpha,
+                                            double beta) {
+    if (!h || (n && !ids)) return fail(h, SBS_EINVAL, "distance: null");
+    if (h->finalized) return fail(h, SBS_ESTATE, "distance constraints after finalize");
+    if (!(alpha >= 0.0) || !(beta >= 0.0) || !std::isfinite(alpha) || !std::isfinite(beta))
+        return fail(h, SBS_EINVAL, "distance: alpha and beta must be finite and >= 0");
+    std::vector<uint32_t> v;
+    std::vector<float4> q;
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t b1 = ids[4ull * k], b2 = ids[4ull * k + 1], v1 = ids[4ull * k + 2], v2 = ids[4ull * k + 3];
+        if (b1 >= h->bodies.size() || b2 >= h->bodies.size() || v1 >= h->bodies[b1].nv || v2 >= h->bodies[b2].nv)
+            return fail(h, SBS_EINVAL, "distance: body or vertex id out of range");
+        const uint32_t g1 = h->bodies[b1].v0 + v1, g2 = h->bodies[b2].v0 + v2;
+        if (g1 == g2) return fail(h, SBS_EINVAL, "distance: both ends are the same vertex");
+        double l2 = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            const double dd = h->x0[3ull * g1 + c] - h->x0[3ull * g2 + c];
+            l2 += dd * dd;
+        }
+        v.push_back(g1);
+        v.push_back(g2);
+        q.push_back(make_float4((float)std::sqrt(l2), (float)alpha, (float)beta, 0.0f));
+    }
+    h->dist_v.insert(h->dist_v.end(), v.begin(), v.end());
+    h->dist_p.insert(h->dist_p.end(), q.begin(), q.end());
+    return SBS_OK;
+}
+
+// First-fit edge colouring in input order: an edge takes the smallest colour
+// neither end has used; colours are then listed largest first, input order
+// kept inside a colour.  Returns the colour count, or -1 above kMaxEdgeColours.
+static int colour_edges(const std::vector<uint32_t>& ends, uint32_t V, std::vector<uint32_t>& order,
+                        std::vector<uint32_t>& offsets) {
+    const size_t E = ends.size() / 2;
+    std::vector<uint64_t> used(V, 0);
+    std::vector<int> col(E);
+    int K = 0;
+    for (size_t k = 0; k < E; ++k) {
+        const uint64_t busy = used[ends[2 * k]] | used[ends[2 * k + 1]];
+        if (busy == ~0ull) return -1;
+        int c = 0;
+        while (busy >> c & 1ull) ++c;
+        col[k] = c;
+        used[ends[2 * k]] |= 1ull << c;
+        used[ends[2 * k + 1]] |= 1ull << c;
+        K = std::max(K, c + 1);
+    }
+    std::vector<uint32_t> size(K, 0);
+    for (int c : col) size[c]++;
+    std::vector<int> rank(K);
+    for (int c = 0; c < K; ++c) rank[c] = c;
+    std::stable_sort(rank.begin(), rank.end(), [&](int a, int b) { return size[a] > size[b]; });
+    std::vector<int> pos(K);
+    for (int r = 0; r < K; ++r) pos[rank[r]] = r;
+    offsets.assign(K + 1, 0);
+    for (int c = 0; c < K; ++c) offsets[pos[c] + 1] = size[c];
+    for (int r = 0; r < K; ++r) offsets[r + 1] += offsets[r];
+    order.assign(E, 0);
+    std::vector<uint32_t> fill(offsets.begin(), offsets.end() - 1);
+    for (size_t k = 0; k < E; ++k) order[fill[pos[col[k]]]++] = (uint32_t)k;
+    return K;
+}
+
 static sbs_status upload(sbs_gpu* h, void* dst, const void* src, size_t bytes) {
     if (bytes == 0) return SBS_OK;
     CU(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->st));
@@ -505,6 +586,48 @@ static void fill_params(sbs_gpu* h, StepParams& p, double dt, uint32_t substeps,
     p.contact_alpha_tilde = (float)(h->prm.collision_compliance / (dt * dt));
     p.substeps = (int)substeps;
     p.iterations = (int)iterations;
+}
+
+// Wavefront mode: CTA b of G owns the slice [c0 + b n / G, c0 + (b+1) n / G)
+// of every colour (c0, n: colour start and size).  Two CTAs are neighbours
+// when some vertex is touched by tets of both.  Returns the CSR lists.
+static void wave_neighbours(const std::vector<uint4>& tid, const std::vector<uint32_t>& offsets, int K, int G,
+                            std::vector<uint32_t>& start, std::vector<uint32_t>& list) {
+    std::vector<uint64_t> pairs;   // vertex * G + cta
+    pairs.reserve(tid.size() * 4);
+    for (int c = 0; c < K; ++c) {
+        const uint64_t c0 = offsets[c], n = offsets[c + 1] - offsets[c];
+        for (int b = 0; b < G; ++b) {
+            const uint64_t lo = c0 + n * b / G, hi = c0 + n * (b + 1) / G;
+            for (uint64_t k = lo; k < hi; ++k) {
+                const uint4 q = tid[k];
+                pairs.push_back((uint64_t)q.x * G + b);
+                pairs.push_back((uint64_t)q.y * G + b);
+                pairs.push_back((uint64_t)q.z * G + b);
+                pairs.push_back((uint64_t)q.w * G + b);
+            }
+        }
+    }
+    std::sort(pairs.begin(), pairs.end());
+    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+    const size_t words = ((size_t)G + 63) / 64;
+    std::vector<uint64_t> bits((size_t)G * words, 0);
+    std::vector<uint32_t> ctas;
+    for (size_t i = 0; i < pairs.size();) {
+        const uint64_t v = pairs[i] / G;
+        ctas.clear();
+        while (i < pairs.size() && pairs[i] / G == v) ctas.push_back((uint32_t)(pairs[i++] % G));
+        for (uint32_t a : ctas)
+            for (uint32_t b : ctas)
+                if (a != b) bits[(size_t)a * words + b / 64] |= 1ull << (b % 64);
+    }
+    start.assign(G + 1, 0);
+    list.clear();
+    for (int a = 0; a < G; ++a) {
+        for (int b = 0; b < G; ++b)
+            if (bits[(size_t)a * words + b / 64] >> (b % 64) & 1ull) list.push_back((uint32_t)b);
+        start[a + 1] = (uint32_t)list.size();
+    }
 }
 
 sbs_status sbs_gpu_finalize(sbs_gpu* h) {
@@ -536,6 +659,12 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
             new_to_old[b.v0 + n] = b.v0 + key[n].second;
         }
     }
+    h->all_bodies.v0 = 0;
+    h->all_bodies.nv = V;
+    h->all_bodies.t0 = 0;
+    h->all_bodies.nt = T;
+    h->all_bodies.old_to_new = old_to_new;
+    h->all_bodies.new_to_old = new_to_old;
     // 2. groups of consecutive bodies for the cluster-resident mode: every
     //    group must fit the shared memory of one cluster (<= 16 CTAs)
     const int P = (int)h->planes.size();
@@ -545,13 +674,23 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     // tets it brings (T/V + 1 tets per vertex, 8 bytes each)
     const size_t per_v = cluster_smem_bytes(1, P, h->prm.body_contacts ? 1 : 0, 0) +
                          8 * ((size_t)T / std::max<uint32_t>(V, 1) + 1);
-    const uint32_t cap_slice = (uint32_t)((size_t)(smem_optin - 4096) / per_v);
+    uint32_t cap_slice = (uint32_t)((size_t)(smem_optin - 4096) / per_v);
+    int shrink_tries = 0;
     uint32_t max_body = 0;
     for (const BodyHost& b : h->bodies) max_body = std::max(max_body, b.nv);
+    // a plan whose cluster turns out not to be launchable is redone: with
+    // smaller vertex slices when the final multiplier slices overflow the
+    // shared memory, else (or after a few tries) with the cluster mode excluded
+    // distance constraints may join any two bodies: they run in the global modes only
+    bool allow_cluster = h->prm.exec_mode != SBS_EXEC_GRAPH && h->prm.exec_mode != SBS_EXEC_PERSISTENT &&
+                         h->dist_p.empty();
+    if (!h->dist_p.empty() && h->prm.exec_mode == SBS_EXEC_CLUSTER)
+        return fail(h, SBS_EINVAL, "distance constraints do not run in the cluster-resident mode");
+plan_again:
+    h->seg_split.clear();
     h->cl_size = 1;
     while (h->cl_size < 16 && (uint64_t)h->cl_size * cap_slice < max_body) h->cl_size *= 2;
-    h->cl_feasible = (uint64_t)h->cl_size * cap_slice >= max_body && h->prm.exec_mode != SBS_EXEC_GRAPH &&
-                     h->prm.exec_mode != SBS_EXEC_PERSISTENT;
+    h->cl_feasible = (uint64_t)h->cl_size * cap_slice >= max_body && allow_cluster;
     h->cl_groups.clear();
     if (h->cl_feasible) {
         const uint64_t cap = (uint64_t)h->cl_size * cap_slice;
@@ -565,6 +704,24 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
             nv += h->bodies[bi].nv;
         }
         h->cl_groups.push_back({b0, (uint32_t)h->bodies.size()});
+        // groups that cannot all be resident at once run in rounds, each
+        // paying the whole frame's chain of barriers; the global sweep is then
+        // faster (measured on 512 boxes: 30 ms in rounds against 17 ms), so
+        // several groups are planned only when they fit in one round
+        if (h->cl_groups.size() > 1) {
+            const size_t est = std::min<size_t>((size_t)smem_optin, (size_t)cap_slice * per_v + 4096);
+            const int blk = h->prm.block_size ? std::min(h->prm.block_size, kClusterMaxBlock) : 256;
+            int active = 0;
+            if (cluster_configure(blk, est) != cudaSuccess ||
+                cluster_max_active(h->cl_size, blk, est, &active) != cudaSuccess ||
+                (size_t)active < h->cl_groups.size()) {
+                cudaGetLastError();
+                if (h->prm.exec_mode != SBS_EXEC_CLUSTER) {
+                    h->cl_feasible = false;
+                    h->cl_groups.clear();
+                }
+            }
+        }
     }
     // 3. sweep order: per group (several groups) or over the whole scene:
     //    colour (size-descending), model, Morton code
@@ -669,6 +826,23 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
             g.col_base = crs_base;
             g.lb_base = lb_base;
         }
+        const size_t need = cluster_smem_bytes(h->cl_slice, P, h->prm.body_contacts ? 1 : 0, h->cl_lcap);
+        const int blk = h->prm.block_size ? std::min(h->prm.block_size, kClusterMaxBlock) : 256;
+        int active = 0;
+        const bool ok = need <= (size_t)smem_optin && cluster_configure(blk, need) == cudaSuccess &&
+                        cluster_max_active(h->cl_size, blk, need, &active) == cudaSuccess && active >= 1;
+        if (!ok) {
+            cudaGetLastError();
+            if (need > (size_t)smem_optin - 4096 && shrink_tries < 4) {
+                ++shrink_tries;
+                cap_slice = (uint32_t)((double)cap_slice * (double)(smem_optin - 4096) / (double)need * 0.97);
+                goto plan_again;
+            }
+            if (h->prm.exec_mode == SBS_EXEC_CLUSTER)
+                return fail(h, SBS_EINVAL, "scene does not fit the cluster-resident mode");
+            allow_cluster = false;
+            goto plan_again;
+        }
     }
     // 4. block size
     h->block = h->prm.block_size ? h->prm.block_size : 256;
@@ -754,6 +928,39 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
                 if (fc[((uint64_t)s3[0] * V + s3[1]) * (uint64_t)V + s3[2]] == 1) h->bmask[k] |= (uint8_t)(1u << f);
             }
         }
+        // visual models (tetrahedral_mesh_boundary.cpp:76-120): the mesh lists
+        // each distinct face once, at its first appearance over tets in input
+        // order and faces_copy order, with that appearance's winding; boundary
+        // faces are those with != 2 incident tets; surface vertices are
+        // numbered by first appearance in the boundary triangles
+        h->vis_tri0.assign(1, 0);
+        h->vis_sv0.assign(1, 0);
+        h->vis_tris.clear();
+        h->vis_map.clear();
+        std::unordered_map<uint64_t, uint8_t> emitted;
+        for (const BodyHost& b : h->bodies) {
+            std::unordered_map<uint32_t, uint32_t> local;
+            for (uint32_t t = b.t0; t < b.t0 + b.nt; ++t) {
+                const uint32_t* q = &h->tets[4ull * t];
+                const uint32_t fl[4][3] = {{q[0], q[1], q[3]}, {q[1], q[2], q[3]}, {q[2], q[0], q[3]}, {q[0], q[2], q[1]}};
+                for (auto& f : fl) {
+                    uint32_t s3[3] = {f[0], f[1], f[2]};
+                    std::sort(s3, s3 + 3);
+                    const uint64_t key = ((uint64_t)s3[0] * V + s3[1]) * (uint64_t)V + s3[2];
+                    if (fc[key] == 2 || !emitted.emplace(key, 1).second) continue;
+                    for (int j = 0; j < 3; ++j) {
+                        auto it = local.find(f[j]);
+                        if (it == local.end()) {
+                            it = local.emplace(f[j], (uint32_t)(h->vis_map.size() - h->vis_sv0.back())).first;
+                            h->vis_map.push_back(f[j] - b.v0);
+                        }
+                        h->vis_tris.push_back(it->second);
+                    }
+                }
+            }
+            h->vis_tri0.push_back((uint32_t)(h->vis_tris.size() / 3));
+            h->vis_sv0.push_back((uint32_t)h->vis_map.size());
+        }
     }
     // 9. device allocations and upload
     SceneDev& d = h->d;
@@ -767,7 +974,8 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     if (need_acc) { AL(d.acc, V); } else d.acc = nullptr;
     AL(d.model, T); AL(d.tet, T); AL(d.dm0, T); AL(d.dm1, T); AL(d.dm2, T); AL(d.lam0, T); AL(d.lam1, T);
     AL(d.surf, d.n_surf);
-    const size_t ncont = (size_t)kMaxPlanes * d.n_surf;
+    // kMaxPlanes ground-contact segments, then the body-contact segment
+    const size_t ncont = (size_t)(kMaxPlanes + 1) * d.n_surf;
     AL(d.contacts, ncont); AL(d.contact_lam, ncont);
     AL(d.counters, 16);
     AL(d.time, 1); AL(d.err, 1); AL(d.bar, 2);
@@ -777,6 +985,29 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     d.kin_vert = nullptr;
     d.kin_rel = nullptr;
     d.body_contact_cap = 0;
+    // distance constraints in colour order, ends in library vertex slots
+    d.n_edges = (uint32_t)h->dist_p.size();
+    d.edge = nullptr;
+    d.edge_p = nullptr;
+    d.edge_lam = nullptr;
+    if (d.n_edges) {
+        const int KE = colour_edges(h->dist_v, V, h->edge_order, h->edge_offsets);
+        if (KE < 0 || KE > kMaxEdgeColours)
+            return fail(h, SBS_ECOLOUR, "distance constraints need more than 64 colours");
+        std::vector<uint2> ev(d.n_edges);
+        std::vector<float4> ep(d.n_edges);
+        for (uint32_t k = 0; k < d.n_edges; ++k) {
+            const uint32_t e = h->edge_order[k];
+            ev[k] = make_uint2(old_to_new[h->dist_v[2ull * e]], old_to_new[h->dist_v[2ull * e + 1]]);
+            ep[k] = h->dist_p[e];
+        }
+        if ((s = dalloc(h, &d.edge, d.n_edges)) != SBS_OK) return s;
+        if ((s = dalloc(h, &d.edge_p, d.n_edges)) != SBS_OK) return s;
+        if ((s = dalloc(h, &d.edge_lam, d.n_edges)) != SBS_OK) return s;
+        if ((s = upload(h, d.edge, ev.data(), ev.size() * sizeof(uint2))) != SBS_OK) return s;
+        if ((s = upload(h, d.edge_p, ep.data(), ep.size() * sizeof(float4))) != SBS_OK) return s;
+        CU(h, cudaMemsetAsync(d.edge_lam, 0, d.n_edges * sizeof(float), h->st));
+    }
     if ((s = upload(h, d.xi, xw.data(), V * sizeof(float4))) != SBS_OK) return s;
     if ((s = upload(h, d.xn, xw.data(), V * sizeof(float4))) != SBS_OK) return s;
     if ((s = upload(h, d.v, vel.data(), V * sizeof(float4))) != SBS_OK) return s;
@@ -791,6 +1022,42 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
         if ((s = upload(h, d.model, mdl.data(), T)) != SBS_OK) return s;
     }
     if ((s = upload(h, d.surf, h->surf.data(), d.n_surf * sizeof(uint32_t))) != SBS_OK) return s;
+    {
+        // visual models on the device: slots, triangle corners, incidence
+        SurfaceDev& sd = h->sd;
+        sd.n_sv = (uint32_t)h->vis_map.size();
+        sd.n_tri = (uint32_t)(h->vis_tris.size() / 3);
+        std::vector<uint32_t> slot(sd.n_sv), cnt(sd.n_sv + 1, 0), inc(3ull * sd.n_tri);
+        std::vector<uint4> tri(sd.n_tri);
+        for (size_t b = 0; b < h->bodies.size(); ++b) {
+            const uint32_t v0 = h->bodies[b].v0, sv0 = h->vis_sv0[b];
+            for (uint32_t i = sv0; i < h->vis_sv0[b + 1]; ++i) slot[i] = old_to_new[v0 + h->vis_map[i]];
+            for (uint32_t k = h->vis_tri0[b]; k < h->vis_tri0[b + 1]; ++k) {
+                const uint32_t* c = &h->vis_tris[3ull * k];
+                tri[k] = make_uint4(slot[sv0 + c[0]], slot[sv0 + c[1]], slot[sv0 + c[2]], 0u);
+                for (int j = 0; j < 3; ++j) cnt[sv0 + c[j] + 1]++;
+            }
+        }
+        for (uint32_t i = 0; i < sd.n_sv; ++i) cnt[i + 1] += cnt[i];
+        std::vector<uint32_t> fill(cnt.begin(), cnt.end() - 1);
+        for (size_t b = 0; b < h->bodies.size(); ++b)
+            for (uint32_t k = h->vis_tri0[b]; k < h->vis_tri0[b + 1]; ++k)
+                for (int j = 0; j < 3; ++j) inc[fill[h->vis_sv0[b] + h->vis_tris[3ull * k + j]]++] = k;
+        if ((s = dalloc(h, &sd.slot, sd.n_sv)) != SBS_OK) return s;
+        if ((s = dalloc(h, &sd.inc_start, sd.n_sv + 1)) != SBS_OK) return s;
+        if ((s = dalloc(h, &sd.inc, 3ull * sd.n_tri)) != SBS_OK) return s;
+        if ((s = dalloc(h, &sd.tri, sd.n_tri)) != SBS_OK) return s;
+        if ((s = dalloc(h, &sd.normal, sd.n_sv)) != SBS_OK) return s;
+        if ((s = dalloc(h, &sd.stage, 6ull * sd.n_sv)) != SBS_OK) return s;
+        if ((s = upload(h, sd.slot, slot.data(), slot.size() * 4)) != SBS_OK) return s;
+        if ((s = upload(h, sd.inc_start, cnt.data(), cnt.size() * 4)) != SBS_OK) return s;
+        if ((s = upload(h, sd.inc, inc.data(), inc.size() * 4)) != SBS_OK) return s;
+        if ((s = upload(h, sd.tri, tri.data(), tri.size() * sizeof(uint4))) != SBS_OK) return s;
+        // the body constructor's update_visual_model (tetrahedral_body.cpp:25)
+        CU(h, cudaMemsetAsync(sd.normal, 0, sd.n_sv * sizeof(float4), h->st));
+        CU(h, launch_surface_update(sd, d.xn, 0, sd.n_sv, 1, nullptr, 6, h->st));
+        CU(h, cudaStreamSynchronize(h->st));   // host vectors above go out of scope
+    }
     CU(h, cudaMemsetAsync(d.lam0, 0, T * sizeof(float), h->st));
     CU(h, cudaMemsetAsync(d.lam1, 0, T * sizeof(float), h->st));
     CU(h, cudaMemsetAsync(d.counters, 0, 16 * sizeof(uint32_t), h->st));
@@ -917,6 +1184,8 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     p.has_acc = h->has_acc ? 1 : 0;
     p.body_contacts = h->body_on ? 1 : 0;
     for (size_t i = 0; i < h->groups.size(); ++i) p.kin[i] = h->groups[i];
+    p.n_edge_colours = d.n_edges ? (int)h->edge_offsets.size() - 1 : 0;
+    for (int c = 0; c <= p.n_edge_colours && d.n_edges; ++c) p.edge_start[c] = h->edge_offsets[c];
     if (h->global_modes) {
         p.n_colours = K;
         for (int c = 0; c <= K; ++c) p.colour_start[c] = h->colour_offsets[c];
@@ -947,6 +1216,31 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
             h->cl_grid = std::max(1, std::min(active, (int)h->cd.n_groups));
         }
     }
+    // wavefront mode: one CTA slice of every colour per CTA, neighbour waits
+    h->d.prog = nullptr;
+    h->d.nb_start = nullptr;
+    h->d.nb = nullptr;
+    h->wave_grid = 0;
+    if (h->global_modes && h->prm.exec_mode != SBS_EXEC_CLUSTER) {
+        int wocc = 0;
+        if (wavefront_occupancy(256, &wocc) == cudaSuccess && wocc > 0) {
+            const int G = wocc * h->n_sm;
+            std::vector<uint32_t> st_, nb_;
+            wave_neighbours(tid, h->colour_offsets, K, G, st_, nb_);
+            if ((s = dalloc(h, &h->d.prog, G)) != SBS_OK) return s;
+            if ((s = dalloc(h, &h->d.nb_start, G + 1)) != SBS_OK) return s;
+            if ((s = dalloc(h, &h->d.nb, nb_.size())) != SBS_OK) return s;
+            if ((s = upload(h, h->d.nb_start, st_.data(), st_.size() * 4)) != SBS_OK) return s;
+            if ((s = upload(h, h->d.nb, nb_.data(), nb_.size() * 4)) != SBS_OK) return s;
+            CU(h, cudaStreamSynchronize(h->st));
+            h->wave_grid = G;
+            h->wave_max_nb = 0;
+            for (int b = 0; b < G; ++b) h->wave_max_nb = std::max(h->wave_max_nb, st_[b + 1] - st_[b]);
+        }
+        cudaGetLastError();
+    }
+    if (h->prm.exec_mode == SBS_EXEC_WAVEFRONT && !h->wave_grid)
+        return fail(h, SBS_EINVAL, "scene does not run in the wavefront mode");
     if (!h->global_modes && !h->cl_feasible) return fail(h, SBS_ESTATE, "no execution mode fits this scene");
     if (h->prm.exec_mode == SBS_EXEC_CLUSTER && !h->cl_feasible)
         return fail(h, SBS_EINVAL, "scene does not fit the cluster-resident mode");
@@ -989,6 +1283,7 @@ static sbs_status enqueue_frame_kernels(sbs_gpu* h, const StepParams& p) {
             CU(h, launch_body_contacts(d, p, it == 0, st));
             for (int c = 0; c < p.first_tail; ++c) CU(h, launch_colour(d, p, c, it == 0, h->block, h->grid, st));
             CU(h, launch_tail(d, p, it == 0, h->block, st));
+            for (int c = 0; c < p.n_edge_colours; ++c) CU(h, launch_edges(d, p, c, it == 0, st));
         }
         CU(h, launch_finalize(d, p, st));
     }
@@ -1004,6 +1299,7 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
     fill_params(h, p, dt, substeps, iterations);
     double t_end = h->sim_time;
     for (uint32_t k = 0; k < substeps; ++k) t_end += dt;   // same double sequence as the CPU loop
+    const uint64_t launches0 = launch_counter();
     if (h->mlp) {
         // learned warm start: per substep predict -> features -> MLP -> fit
         // sweep, then the sweeps continue from the fitted multipliers
@@ -1025,21 +1321,32 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
         CU(h, launch_cluster_frame(h->d, h->cd, p, h->sim_time, h->cl_grid, h->cl_block, h->cl_smem, h->st));
         CU(h, launch_end_frame(h->d, h->st));
         CU(h, launch_store_time(h->d.time, t_end, h->st));
+    } else if (h->exec_mode == SBS_EXEC_WAVEFRONT) {
+        if (h->contacts_live)
+            CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+        if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
+        CU(h, cudaMemsetAsync(h->d.bar, 0, 2 * sizeof(unsigned), h->st));
+        CU(h, cudaMemsetAsync(h->d.prog, 0, h->wave_grid * sizeof(uint32_t), h->st));
+        CU(h, launch_wavefront_frame(h->d, p, 256, h->wave_grid, h->st));
     } else if (h->exec_mode == SBS_EXEC_PERSISTENT) {
         // the frame kernel expects zero live contact counters (it zeroes them
         // itself at frame end); a standalone detect may have left them set
         if (h->contacts_live)
             CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
         if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
+        CU(h, cudaMemsetAsync(h->d.bar, 0, 2 * sizeof(unsigned), h->st));   // barrier arrival count
         CU(h, launch_persistent_frame(h->d, p, h->pers_block, h->pers_grid, h->st));
     } else {
         GraphKey key{dt, substeps, iterations};
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             cudaGraph_t g;
+            const uint64_t k0 = launch_counter();
             CU(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
             sbs_status s = enqueue_frame_kernels(h, p);
             cudaError_t e = cudaStreamEndCapture(h->st, &g);
+            h->graph_kernels[key] = launch_counter() - k0;
+            launch_counter() = k0;   // captured, not run
             if (s != SBS_OK) return s;
             if (e != cudaSuccess) return fail(h, SBS_ECUDA, std::string("capture: ") + cudaGetErrorString(e));
             cudaGraphExec_t ge;
@@ -1049,11 +1356,14 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
             it = h->graphs.emplace(key, ge).first;
         }
         CU(h, cudaGraphLaunch(it->second, h->st));
+        count_launch(h->graph_kernels[key]);
     }
+    h->kernel_launches += launch_counter() - launches0;
     h->frames++;
     h->projections += (uint64_t)substeps * iterations * h->n_tets;
     h->contacts_live = false;
     h->sim_time = t_end;
+    if (!h->mlp) h->xpred_valid = false;   // a plain frame does not record its predictions
     return SBS_OK;
 }
 
@@ -1092,6 +1402,7 @@ static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t it
         }
     }
     if (h->global_modes) cands.push_back({SBS_EXEC_GRAPH, 256, h->grid});
+    if (h->wave_grid) cands.push_back({SBS_EXEC_WAVEFRONT, 256, h->wave_grid});
     const int saved_mode = h->exec_mode, saved_pb = h->pers_block, saved_pg = h->pers_grid;
     const uint64_t saved_frames = h->frames, saved_proj = h->projections;
     const double saved_time = h->sim_time;
@@ -1221,19 +1532,7 @@ sbs_status sbs_gpu_solve(sbs_gpu* h, double dt, uint32_t iterations) {
     if (!h->contacts_live) CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
     // one launch per vertex-disjoint colour segment (all groups' colours in
     // sweep order), whatever the execution mode of sbs_gpu_step
-    for (uint32_t it = 0; it < iterations; ++it) {
-        CU(h, launch_contacts(h->d, p, it == 0, h->st));
-        CU(h, launch_body_contacts(h->d, p, it == 0, h->st));
-        for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c) {
-            StepParams q = p;
-            q.n_colours = 1;
-            q.first_tail = 1;
-            q.colour_start[0] = h->colour_offsets[c];
-            q.colour_start[1] = h->colour_offsets[c + 1];
-            q.colour_split[0] = h->seg_split[c];
-            CU(h, launch_colour(h->d, q, 0, it == 0, h->block, h->grid, h->st));
-        }
-    }
+    if ((s = enqueue_segments(h, p, iterations, true)) != SBS_OK) return s;
     h->projections += (uint64_t)iterations * h->n_tets;
     return SBS_OK;
 }
@@ -1266,9 +1565,18 @@ static sbs_status body_range(sbs_gpu* h, int32_t body, const BodyHost** b) {
     return SBS_OK;
 }
 
+// body >= 0: one body; body == -1: the whole scene in global vertex order
+static sbs_status state_range(sbs_gpu* h, int32_t body, const BodyHost** b) {
+    if (body != -1) return body_range(h, body, b);
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    *b = &h->all_bodies;
+    return SBS_OK;
+}
+
 static sbs_status read_field(sbs_gpu* h, int32_t body, const float4* dsrc, float* out, bool check) {
     const BodyHost* b;
-    sbs_status s = body_range(h, body, &b);
+    sbs_status s = state_range(h, body, &b);
     if (s) return s;
     CU(h, cudaMemcpyAsync(h->h_stage, dsrc + b->v0, b->nv * sizeof(float4), cudaMemcpyDeviceToHost, h->st));
     CU(h, cudaStreamSynchronize(h->st));
@@ -1301,7 +1609,7 @@ sbs_status sbs_gpu_get_predicted(sbs_gpu* h, int32_t body, float* xi) {
 
 static sbs_status write_positions(sbs_gpu* h, int32_t body, const float* x, bool all) {
     const BodyHost* b;
-    sbs_status s = body_range(h, body, &b);
+    sbs_status s = state_range(h, body, &b);
     if (s) return s;
     CU(h, cudaStreamSynchronize(h->st));  // staging buffer reuse
     for (uint32_t o = 0; o < b->nv; ++o) {
@@ -1318,11 +1626,12 @@ static sbs_status write_positions(sbs_gpu* h, int32_t body, const float* x, bool
 
 sbs_status sbs_gpu_set_state(sbs_gpu* h, int32_t body, const float* x, const float* v) {
     if (!h) return SBS_EINVAL;
+    h->xpred_valid = false;
     sbs_status s;
     if (x && (s = write_positions(h, body, x, true)) != SBS_OK) return s;
     if (v) {
         const BodyHost* b;
-        if ((s = body_range(h, body, &b)) != SBS_OK) return s;
+        if ((s = state_range(h, body, &b)) != SBS_OK) return s;
         for (uint32_t o = 0; o < b->nv; ++o) {
             const uint32_t n = b->old_to_new[o];
             float flag = 0.0f;
@@ -1337,6 +1646,7 @@ sbs_status sbs_gpu_set_state(sbs_gpu* h, int32_t body, const float* x, const flo
 
 sbs_status sbs_gpu_set_predicted(sbs_gpu* h, int32_t body, const float* xi) {
     if (!h || !xi) return fail(h, SBS_EINVAL, "null");
+    h->xpred_valid = false;
     sbs_status s = write_positions(h, body, xi, false);
     if (s) return s;
     CU(h, cudaStreamSynchronize(h->st));
@@ -1368,6 +1678,33 @@ sbs_status sbs_gpu_get_lambdas(sbs_gpu* h, float* lambdas) {
         lambdas[2ull * h->tet_order[k]] = a[k];
         lambdas[2ull * h->tet_order[k] + 1] = b[k];
     }
+    return check_err(h);
+}
+
+sbs_status sbs_gpu_get_distance_order(sbs_gpu* h, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
+                                      uint32_t* n_colours) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    const uint32_t K = h->d.n_edges ? (uint32_t)h->edge_offsets.size() - 1 : 0;
+    if (n_colours) *n_colours = K;
+    if (order) std::copy(h->edge_order.begin(), h->edge_order.end(), order);
+    if (offsets && K) {
+        if (cap_offsets < K + 1) return fail(h, SBS_EINVAL, "offsets capacity");
+        std::copy(h->edge_offsets.begin(), h->edge_offsets.end(), offsets);
+    }
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_distance_lambdas(sbs_gpu* h, float* lambdas) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!lambdas) return fail(h, SBS_EINVAL, "null");
+    const uint32_t E = h->d.n_edges;
+    if (!E) return SBS_OK;
+    std::vector<float> a(E);
+    CU(h, cudaMemcpyAsync(a.data(), h->d.edge_lam, E * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    for (uint32_t k = 0; k < E; ++k) lambdas[h->edge_order[k]] = a[k];
     return check_err(h);
 }
 
@@ -1469,24 +1806,32 @@ static sbs_status warm_prepare(sbs_gpu* h) {
     return SBS_OK;
 }
 
-sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m) {
+sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps) {
     sbs_status s = check_ready(h);
     if (s) return s;
+    if (m && (fit_sweeps < 1 || fit_sweeps > 16)) return fail(h, SBS_EINVAL, "fit_sweeps must be 1..16");
     if (m && m->d.device != h->prm.device) return fail(h, SBS_EINVAL, "MLP lives on another device");
     if (m && (s = warm_prepare(h)) != SBS_OK) return s;
     if (m) CU(h, mlp_reserve(m->d, (int)h->n_verts));
     h->mlp = m;
+    if (m) h->fit_sweeps = fit_sweeps;
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
+    h->graph_kernels.clear();
     return SBS_OK;
 }
 
 // features -> MLP -> fit sweep (multipliers initialised), on the predicted state
 static sbs_status enqueue_warm_init(sbs_gpu* h, const StepParams& p) {
-    CU(h, launch_features(h->d, h->wd, p, h->st));
+    CU(h, launch_features(h->d, h->wd, p, h->xpred_valid ? 1 : 0, h->st));
+    h->xpred_valid = true;
     CU(h, mlp_forward_dev(h->mlp->d, h->wd.feat, (int)h->n_verts, h->wd.delta, h->st));
-    for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c)
-        CU(h, launch_fit_segment(h->d, h->wd, p, h->colour_offsets[c], h->colour_offsets[c + 1], h->st));
+    for (uint32_t k = 0; k < h->fit_sweeps; ++k)
+        for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c)
+            CU(h, launch_fit_segment(h->d, h->wd, p, h->colour_offsets[c], h->colour_offsets[c + 1], k == 0 ? 1 : 0,
+                                     h->st));
     CU(h, cudaMemsetAsync(h->d.contact_lam, 0, (size_t)(kMaxPlanes + 1) * h->d.n_surf * sizeof(float), h->st));
+    if (h->d.n_edges) CU(h, cudaMemsetAsync(h->d.edge_lam, 0, h->d.n_edges * sizeof(float), h->st));
     return SBS_OK;
 }
 
@@ -1514,6 +1859,7 @@ static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t ite
             q.colour_split[0] = h->seg_split[c];
             CU(h, launch_colour(h->d, q, 0, first, h->block, h->grid, h->st));
         }
+        for (int c = 0; c < p.n_edge_colours; ++c) CU(h, launch_edges(h->d, p, c, first, h->st));
     }
     return SBS_OK;
 }
@@ -1537,7 +1883,8 @@ sbs_status sbs_gpu_get_features(sbs_gpu* h, float* feat) {
     if ((s = warm_prepare(h)) != SBS_OK) return s;
     StepParams p;
     fill_params(h, p, 1.0, 1, 1);
-    CU(h, launch_features(h->d, h->wd, p, h->st));
+    CU(h, launch_features(h->d, h->wd, p, h->xpred_valid ? 1 : 0, h->st));
+    h->xpred_valid = true;
     std::vector<float> buf(16ull * h->n_verts);
     CU(h, cudaMemcpyAsync(buf.data(), h->wd.feat, buf.size() * 4, cudaMemcpyDeviceToHost, h->st));
     CU(h, cudaStreamSynchronize(h->st));
@@ -1566,6 +1913,55 @@ sbs_status sbs_gpu_get_surface(sbs_gpu* h, uint32_t* verts, uint32_t cap, uint32
     return SBS_OK;
 }
 
+sbs_status sbs_gpu_get_surface_mesh(sbs_gpu* h, int32_t body, uint32_t* triangles, uint32_t cap_triangles,
+                                    uint32_t* n_triangles, uint32_t* vertex_map, uint32_t cap_vertices,
+                                    uint32_t* n_vertices) {
+    const BodyHost* b;
+    sbs_status s = body_range(h, body, &b);
+    if (s) return s;
+    const uint32_t t0 = h->vis_tri0[body], nt = h->vis_tri0[body + 1] - t0;
+    const uint32_t v0 = h->vis_sv0[body], nv = h->vis_sv0[body + 1] - v0;
+    if (n_triangles) *n_triangles = nt;
+    if (n_vertices) *n_vertices = nv;
+    if (triangles) {
+        if (cap_triangles < nt) return fail(h, SBS_EINVAL, "triangle capacity");
+        std::copy(&h->vis_tris[3ull * t0], &h->vis_tris[3ull * t0] + 3ull * nt, triangles);
+    }
+    if (vertex_map) {
+        if (cap_vertices < nv) return fail(h, SBS_EINVAL, "vertex capacity");
+        std::copy(&h->vis_map[v0], &h->vis_map[v0] + nv, vertex_map);
+    }
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_update_surface(sbs_gpu* h, int32_t body, int32_t accumulate_normals, float* vertex_buffer,
+                                  uint32_t stride) {
+    const BodyHost* b;
+    sbs_status s = body_range(h, body, &b);
+    if (s) return s;
+    if (vertex_buffer && stride < 6) return fail(h, SBS_EINVAL, "stride must be >= 6 floats");
+    const uint32_t v0 = h->vis_sv0[body], nv = h->vis_sv0[body + 1] - v0;
+    bool on_device = false;
+    if (vertex_buffer) {
+        cudaPointerAttributes attr{};
+        CU(h, cudaPointerGetAttributes(&attr, vertex_buffer));
+        on_device = attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+        if (on_device && attr.device != h->prm.device) return fail(h, SBS_EINVAL, "buffer lives on another device");
+    }
+    float* out = !vertex_buffer ? nullptr : on_device ? vertex_buffer : h->sd.stage;
+    CU(h, launch_surface_update(h->sd, h->d.xn, v0, nv, accumulate_normals ? 1 : 0, out, on_device ? stride : 6,
+                                h->st));
+    if (vertex_buffer && !on_device) {
+        std::vector<float> buf(6ull * nv);
+        CU(h, cudaMemcpyAsync(buf.data(), h->sd.stage, buf.size() * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+        CU(h, cudaStreamSynchronize(h->st));
+        for (uint32_t i = 0; i < nv; ++i) std::copy(&buf[6ull * i], &buf[6ull * i + 6], vertex_buffer + (size_t)i * stride);
+    } else {
+        CU(h, cudaStreamSynchronize(h->st));
+    }
+    return check_err(h);
+}
+
 sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st) {
     sbs_status s = check_ready(h);
     if (s) return s;
@@ -1584,15 +1980,18 @@ sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st) {
     for (size_t pl = 0; pl < h->planes.size(); ++pl) st->n_contacts += c[pl];
     st->n_body_contacts = c[kMaxPlanes];
     st->exec_mode = h->exec_mode;
-    st->grid_ctas = h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_grid
+    st->grid_ctas = h->exec_mode == SBS_EXEC_WAVEFRONT     ? h->wave_grid
+                    : h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_grid
                     : h->exec_mode == SBS_EXEC_CLUSTER  ? h->cl_grid * h->cl_size
                                                         : h->grid;
-    st->block_size = h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_block
+    st->block_size = h->exec_mode == SBS_EXEC_WAVEFRONT     ? 256
+                     : h->exec_mode == SBS_EXEC_PERSISTENT ? h->pers_block
                      : h->exec_mode == SBS_EXEC_CLUSTER  ? h->cl_block
                                                          : h->block;
     st->residual = h->residual;
     st->energy = h->energy;
     st->last_frame_ms = h->last_frame_ms;
+    st->kernel_launches = h->kernel_launches;
     return check_err(h);
 }
 

@@ -17,6 +17,7 @@
 #include <stdint.h>
 
 #include "cluster_internal.cuh"
+#include "launch_count.cuh"
 #include "xpbd_internal.cuh"
 #include "xpbd_math.cuh"
 
@@ -40,6 +41,7 @@ __device__ __forceinline__ uint32_t cl_count() {
 __device__ __forceinline__ void cluster_sync() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -64,17 +66,37 @@ __device__ __forceinline__ uint32_t vaddr(uint32_t packed, uint32_t xi_base) {
     return map_rank(xi_base + ((packed & 0xFFFFFFu) << 4), packed >> 24);
 }
 
+// The read-only part of a tet's record: the DSMEM addresses of its corners'
+// xi and its rest data.  (Loading the next colour's record across the
+// cluster barrier was measured slower: 6.9 against 6.3 ms per frame of the
+// 98k-tet beam.)
+struct ClTet {
+    uint32_t a0, a1, a2, a3;
+    float4 a, b, c;   // DmInv rows; w: V0, mu, lambda
+    uint32_t snh;
+};
+
+__device__ __forceinline__ ClTet cl_load_tet(const SceneDev& s, const ClusterDev& c, uint32_t t, uint32_t xi_base) {
+    ClTet r;
+    const uint4 id = __ldg(&c.tet_packed[t]);
+    r.a0 = vaddr(id.x, xi_base);
+    r.a1 = vaddr(id.y, xi_base);
+    r.a2 = vaddr(id.z, xi_base);
+    r.a3 = vaddr(id.w, xi_base);
+    r.a = __ldg(&s.dm0[t]);
+    r.b = __ldg(&s.dm1[t]);
+    r.c = __ldg(&s.dm2[t]);
+    r.snh = s.model[t] != 0;
+    return r;
+}
+
 // lam: this tet's multipliers in the CTA's shared memory (lam[0]; SNH's
 // hydrostatic one at lam[lstride]).
-__device__ __forceinline__ void project_tet_dsmem(const SceneDev& s, const ClusterDev& c, const StepParams& p,
-                                                  uint32_t t, bool snh, bool first, uint32_t xi_base, float* lam,
-                                                  uint32_t lstride) {
-    const uint4 id = __ldg(&c.tet_packed[t]);
-    const float4 a = __ldg(&s.dm0[t]);
-    const float4 b = __ldg(&s.dm1[t]);
-    const float4 cc = __ldg(&s.dm2[t]);
-    const uint32_t a0 = vaddr(id.x, xi_base), a1 = vaddr(id.y, xi_base), a2 = vaddr(id.z, xi_base),
-                   a3 = vaddr(id.w, xi_base);
+__device__ __forceinline__ void project_tet_dsmem(const ClusterDev& c, const StepParams& p, const ClTet& T,
+                                                  bool first, float* lam, uint32_t lstride) {
+    const bool snh = T.snh != 0;
+    const float4 a = T.a, b = T.b, cc = T.c;
+    const uint32_t a0 = T.a0, a1 = T.a1, a2 = T.a2, a3 = T.a3;
     float4 q0 = ld_dsmem(a0), q1 = ld_dsmem(a1), q2 = ld_dsmem(a2), q3 = ld_dsmem(a3);
     const float w[4] = {q0.w, q1.w, q2.w, q3.w};
     const f3 x0 = mk(q0), x1 = mk(q1), x2 = mk(q2), x3 = mk(q3);
@@ -237,6 +259,12 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
             cluster_sync();
             for (int it = 0; it < p.iterations; ++it) {
                 const bool first = it == 0;
+                // this CTA's tets of colour `col`: those owning most of their vertices here
+                auto col_range = [&](uint32_t col, uint32_t& b, uint32_t& e) {
+                    const uint32_t k = gd.col_base + col * C + rank;
+                    b = c.col_start[k];
+                    e = c.col_start[k + 1];
+                };
                 // contacts: own vertices only (collision_constraint.cpp:21-41)
                 for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
                     const uint32_t i = clist[k];
@@ -267,12 +295,11 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                 }
                 if (S > 0) cluster_sync();  // cluster-uniform condition
                 for (uint32_t col = 0; col < gd.n_col; ++col) {
-                    // this CTA's tets of the colour: those owning most of their vertices here
-                    const uint32_t k = gd.col_base + col * C + rank;
-                    const uint32_t b = c.col_start[k], e = c.col_start[k + 1];
+                    uint32_t b, e;
+                    col_range(col, b, e);
                     float* lb = lam_s + c.lam_base[gd.lb_base + col * C + rank] - b;
                     for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
-                        project_tet_dsmem(s, c, p, tt, s.model[tt] != 0, first, xi_base, lb + tt, c.lcap);
+                        project_tet_dsmem(c, p, cl_load_tet(s, c, tt, xi_base), first, lb + tt, c.lcap);
                     cluster_sync();
                 }
             }
@@ -356,6 +383,7 @@ cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const S
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    count_launch();
     return cudaLaunchKernelEx(&cfg, k_cluster_frame, s, c, p, t0);
 }
 
@@ -363,6 +391,7 @@ __global__ void k_store_time(double* t, double v) { *t = v; }
 
 cudaError_t launch_store_time(double* t, double v, cudaStream_t st) {
     k_store_time<<<1, 1, 0, st>>>(t, v);
+    count_launch();
     return cudaGetLastError();
 }
 

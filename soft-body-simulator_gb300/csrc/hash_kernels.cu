@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "hash_internal.cuh"
+#include "launch_count.cuh"
 #include "xpbd_internal.cuh"
 #include "xpbd_math.cuh"
 
@@ -246,20 +247,31 @@ cudaError_t launch_body_detect(const SceneDev& s, const HashDev& hd, cudaStream_
     if ((e = cudaMemsetAsync(hd.best, 0, (size_t)s.n_verts * sizeof(unsigned long long), st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(hd.n_cand, 0, sizeof(unsigned long long), st)) != cudaSuccess) return e;
     k_hash_insert<<<blocks_for(s.n_surf, 4096), 256, 0, st>>>(s, hd);
+    count_launch();
     const uint32_t tiles = (cap + 1023) / 1024;
     k_scan_tiles<<<tiles, 1024, 0, st>>>(hd.count, hd.start, hd.tile_sums, cap);
+    count_launch();
     if (tiles > 1) {
         // tiles <= 4096 -> at most 4 levels; the second level fits one CTA for tiles <= 1024
         k_scan_tiles<<<(tiles + 1023) / 1024, 1024, 0, st>>>(hd.tile_sums, hd.tile_scan, hd.tile_sums2, tiles);
+        count_launch();
         if (tiles > 1024) {
             k_scan_tiles<<<1, 1024, 0, st>>>(hd.tile_sums2, hd.tile_scan2, nullptr, (tiles + 1023) / 1024);
+            count_launch();
             k_scan_add<<<(tiles + 1023) / 1024, 1024, 0, st>>>(hd.tile_scan, hd.tile_scan2, tiles);
+            count_launch();
         }
         k_scan_add<<<tiles, 1024, 0, st>>>(hd.start, hd.tile_scan, cap);
+        count_launch();
     }
     k_hash_fill<<<blocks_for(s.n_surf, 4096), 256, 0, st>>>(s, hd);
-    if (hd.n_query) k_hash_query<<<blocks_for(hd.n_query, 8192), 256, 0, st>>>(s, hd);
+    count_launch();
+    if (hd.n_query) {
+        k_hash_query<<<blocks_for(hd.n_query, 8192), 256, 0, st>>>(s, hd);
+        count_launch();
+    }
     k_body_contacts<<<blocks_for(s.n_surf, 4096), 256, 0, st>>>(s, hd);
+    count_launch();
     return cudaGetLastError();
 }
 

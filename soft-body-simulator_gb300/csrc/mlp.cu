@@ -19,6 +19,7 @@
 
 #include "../../include/sbs_gpu.h"
 #include "mlp_internal.cuh"
+#include "launch_count.cuh"
 
 namespace sbs {
 
@@ -136,6 +137,7 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
 static cudaError_t gemm(const GemmArgs& g, cudaStream_t st) {
     dim3 grid((g.N + GN - 1) / GN, (g.M + GM - 1) / GM, g.splitk > 1 ? g.splitk : 1);
     k_gemm<<<grid, 128, 0, st>>>(g);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -246,6 +248,7 @@ cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cuda
     cudaError_t e;
     if ((e = mlp_reserve(d, n)) != cudaSuccess) return e;
     k_norm_in<<<nb((long long)n * kIn), 256, 0, st>>>(x, d.mean, d.inv_std, d.xn, n);
+    count_launch();
     const __nv_bfloat16* in = d.xn;
     int kin = kIn;
     for (int l = 0; l < 3; ++l) {
@@ -265,7 +268,10 @@ cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cuda
     g.C = d.z[3]; g.ldc = kOut; g.beta = 0.0f; g.bias = d.b[3];
     g.M = n; g.N = kOut; g.K = kHid;
     if ((e = gemm(g, st)) != cudaSuccess) return e;
-    if (y_raw) k_scale_out<<<nb((long long)n * kOut), 256, 0, st>>>(d.z[3], d.out_scale, y_raw, n);
+    if (y_raw) {
+        k_scale_out<<<nb((long long)n * kOut), 256, 0, st>>>(d.z[3], d.out_scale, y_raw, n);
+        count_launch();
+    }
     return cudaGetLastError();
 }
 
@@ -275,6 +281,7 @@ cudaError_t mlp_backward_dev(MlpDev& d, const float* x, const float* t, int n, c
     if ((e = mlp_forward_dev(d, x, n, nullptr, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(d.loss, 0, sizeof(float), st)) != cudaSuccess) return e;
     k_loss<<<nb((long long)n * kOut), 256, 0, st>>>(d.z[3], t, d.out_scale, d.dz[3], d.dzb[3], d.loss, n);
+    count_launch();
     const int fin[4] = {kIn, kHid, kHid, kHid};
     const int fout[4] = {kHid, kHid, kHid, kOut};
     for (int l = 3; l >= 0; --l) {
@@ -291,6 +298,7 @@ cudaError_t mlp_backward_dev(MlpDev& d, const float* x, const float* t, int n, c
             return e;
         if ((e = gemm(g, st)) != cudaSuccess) return e;
         k_colsum<<<fout[l], 256, 0, st>>>(d.dz[l], d.grad + d.boff[l], n, fout[l]);
+        count_launch();
         if (l == 0) break;
         // da_{l-1}[r][i] = sum_o dz_l[r][o] * W_l[o][i]
         GemmArgs h{};
@@ -300,6 +308,7 @@ cudaError_t mlp_backward_dev(MlpDev& d, const float* x, const float* t, int n, c
         h.M = n; h.N = fin[l]; h.K = fout[l];
         if ((e = gemm(h, st)) != cudaSuccess) return e;
         k_silu_back<<<nb((long long)n * kHid), 256, 0, st>>>(d.da, d.z[l - 1], d.dzb[l - 1], d.dz[l - 1], n * kHid);
+        count_launch();
     }
     return cudaGetLastError();
 }
@@ -309,11 +318,13 @@ cudaError_t mlp_adam_dev(MlpDev& d, float lr, cudaStream_t st) {
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     const float c1 = 1.0f - powf(b1, (float)d.step), c2 = 1.0f - powf(b2, (float)d.step);
     k_adam<<<nb(kParams), 256, 0, st>>>(d.w, d.grad, d.m1, d.m2, d.wball, kParams, lr, b1, b2, eps, c1, c2);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t mlp_sync_bf16(MlpDev& d, cudaStream_t st) {
     k_to_bf16<<<nb(kParams), 256, 0, st>>>(d.w, d.wball, kParams);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -322,7 +333,9 @@ cudaError_t mlp_train_steps(MlpDev& d, int steps, int batch, float lr, unsigned 
     if ((e = mlp_reserve(d, batch)) != cudaSuccess) return e;
     for (int s = 0; s < steps; ++s) {
         k_sample<<<nb(batch), 256, 0, st>>>(d.idx, batch, d.n_data, seed + 1000003ull * (unsigned long long)d.step);
+        count_launch();
         k_gather<<<nb(batch), 256, 0, st>>>(d.data_x, d.data_t, d.idx, d.bx, d.bt, batch);
+        count_launch();
         if ((e = mlp_backward_dev(d, d.bx, d.bt, batch, st)) != cudaSuccess) return e;
         if ((e = mlp_adam_dev(d, lr, st)) != cudaSuccess) return e;
     }

@@ -1,34 +1,49 @@
 // Learned warm start of a substep's Gauss-Seidel sweeps.
 //
-// After the prediction (timestep.cpp:35-43) the per-vertex MLP maps 16
-// features to a displacement guess d_i for the substep's solution.  Moving
-// the positions alone would break XPBD's bookkeeping (x - x_pred must stay
-// sum_j M^-1 grad C_j^T lambda_j, with lambda starting at 0), so the guess is
-// turned into multipliers by one "fit" sweep in the solver's colour order:
-// each constraint takes the multiplier increment whose position update best
-// matches the displacement still missing at its vertices,
-//     dl = argmin sum_i m_i |w_i grad_i C dl - r_i|^2,  r_i = x_pred_i + d_i - x_i,
-// (2x2 normal equations with the XPBD compliance terms for SNH), and moves
-// its vertices accordingly.  The ordinary sweeps then continue from those
-// multipliers.  Features (per vertex): x_pred - x (3), mean deformation
-// gradient of the incident tets at x_pred (9, row-major), external
-// acceleration (3), pin flag (1).
+// After the prediction (timestep.cpp:35-43) the displacement the substep's
+// solve will apply is guessed per vertex as d_i = d_prev_i + MLP(features_i):
+// the solve displacement of the previous substep (the motion is smooth, so it
+// is already close) plus a learned correction.  Moving the positions alone
+// would break XPBD's bookkeeping (x - x_pred must stay sum_j M^-1 grad C_j^T
+// lambda_j, with lambda starting at 0), so the guess is turned into
+// multipliers by "fit" sweeps in the solver's colour order: each constraint
+// takes the multiplier increment whose position update best matches the
+// displacement still missing at its vertices,
+//     dl = argmin sum_i m_i |w_i grad_i C dl - r_i|^2 + alpha~ (lambda + dl)^2,
+//     r_i = x_pred_i + d_i - x_i,
+// (2x2 normal equations for SNH), and moves its vertices accordingly.  The
+// ordinary sweeps then continue from those multipliers.  Features (per
+// vertex): x_pred - x (3), d_prev (3), Green strain of the mean deformation
+// gradient of the incident tets at x_pred (6: E00 E11 E22 E01 E02 E12),
+// external acceleration (3), pin flag (1).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "warmstart_internal.cuh"
+#include "launch_count.cuh"
 #include "xpbd_internal.cuh"
 #include "xpbd_math.cuh"
 
 namespace sbs {
 
-__global__ void k_features(SceneDev s, WarmDev w, StepParams p) {
+// dprev_valid: w.xpred holds the prediction of the substep that produced the
+// current x (features ran on it and the state was not replaced since), so
+// x - w.xpred is that substep's solve displacement.
+__global__ void k_features(SceneDev s, WarmDev w, StepParams p, int dprev_valid) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < s.n_verts; v += gridDim.x * blockDim.x) {
         const float4 xp = s.xi[v], x = s.xn[v];
         float* f = w.feat + (size_t)v * 16;
         f[0] = xp.x - x.x;
         f[1] = xp.y - x.y;
         f[2] = xp.z - x.z;
+        if (dprev_valid) {
+            const float4 xo = w.xpred[v];
+            f[3] = x.x - xo.x;
+            f[4] = x.y - xo.y;
+            f[5] = x.z - xo.z;
+        } else {
+            f[3] = f[4] = f[5] = 0.0f;
+        }
         float F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         const uint32_t b = w.inc_start[v], e = w.inc_start[v + 1];
         for (uint32_t k = b; k < e; ++k) {
@@ -42,7 +57,15 @@ __global__ void k_features(SceneDev s, WarmDev w, StepParams p) {
             F[6] += Fm.c0.z; F[7] += Fm.c1.z; F[8] += Fm.c2.z;
         }
         const float inv = e > b ? 1.0f / (float)(e - b) : 0.0f;
-        for (int i = 0; i < 9; ++i) f[3 + i] = F[i] * inv;
+        for (int i = 0; i < 9; ++i) F[i] *= inv;
+        // E = (F^T F - I) / 2 of the mean gradient (F row-major)
+        const f3 c0 = mk(F[0], F[3], F[6]), c1 = mk(F[1], F[4], F[7]), c2 = mk(F[2], F[5], F[8]);
+        f[6] = 0.5f * (dot(c0, c0) - 1.0f);
+        f[7] = 0.5f * (dot(c1, c1) - 1.0f);
+        f[8] = 0.5f * (dot(c2, c2) - 1.0f);
+        f[9] = 0.5f * dot(c0, c1);
+        f[10] = 0.5f * dot(c0, c2);
+        f[11] = 0.5f * dot(c1, c2);
         const bool pinned = !(xp.w > 0.0f);
         float ax = 0.f, ay = 0.f, az = 0.f;
         if (!pinned) {
@@ -61,8 +84,10 @@ __global__ void k_features(SceneDev s, WarmDev w, StepParams p) {
     }
 }
 
-// One tet of the fit sweep; lambda starts from 0 (first sweep of the substep).
-__device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, const StepParams& p, uint32_t t) {
+// One tet of a fit sweep; the first fit sweep of the substep starts the
+// multipliers from 0, later ones accumulate.
+__device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, const StepParams& p, uint32_t t,
+                                        bool first) {
     const uint4 id = s.tet[t];
     const float4 a = s.dm0[t], b = s.dm1[t], c = s.dm2[t];
     float4 q[4] = {__ldcg(&s.xi[id.x]), __ldcg(&s.xi[id.y]), __ldcg(&s.xi[id.z]), __ldcg(&s.xi[id.w])};
@@ -73,7 +98,8 @@ __device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, con
     for (int i = 0; i < 4; ++i) {
         const float4 xp = w.xpred[vid[i]];
         const float* d = w.delta + (size_t)vid[i] * 3;
-        r[i] = mk(xp.x + d[0] - q[i].x, xp.y + d[1] - q[i].y, xp.z + d[2] - q[i].z);
+        const float* dp = w.feat + (size_t)vid[i] * 16 + 3;
+        r[i] = mk(xp.x + dp[0] + d[0] - q[i].x, xp.y + dp[1] + d[1] - q[i].y, xp.z + dp[2] + d[2] - q[i].z);
         wgt[i] = q[i].w;
     }
     const f3 x0 = mk(q[0]), x1 = mk(q[1]), x2 = mk(q[2]), x3 = mk(q[3]);
@@ -88,14 +114,16 @@ __device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, con
             num += wgt[i] > 0.0f ? dot(e.g[i], r[i]) : 0.0f;
             den += wgt[i] * dot(e.g[i], e.g[i]);
         }
-        const float dl = den > 1e-20f ? num / (den + p.stvk_alpha_tilde) : 0.0f;
-        s.lam0[t] = dl;
+        const float l0 = first ? 0.0f : s.lam0[t];
+        const float dl = den > 1e-20f ? (num - p.stvk_alpha_tilde * l0) / (den + p.stvk_alpha_tilde) : 0.0f;
+        s.lam0[t] = l0 + dl;
 #pragma unroll
         for (int i = 0; i < 4; ++i) dx[i] = e.g[i] * (wgt[i] * dl);
     } else {
         const float aV0 = fabsf(a.w), mu = b.w, lam = c.w;
         const m3 F = deformation(x0 - x3, x1 - x3, x2 - x3, r0, r1, r2);
         const float cD = sqrtf(dot(F.c0, F.c0) + dot(F.c1, F.c1) + dot(F.c2, F.c2));
+        const float lD = first ? 0.0f : s.lam0[t], lH = first ? 0.0f : s.lam1[t];
         float dlD = 0.f, dlH = 0.f;
         f3 gD[4], gH[4];
         if (cD > 1e-12f) {
@@ -109,7 +137,8 @@ __device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, con
             gH[1] = h0 * r1.x + h1 * r1.y + h2 * r1.z;
             gH[2] = h0 * r2.x + h1 * r2.y + h2 * r2.z;
             gH[3] = -(gH[0] + gH[1] + gH[2]);
-            float a11 = p.inv_dt2 / (mu * aV0), a22 = p.inv_dt2 / (lam * aV0), a12 = 0.f, b1 = 0.f, b2 = 0.f;
+            const float atD = p.inv_dt2 / (mu * aV0), atH = p.inv_dt2 / (lam * aV0);
+            float a11 = atD, a22 = atH, a12 = 0.f, b1 = -atD * lD, b2 = -atH * lH;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 a11 += wgt[i] * dot(gD[i], gD[i]);
@@ -129,8 +158,8 @@ __device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, con
 #pragma unroll
             for (int i = 0; i < 4; ++i) gD[i] = gH[i] = mk(0.f, 0.f, 0.f);
         }
-        s.lam0[t] = dlD;
-        s.lam1[t] = dlH;
+        s.lam0[t] = lD + dlD;
+        s.lam1[t] = lH + dlH;
 #pragma unroll
         for (int i = 0; i < 4; ++i) dx[i] = (gD[i] * dlD + gH[i] * dlH) * wgt[i];
     }
@@ -143,21 +172,25 @@ __device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, con
     }
 }
 
-__global__ void k_fit_segment(SceneDev s, WarmDev w, StepParams p, uint32_t b, uint32_t e) {
-    for (uint32_t t = b + blockIdx.x * blockDim.x + threadIdx.x; t < e; t += gridDim.x * blockDim.x) fit_tet(s, w, p, t);
+__global__ void k_fit_segment(SceneDev s, WarmDev w, StepParams p, uint32_t b, uint32_t e, int first) {
+    for (uint32_t t = b + blockIdx.x * blockDim.x + threadIdx.x; t < e; t += gridDim.x * blockDim.x)
+        fit_tet(s, w, p, t, first != 0);
 }
 
-cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParams& p, cudaStream_t st) {
+cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParams& p, int dprev_valid,
+                            cudaStream_t st) {
     const int grid = (int)std::min<uint32_t>(4096, (s.n_verts + 255) / 256);
-    k_features<<<grid > 0 ? grid : 1, 256, 0, st>>>(s, w, p);
+    k_features<<<grid > 0 ? grid : 1, 256, 0, st>>>(s, w, p, dprev_valid);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_fit_segment(const SceneDev& s, const WarmDev& w, const StepParams& p, uint32_t b, uint32_t e,
-                               cudaStream_t st) {
+                               int first, cudaStream_t st) {
     if (e <= b) return cudaSuccess;
     const int grid = (int)std::min<uint32_t>(2048, (e - b + 127) / 128);
-    k_fit_segment<<<grid, 128, 0, st>>>(s, w, p, b, e);
+    k_fit_segment<<<grid, 128, 0, st>>>(s, w, p, b, e, first);
+    count_launch();
     return cudaGetLastError();
 }
 

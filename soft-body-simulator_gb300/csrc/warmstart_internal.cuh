@@ -11,15 +11,16 @@
 namespace sbs {
 
 struct WarmDev {
-    float* feat;          // [V][16] features
-    float* delta;         // [V][3] MLP displacement guess
-    float4* xpred;        // [V] predicted positions of the substep
+    float* feat;          // [V][16] features; [3..6) is the previous substep's solve displacement
+    float* delta;         // [V][3] MLP correction to that displacement
+    float4* xpred;        // [V] predicted positions of the last substep that computed features
     uint32_t* inc_start;  // [V + 1] CSR of incident tet slots
     uint32_t* inc;        // [4T]
 };
 
-cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParams& p, cudaStream_t st);
+cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParams& p, int dprev_valid,
+                            cudaStream_t st);
 cudaError_t launch_fit_segment(const SceneDev& s, const WarmDev& w, const StepParams& p, uint32_t b, uint32_t e,
-                               cudaStream_t st);
+                               int first, cudaStream_t st);
 
 }  // namespace sbs

@@ -9,6 +9,7 @@ namespace sbs {
 constexpr int kMaxColours = 128;  // colour masks are two 64-bit words per vertex
 constexpr int kMaxPlanes = 4;
 constexpr int kMaxKinGroups = 8;
+constexpr int kMaxEdgeColours = 64;  // colours of the distance constraints
 
 // A contact against a frozen plane (q, n), as collision_constraint_t holds
 // (src/physics/xpbd/collision_constraint.cpp:11-19): xyz of `q` is the contact
@@ -47,10 +48,20 @@ struct SceneDev {
     float* contact_lam;
     uint32_t* counters;    // [0..kMaxPlanes) ground contacts per plane, [kMaxPlanes] body contacts
     uint32_t body_contact_cap;
+    // distance constraints (distance_constraint.cpp:8-53), colour-major
+    uint2* edge;           // vertex slots of the two ends
+    float4* edge_p;        // x: rest length, y: compliance alpha, z: damping beta
+    float* edge_lam;
+    uint32_t n_edges;
     // control
     double* time;          // simulation time (s)
     int* err;              // first error code seen on the device
     unsigned* bar;         // grid barrier: [0] arrival count, [1] generation
+    // wavefront mode: per-CTA count of finished colour phases, and the CTAs
+    // whose tets share a vertex with each CTA's tets (CSR)
+    uint32_t* prog;
+    uint32_t* nb_start;
+    uint32_t* nb;
     // reductions
     double* red_out;       // [4]: residual^2 (elastic), energy, residual^2 (contacts), spare
     float* partials;       // per-CTA partial sums for the residual kernel
@@ -87,6 +98,8 @@ struct StepParams {
     KinGroup kin[kMaxKinGroups];
     uint32_t colour_start[kMaxColours + 1];
     uint32_t colour_split[kMaxColours];  // first SNH tet of each colour
+    int n_edge_colours;
+    uint32_t edge_start[kMaxEdgeColours + 1];
 };
 
 // Kernel launchers (xpbd_kernels.cu).  All enqueue on `st`.
@@ -98,12 +111,19 @@ cudaError_t launch_colour(const SceneDev& s, const StepParams& p, int colour, in
                           int grid, cudaStream_t st);
 cudaError_t launch_tail(const SceneDev& s, const StepParams& p, int first_iter, int block, cudaStream_t st);
 cudaError_t launch_finalize(const SceneDev& s, const StepParams& p, cudaStream_t st);
+cudaError_t launch_edges(const SceneDev& s, const StepParams& p, int colour, int first_iter, cudaStream_t st);
 cudaError_t launch_residual_ex(const SceneDev& s, const StepParams& p, int block, int grid, int cnt_base,
                                cudaStream_t st);
 cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st);
 cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
                                     cudaStream_t st);
 cudaError_t persistent_occupancy(int block, int* ctas_per_sm);
+// Wavefront variant of the frame kernel: every CTA owns the contiguous slice
+// [start + b n / G, start + (b + 1) n / G) of each colour and, instead of a
+// grid barrier per colour, waits until the CTAs it shares vertices with have
+// finished the previous colour.  Needs s.prog zeroed before the launch.
+cudaError_t wavefront_occupancy(int block, int* ctas_per_sm);
+cudaError_t launch_wavefront_frame(const SceneDev& s, const StepParams& p, int block, int grid, cudaStream_t st);
 cudaError_t launch_set_error(int* err, int code, cudaStream_t st);
 
 }  // namespace sbs

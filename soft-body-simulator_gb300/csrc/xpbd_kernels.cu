@@ -16,9 +16,15 @@
 #include <stdint.h>
 
 #include "xpbd_internal.cuh"
+#include "launch_count.cuh"
 #include "xpbd_math.cuh"
 
 namespace sbs {
+
+uint64_t& launch_counter() {
+    static thread_local uint64_t n = 0;
+    return n;
+}
 
 constexpr int kErrTimeout = 3;  // SBS_ETIMEOUT
 constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s
@@ -41,34 +47,39 @@ __device__ __forceinline__ int ld_relaxed(const int* p) {
     return v;
 }
 
-// Grid-wide barrier for a cooperative launch.  Thread 0 of each CTA arrives
-// on a counter; the last arrival resets it and bumps the generation; the
-// others wait for the generation to change for at most kBarrierLimitNs, then
-// record SBS_ETIMEOUT.  Returns false when the kernel must stop (timeout
-// here or an error recorded by another CTA).
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
-    __shared__ int s_ok;
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier for a cooperative launch.  bar[0] counts arrivals over
+// the whole launch (zeroed by the host before it); barrier number k of the
+// launch completes when the count reaches k * gridDim.x, so thread 0 of each
+// CTA adds one with release semantics and waits, with acquire loads, for the
+// count to reach its target - one round trip, no reset.  A wait longer than
+// kBarrierLimitNs records SBS_ETIMEOUT.  Returns false when the kernel must
+// stop (timeout here or an error recorded by another CTA).
+__device__ __forceinline__ void grid_arrive(unsigned* bar, unsigned& target) {
+    target += gridDim.x;
     __syncthreads();
     if (threadIdx.x == 0) {
-        int ok = 1;
-        const unsigned gen = ld_acquire(bar + 1);
         __threadfence();
-        const unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            const unsigned long long t0 = global_ns();
-            unsigned spins = 0;
-            while (ld_acquire(bar + 1) == gen) {
-                if ((++spins & 63u) == 0) {
-                    if (ld_relaxed(err) != 0) { ok = 0; break; }
-                    if (global_ns() - t0 > kBarrierLimitNs) {
-                        atomicCAS(err, 0, kErrTimeout);
-                        ok = 0;
-                        break;
-                    }
+        red_release_add(bar, 1u);
+    }
+}
+
+__device__ __forceinline__ bool grid_wait(unsigned* bar, int* err, unsigned target) {
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned long long t0 = global_ns();
+        unsigned spins = 0;
+        while (ld_acquire(bar) < target) {
+            if ((++spins & 63u) == 0) {
+                if (ld_relaxed(err) != 0) { ok = 0; break; }
+                if (global_ns() - t0 > kBarrierLimitNs) {
+                    atomicCAS(err, 0, kErrTimeout);
+                    ok = 0;
+                    break;
                 }
             }
         }
@@ -78,6 +89,13 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// grid_arrive + grid_wait.  Loads of read-only data issued between the two
+// overlap the wait without holding back the CTA's arrival.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, unsigned& target) {
+    grid_arrive(bar, target);
+    return grid_wait(bar, err, target);
 }
 
 // Work mapping for one phase: 32-item chunks dealt round-robin over CTAs
@@ -193,13 +211,31 @@ __device__ __forceinline__ void project_contact(const SceneDev& s, const StepPar
     s.contact_lam[ci] = lam;
 }
 
+// The read-only part of a tet's record (indices and rest data).  It does not
+// depend on positions, so the persistent kernel loads a thread's next tet
+// before the grid barrier that precedes its projection.
+struct TetRec {
+    uint4 id;
+    float4 a, b, c;   // DmInv rows; w: V0, mu, lambda
+    uint32_t snh;
+};
+
+__device__ __forceinline__ TetRec load_tet(const SceneDev& s, uint32_t t) {
+    TetRec r;
+    r.id = __ldg(&s.tet[t]);
+    r.a = __ldg(&s.dm0[t]);
+    r.b = __ldg(&s.dm1[t]);
+    r.c = __ldg(&s.dm2[t]);
+    r.snh = s.model[t] != 0;
+    return r;
+}
+
 // One elastic tet constraint (StVK: green_constraint.cpp:49-158; SNH coupled).
-__device__ __forceinline__ void project_tet(const SceneDev& s, const StepParams& p, uint32_t t, bool snh,
-                                            bool first) {
-    const uint4 id = __ldg(&s.tet[t]);
-    const float4 a = __ldg(&s.dm0[t]);
-    const float4 b = __ldg(&s.dm1[t]);
-    const float4 c = __ldg(&s.dm2[t]);
+__device__ __forceinline__ void project_tet_rec(const SceneDev& s, const StepParams& p, uint32_t t,
+                                                const TetRec& R, bool first) {
+    const bool snh = R.snh != 0;
+    const uint4 id = R.id;
+    const float4 a = R.a, b = R.b, c = R.c;
     float4 q0 = __ldcg(&s.xi[id.x]);
     float4 q1 = __ldcg(&s.xi[id.y]);
     float4 q2 = __ldcg(&s.xi[id.z]);
@@ -252,10 +288,37 @@ __device__ __forceinline__ void project_tet(const SceneDev& s, const StepParams&
     }
 }
 
+__device__ __forceinline__ void project_tet(const SceneDev& s, const StepParams& p, uint32_t t, bool first) {
+    project_tet_rec(s, p, t, load_tet(s, t), first);
+}
+
+// First tet slot of this thread in colour `col` under for_each_spread's
+// mapping (chunk wib * gridDim.x + blockIdx.x, lane), or ~0u.
+__device__ __forceinline__ uint32_t first_slot(const StepParams& p, int col) {
+    const uint32_t b = p.colour_start[col], n = p.colour_start[col + 1] - b;
+    const uint32_t c = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+    const uint32_t i = (c << 5) + (threadIdx.x & 31u);
+    return i < n ? b + i : ~0u;
+}
+
+// colour_phase with the first tet's record already loaded (slot ~0u: none).
+__device__ __forceinline__ void colour_phase_pf(const SceneDev& s, const StepParams& p, int col, bool first,
+                                                uint32_t slot, const TetRec& rec) {
+    if (slot != ~0u) project_tet_rec(s, p, slot, rec, first);
+    const uint32_t lane = threadIdx.x & 31u, wpb = blockDim.x >> 5;
+    const uint32_t b = p.colour_start[col], n = p.colour_start[col + 1] - b;
+    const uint32_t chunks = (n + 31u) >> 5;
+    for (uint32_t c = (threadIdx.x >> 5) * gridDim.x + blockIdx.x + gridDim.x * wpb; c < chunks;
+         c += gridDim.x * wpb) {
+        const uint32_t i = (c << 5) + lane;
+        if (i < n) project_tet(s, p, b + i, first);
+    }
+}
+
 __device__ __forceinline__ void colour_phase(const SceneDev& s, const StepParams& p, int col, bool first) {
     const uint32_t b = p.colour_start[col], e = p.colour_start[col + 1], m = p.colour_split[col];
     (void)m;
-    for_each_spread(b, e, [&](uint32_t t) { project_tet(s, p, t, s.model[t] != 0, first); });
+    for_each_spread(b, e, [&](uint32_t t) { project_tet(s, p, t, first); });
 }
 
 // Tail colours in one CTA, separated by CTA barriers.
@@ -263,9 +326,45 @@ __device__ __forceinline__ void tail_phase(const SceneDev& s, const StepParams& 
     for (int col = p.first_tail; col < p.n_colours; ++col) {
         const uint32_t b = p.colour_start[col], e = p.colour_start[col + 1], m = p.colour_split[col];
         (void)m;
-        for (uint32_t t = b + threadIdx.x; t < e; t += blockDim.x) project_tet(s, p, t, s.model[t] != 0, first);
+        for (uint32_t t = b + threadIdx.x; t < e; t += blockDim.x) project_tet(s, p, t, first);
         __syncthreads();
     }
+}
+
+// distance_constraint_t::project_positions (distance_constraint.cpp:24-53).
+// Coincident ends (where the reference divides by zero) and a zero
+// denominator leave the constraint unchanged.
+__device__ __forceinline__ void project_edge(const SceneDev& s, const StepParams& p, uint32_t k, bool first) {
+    const uint2 e = s.edge[k];
+    const float4 q = s.edge_p[k];
+    float lam = first ? 0.0f : s.edge_lam[k];
+    float4 p1 = __ldcg(&s.xi[e.x]);
+    float4 p2 = __ldcg(&s.xi[e.y]);
+    const float w1 = p1.w, w2 = p2.w;
+    const f3 diff = mk(p1) - mk(p2);
+    const float length = sqrtf(dot(diff, diff));
+    if (length > 0.0f) {
+        const f3 n = diff * (1.0f / length);
+        const float C = length - q.x;
+        const float at = q.y * p.inv_dt2;
+        const float bt = q.z * p.dt * p.dt;
+        const float gamma = at * bt * p.inv_dt;
+        float gd = 0.0f;
+        if (q.z != 0.0f) {
+            const float4 n1 = s.xn[e.x], n2 = s.xn[e.y];
+            gd = dot(n, mk(p1) - mk(n1)) - dot(n, mk(p2) - mk(n2));
+        }
+        const float den = (1.0f + gamma) * (w1 + w2) + at;
+        if (den > 0.0f) {
+            const float dl = (-(C + at * lam) + gamma * gd) / den;
+            lam += dl;
+            p1.x += w1 * n.x * dl; p1.y += w1 * n.y * dl; p1.z += w1 * n.z * dl;
+            p2.x -= w2 * n.x * dl; p2.y -= w2 * n.y * dl; p2.z -= w2 * n.z * dl;
+            s.xi[e.x] = p1;
+            s.xi[e.y] = p2;
+        }
+    }
+    s.edge_lam[k] = lam;
 }
 
 __device__ __forceinline__ void contact_phase(const SceneDev& s, uint32_t seg, uint32_t count,
@@ -275,6 +374,11 @@ __device__ __forceinline__ void contact_phase(const SceneDev& s, uint32_t seg, u
 
 // ---------------------------------------------------------------------------
 // Per-phase kernels (graph mode)
+
+__global__ void k_edges(SceneDev s, StepParams p, int colour, int first) {
+    for_each_spread(p.edge_start[colour], p.edge_start[colour + 1],
+                    [&](uint32_t k) { project_edge(s, p, k, first != 0); });
+}
 
 __global__ void k_detect(SceneDev s, StepParams p) {
     const uint32_t n = s.n_surf * (uint32_t)p.n_planes;
@@ -331,8 +435,52 @@ __global__ void k_end_frame(SceneDev s) {
 // ---------------------------------------------------------------------------
 // Persistent frame kernel
 
-__global__ void __launch_bounds__(512) k_frame(SceneDev s, StepParams p, int has_acc) {
+__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Wavefront wait: warp 0 polls the progress counters of this CTA's
+// neighbours until each has finished `need` colour phases (bounded by
+// kBarrierLimitNs, then SBS_ETIMEOUT); the CTA then passes a CTA barrier.
+__device__ __forceinline__ bool wave_wait(const SceneDev& s, uint32_t need) {
+    __shared__ int s_ok;
+    if (threadIdx.x < 32) {
+        int ok = 1;
+        const uint32_t b = s.nb_start[blockIdx.x], e = s.nb_start[blockIdx.x + 1];
+        const unsigned long long t0 = global_ns();
+        for (uint32_t k = b + threadIdx.x; k < e && ok; k += 32) {
+            const unsigned* c = s.prog + s.nb[k];
+            unsigned spins = 0;
+            while (ld_acquire(c) < need) {
+                if ((++spins & 63u) == 0) {
+                    if (ld_relaxed(s.err) != 0) { ok = 0; break; }
+                    if (global_ns() - t0 > kBarrierLimitNs) {
+                        atomicCAS(s.err, 0, kErrTimeout);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        if (threadIdx.x == 0) s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// This CTA's slice of colour `col` in the wavefront mapping.
+__device__ __forceinline__ void wave_range(const StepParams& p, int col, uint32_t& b, uint32_t& e) {
+    const uint32_t c0 = p.colour_start[col], n = p.colour_start[col + 1] - c0;
+    b = c0 + (uint32_t)(((uint64_t)n * blockIdx.x) / gridDim.x);
+    e = c0 + (uint32_t)(((uint64_t)n * (blockIdx.x + 1)) / gridDim.x);
+}
+
+template <bool kWave>
+__global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int has_acc) {
     if (ld_relaxed(s.err) != 0) return;
+    uint32_t done = 0;         // wavefront: colour phases this CTA has finished
+    unsigned bar_target = 0;   // arrivals expected by the next barrier (host zeroes s.bar[0])
     double t = *s.time;
     // contacts from frame-start positions
     {
@@ -343,38 +491,83 @@ __global__ void __launch_bounds__(512) k_frame(SceneDev s, StepParams p, int has
             if (k < n) detect_item(s, p, k);
         }
     }
-    if (!grid_barrier(s.bar, s.err)) return;
+    if (!grid_barrier(s.bar, s.err, bar_target)) return;
     uint32_t cnt[kMaxPlanes];
     for (int pl = 0; pl < kMaxPlanes; ++pl) cnt[pl] = pl < p.n_planes ? min(__ldcg(&s.counters[pl]), s.n_surf) : 0u;
     const uint32_t cnt_body = p.body_contacts ? min(__ldcg(&s.counters[kMaxPlanes]), s.n_surf) : 0u;
+    bool any_contact = cnt_body > 0;
+    for (int pl = 0; pl < p.n_planes; ++pl) any_contact |= cnt[pl] > 0;
     for (int sub = 0; sub < p.substeps; ++sub) {
         const double t_next = t + p.dt_d;
         for_each_vertex(s.n_verts, [&](uint32_t i) { predict_vertex(s, p, i, t_next, has_acc); });
-        if (!grid_barrier(s.bar, s.err)) return;
+        if (!grid_barrier(s.bar, s.err, bar_target)) return;
         for (int it = 0; it < p.iterations; ++it) {
             const bool first = it == 0;
+            uint32_t slot = (!kWave && p.first_tail > 0) ? first_slot(p, 0) : ~0u;
+            TetRec rec;
+            if (slot != ~0u) rec = load_tet(s, slot);
             for (int pl = 0; pl < p.n_planes; ++pl) {
                 if (cnt[pl] == 0) continue;
                 contact_phase(s, (uint32_t)pl * s.n_surf, cnt[pl], p, first);
-                if (!grid_barrier(s.bar, s.err)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target)) return;
             }
             if (cnt_body) {
                 contact_phase(s, (uint32_t)kMaxPlanes * s.n_surf, cnt_body, p, first);
-                if (!grid_barrier(s.bar, s.err)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target)) return;
             }
+            if (kWave) {
+                // every colour, each CTA its own slice; wait only for the
+                // neighbours (GS order is kept: a tet of colour c runs after
+                // every vertex-sharing tet of colours < c has finished, and
+                // before any of colours > c starts)
+                for (int col = 0; col < p.n_colours; ++col) {
+                    uint32_t b, e;
+                    wave_range(p, col, b, e);
+                    const uint32_t t0 = b + threadIdx.x;
+                    TetRec r;
+                    if (t0 < e) r = load_tet(s, t0);
+                    if (!wave_wait(s, done)) return;
+                    if (t0 < e) project_tet_rec(s, p, t0, r, first);
+                    for (uint32_t u = t0 + blockDim.x; u < e; u += blockDim.x) project_tet(s, p, u, first);
+                    __syncthreads();
+                    ++done;
+                    if (threadIdx.x == 0) {
+                        __threadfence();
+                        st_release(s.prog + blockIdx.x, done);
+                    }
+                }
+            } else {
             for (int col = 0; col < p.first_tail; ++col) {
-                colour_phase(s, p, col, first);
-                if (!grid_barrier(s.bar, s.err)) return;
+                colour_phase_pf(s, p, col, first, slot, rec);
+                grid_arrive(s.bar, bar_target);
+                slot = col + 1 < p.first_tail ? first_slot(p, col + 1) : ~0u;
+                if (slot != ~0u) rec = load_tet(s, slot);
+                if (!grid_wait(s.bar, s.err, bar_target)) return;
             }
-            if (p.first_tail < p.n_colours) {
+            }
+            if (!kWave && p.first_tail < p.n_colours) {
                 if (blockIdx.x == 0) tail_phase(s, p, first);
-                if (!grid_barrier(s.bar, s.err)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target)) return;
             }
+            if (kWave && (p.n_edge_colours > 0 || (it + 1 < p.iterations && any_contact))) {
+                // distance constraints and the next iteration's contacts touch
+                // vertices of any CTA: a grid barrier before them
+                if (!grid_barrier(s.bar, s.err, bar_target)) return;
+            }
+            for (int col = 0; col < p.n_edge_colours; ++col) {
+                for_each_spread(p.edge_start[col], p.edge_start[col + 1],
+                                [&](uint32_t k) { project_edge(s, p, k, first); });
+                if (!grid_barrier(s.bar, s.err, bar_target)) return;
+            }
+        }
+        if (kWave && !(p.n_edge_colours > 0)) {
+            // the velocity update reads every vertex
+            if (!grid_barrier(s.bar, s.err, bar_target)) return;
         }
         for_each_vertex(s.n_verts, [&](uint32_t i) { finalize_vertex(s, p, i); });
         t = t_next;
     }
-    if (!grid_barrier(s.bar, s.err)) return;
+    if (!grid_barrier(s.bar, s.err, bar_target)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *s.time = t;
         for (int i = 0; i <= kMaxPlanes; ++i) {
@@ -444,6 +637,15 @@ __global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
             en.add(E);
         }
     }
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < s.n_edges; k += stride) {
+        const uint2 e = s.edge[k];
+        const float4 q = s.edge_p[k];
+        const f3 d = mk(s.xi[e.x]) - mk(s.xi[e.y]);
+        const float C = sqrtf(dot(d, d)) - q.x;
+        const float h = C + q.y * p.inv_dt2 * s.edge_lam[k];
+        re.add(h * h);
+        if (q.y > 0.0f) en.add(0.5f * C * C / q.y);
+    }
     for (int pl = 0; pl <= kMaxPlanes; ++pl) {
         // planes, then the body-contact segment (index kMaxPlanes)
         if (pl < kMaxPlanes && pl >= p.n_planes) continue;
@@ -495,12 +697,22 @@ cudaError_t launch_detect_ground(const SceneDev& s, const StepParams& p, cudaStr
     const uint32_t n = s.n_surf * (uint32_t)p.n_planes;
     if (n == 0) return cudaSuccess;
     k_detect<<<grid_for(n, 256, 4096), 256, 0, st>>>(s, p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edges(const SceneDev& s, const StepParams& p, int colour, int first_iter, cudaStream_t st) {
+    const uint32_t n = p.edge_start[colour + 1] - p.edge_start[colour];
+    if (n == 0) return cudaSuccess;
+    k_edges<<<grid_for((n + 31) / 32 * 32, 256, 1024), 256, 0, st>>>(s, p, colour, first_iter);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_predict(const SceneDev& s, const StepParams& p, int substep, cudaStream_t st) {
     (void)substep;
     k_predict<<<grid_for(s.n_verts, 256, 8192), 256, 0, st>>>(s, p, substep, p.has_acc);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -508,29 +720,34 @@ cudaError_t launch_contacts(const SceneDev& s, const StepParams& p, int first_it
     if (p.n_planes == 0 || s.n_surf == 0) return cudaSuccess;
     const int grid = p.n_planes > 1 ? 1 : grid_for(s.n_surf, 256, 1024);
     k_contacts<<<grid, 256, 0, st>>>(s, p, first_iter);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_body_contacts(const SceneDev& s, const StepParams& p, int first_iter, cudaStream_t st) {
     if (!p.body_contacts || s.n_surf == 0) return cudaSuccess;
     k_contacts_body<<<grid_for(s.n_surf, 256, 1024), 256, 0, st>>>(s, p, first_iter);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_colour(const SceneDev& s, const StepParams& p, int colour, int first_iter, int block,
                           int grid, cudaStream_t st) {
     k_colour<<<grid, block, 0, st>>>(s, p, colour, first_iter);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_tail(const SceneDev& s, const StepParams& p, int first_iter, int block, cudaStream_t st) {
     if (p.first_tail >= p.n_colours) return cudaSuccess;
     k_tail<<<1, block, 0, st>>>(s, p, first_iter);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_finalize(const SceneDev& s, const StepParams& p, cudaStream_t st) {
     k_finalize<<<grid_for(s.n_verts, 256, 8192), 256, 0, st>>>(s, p);
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return cudaSuccess;
@@ -538,6 +755,7 @@ cudaError_t launch_finalize(const SceneDev& s, const StepParams& p, cudaStream_t
 
 cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st) {
     k_end_frame<<<1, 32, 0, st>>>(s);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -545,14 +763,29 @@ cudaError_t launch_residual_ex(const SceneDev& s, const StepParams& p, int block
                                cudaStream_t st) {
     const size_t shm = 2 * sizeof(float) * (size_t)block;
     k_residual<<<grid, block, shm, st>>>(s, p, cnt_base);
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_residual_final<<<1, 256, 2 * sizeof(float) * 256, st>>>(s, grid);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t persistent_occupancy(int block, int* ctas_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame, block, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame_t<false>, block, 0);
+}
+
+cudaError_t wavefront_occupancy(int block, int* ctas_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame_t<true>, block, 0);
+}
+
+cudaError_t launch_wavefront_frame(const SceneDev& s, const StepParams& p, int block, int grid, cudaStream_t st) {
+    int has_acc = p.has_acc;
+    SceneDev sc = s;
+    StepParams pc = p;
+    void* args[] = {&sc, &pc, &has_acc};
+    count_launch();
+    return cudaLaunchCooperativeKernel((const void*)k_frame_t<true>, dim3(grid), dim3(block), args, 0, st);
 }
 
 cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
@@ -561,11 +794,13 @@ cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int 
     SceneDev sc = s;
     StepParams pc = p;
     void* args[] = {&sc, &pc, &has_acc};
-    return cudaLaunchCooperativeKernel((const void*)k_frame, dim3(grid), dim3(block), args, 0, st);
+    count_launch();
+    return cudaLaunchCooperativeKernel((const void*)k_frame_t<false>, dim3(grid), dim3(block), args, 0, st);
 }
 
 cudaError_t launch_set_error(int* err, int code, cudaStream_t st) {
     k_set_error<<<1, 1, 0, st>>>(err, code);
+    count_launch();
     return cudaGetLastError();
 }
 

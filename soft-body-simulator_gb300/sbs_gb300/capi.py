@@ -14,7 +14,7 @@ import numpy as np
 from . import build as _build
 
 SBS_OK, SBS_EINVAL, SBS_ECUDA, SBS_ETIMEOUT, SBS_ENAN, SBS_ESTATE, SBS_ENOMEM, SBS_ECOLOUR = range(8)
-EXEC_AUTO, EXEC_GRAPH, EXEC_PERSISTENT, EXEC_CLUSTER = 0, 1, 2, 3
+EXEC_AUTO, EXEC_GRAPH, EXEC_PERSISTENT, EXEC_CLUSTER, EXEC_WAVEFRONT = 0, 1, 2, 3, 4
 GRAVITY_ACCELERATION, GRAVITY_FORCE = 0, 1
 
 HEADER = _build.INCLUDE / "sbs_gpu.h"
@@ -47,7 +47,8 @@ class Stats(C.Structure):
                 ("n_tail_colours", C.c_uint32), ("n_contacts", C.c_uint32),
                 ("n_body_contacts", C.c_uint32), ("body_contact_overflow", C.c_uint32),
                 ("exec_mode", C.c_int32), ("grid_ctas", C.c_int32), ("block_size", C.c_int32),
-                ("residual", C.c_double), ("energy", C.c_double), ("last_frame_ms", C.c_double)]
+                ("residual", C.c_double), ("energy", C.c_double), ("last_frame_ms", C.c_double),
+                ("kernel_launches", C.c_uint64)]
 
 
 _lib = None
@@ -96,12 +97,18 @@ def load(build: bool = True):
         "sbs_gpu_get_contacts": [P, C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
         "sbs_gpu_get_masses": [P, f32],
         "sbs_gpu_get_surface": [P, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_add_distance_constraints": [P, C.c_void_p, C.c_uint32, C.c_double, C.c_double],
+        "sbs_gpu_get_distance_order": [P, C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_get_distance_lambdas": [P, C.c_void_p],
+        "sbs_gpu_get_surface_mesh": [P, C.c_int32, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_void_p,
+                                     C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_update_surface": [P, C.c_int32, C.c_int32, C.c_void_p, C.c_uint32],
         "sbs_gpu_get_stats": [P, C.POINTER(Stats)],
         "sbs_gpu_destroy": [P],
         "sbs_gpu_plan_sweep": [f64, C.c_uint32, u32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_uint32, C.POINTER(C.c_uint32)],
         "sbs_gpu_get_candidates": [P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)],
-        "sbs_gpu_set_warm_start": [P, C.c_void_p],
+        "sbs_gpu_set_warm_start": [P, C.c_void_p, C.c_uint32],
         "sbs_gpu_warm_start_init": [P, C.c_double],
         "sbs_gpu_solve_ex": [P, C.c_double, C.c_uint32, C.c_int32],
         "sbs_gpu_get_features": [P, f32],
@@ -214,6 +221,11 @@ class Solver:
                 self._check(L.sbs_gpu_set_external_acceleration(
                     h, bid, np.ascontiguousarray(b.ext_acc, np.float32).ravel()))
             self.body_sizes.append(len(b.x0))
+        dist = getattr(scene, "distance", None)
+        if dist is not None and len(dist):
+            ids = np.ascontiguousarray(dist, np.uint32).ravel()
+            self._check(L.sbs_gpu_add_distance_constraints(h, ids.ctypes.data, len(dist),
+                                                           scene.distance_compliance, scene.distance_damping))
         if scene.ground is not None:
             n, d = scene.ground
             self._check(L.sbs_gpu_add_ground_plane(h, np.asarray(n, np.float64), d))
@@ -273,18 +285,22 @@ class Solver:
         return r.value, e.value
 
     # -- state --------------------------------------------------------------
+    def _nv(self, body: int) -> int:
+        return self.scene.n_verts if body == -1 else self.body_sizes[body]
+
     def get_state(self, body: int = 0):
-        n = self.body_sizes[body]
+        """(x, v) of one body, or of the whole scene with body = -1."""
+        n = self._nv(body)
         x = np.zeros(3 * n, np.float32)
         v = np.zeros(3 * n, np.float32)
         self._check(self.L.sbs_gpu_get_state(self.h, body, x.ctypes.data, v.ctypes.data))
         return x.reshape(-1, 3), v.reshape(-1, 3)
 
     def positions(self) -> np.ndarray:
-        return np.concatenate([self.get_state(b)[0] for b in range(len(self.body_sizes))])
+        return self.get_state(-1)[0]
 
     def velocities(self) -> np.ndarray:
-        return np.concatenate([self.get_state(b)[1] for b in range(len(self.body_sizes))])
+        return self.get_state(-1)[1]
 
     def set_state(self, body: int, x=None, v=None):
         xa = None if x is None else np.ascontiguousarray(x, np.float32).ravel()
@@ -292,7 +308,7 @@ class Solver:
         self._check(self.L.sbs_gpu_set_state(self.h, body, _ptr(xa), _ptr(va)))
 
     def get_predicted(self, body: int = 0) -> np.ndarray:
-        x = np.zeros(3 * self.body_sizes[body], np.float32)
+        x = np.zeros(3 * self._nv(body), np.float32)
         self._check(self.L.sbs_gpu_get_predicted(self.h, body, x))
         return x.reshape(-1, 3)
 
@@ -325,9 +341,9 @@ class Solver:
         return v, qn.reshape(-1, 6)
 
     # -- learned warm start -------------------------------------------------
-    def set_warm_start(self, mlp):
+    def set_warm_start(self, mlp, fit_sweeps: int = 1):
         self._warm = mlp
-        self._check(self.L.sbs_gpu_set_warm_start(self.h, None if mlp is None else mlp.h))
+        self._check(self.L.sbs_gpu_set_warm_start(self.h, None if mlp is None else mlp.h, fit_sweeps))
 
     def warm_start_init(self, dt: float):
         self._check(self.L.sbs_gpu_warm_start_init(self.h, dt))
@@ -341,7 +357,7 @@ class Solver:
         return out.reshape(-1, 16)
 
     def predicted_all(self) -> np.ndarray:
-        return np.concatenate([self.get_predicted(b) for b in range(len(self.body_sizes))])
+        return self.get_predicted(-1)
 
     def candidates(self) -> np.ndarray:
         """Broad-phase (vertex << 32 | tet) pairs of the last detection, sorted."""
@@ -362,6 +378,46 @@ class Solver:
         out = np.zeros(n.value, np.uint32)
         self._check(self.L.sbs_gpu_get_surface(self.h, out.ctypes.data, n.value, C.byref(n)))
         return out
+
+    def distance_order(self):
+        """(projection order of the distance constraints, colour offsets)."""
+        n = C.c_uint32()
+        self._check(self.L.sbs_gpu_get_distance_order(self.h, None, None, 0, C.byref(n)))
+        dist = getattr(self.scene, "distance", None)
+        order = np.zeros(0 if dist is None else len(dist), np.uint32)
+        off = np.zeros(n.value + 1, np.uint32)
+        self._check(self.L.sbs_gpu_get_distance_order(self.h, order.ctypes.data, off.ctypes.data, len(off),
+                                                      C.byref(n)))
+        return order, off
+
+    def distance_lambdas(self) -> np.ndarray:
+        dist = getattr(self.scene, "distance", None)
+        out = np.zeros(0 if dist is None else len(dist), np.float32)
+        if len(out):
+            self._check(self.L.sbs_gpu_get_distance_lambdas(self.h, out.ctypes.data))
+        return out
+
+    def surface_mesh(self, body: int = 0):
+        """Visual model of a body: (triangles [n_tri, 3] in surface-vertex
+        ids, surface vertex -> body vertex map)."""
+        nt, nv = C.c_uint32(), C.c_uint32()
+        self._check(self.L.sbs_gpu_get_surface_mesh(self.h, body, None, 0, C.byref(nt), None, 0, C.byref(nv)))
+        tris = np.zeros(3 * nt.value, np.uint32)
+        vmap = np.zeros(nv.value, np.uint32)
+        self._check(self.L.sbs_gpu_get_surface_mesh(self.h, body, tris.ctypes.data, nt.value, C.byref(nt),
+                                                    vmap.ctypes.data, nv.value, C.byref(nv)))
+        return tris.reshape(-1, 3), vmap
+
+    def update_surface(self, body: int = 0, accumulate: bool = True, buffer=None, stride: int = 9):
+        """One visual-model update.  `buffer`: None (returns a new host array
+        [n_sv, stride], floats past the normal zero), a float32 host array
+        to fill in place, or an int device pointer (written by the kernel)."""
+        if buffer is None:
+            nv = len(self.surface_mesh(body)[1])
+            buffer = np.zeros((nv, stride), np.float32)
+        ptr = buffer if isinstance(buffer, int) else buffer.ctypes.data
+        self._check(self.L.sbs_gpu_update_surface(self.h, body, 1 if accumulate else 0, ptr, stride))
+        return buffer
 
     def stats(self) -> Stats:
         st = Stats()

@@ -195,6 +195,10 @@ class Scene:
     collision_compliance: float = 1e-8  # simulation_parameters.h:26
     gravity: tuple = (0.0, -9.81, 0.0)
     gravity_mode: int = 0             # 0: acceleration, 1: force on m (reference)
+    # distance_constraint_t (distance_constraint.cpp:8-53): rows (b1, b2, v1, v2)
+    distance: list | None = None
+    distance_compliance: float = 0.0
+    distance_damping: float = 0.0
     ground: tuple | None = ((0.0, 1.0, 0.0), 1.0)  # (n, d): n.x + d = 0
     body_contacts: bool = False
     hash_cell: float = 0.0
@@ -302,17 +306,46 @@ def box_drop(n_bodies: int = 512, seed: int = 3, cell: float = 0.05,
                  body_contacts=body_contacts, hash_cell=2.0 * mean_edge)
 
 
+def hanging_block(alpha: float = 1e-7, beta: float = 0.0, frames: int = 60, iterations: int = 20) -> Scene:
+    """Distance constraints: a 4x2x2-cube StVK cantilever (pinned at x = 0)
+    with a 2x2x2-cube block hanging 0.2 m below its free end on four springs
+    (bottom corners of the end face to the block's top corners), plus four
+    springs inside the cantilever (diagonals across its top face)."""
+    xa, ta = bar_5tet(5, 3, 3, 0.1)
+    xb, tb = bar_5tet(3, 3, 3, 0.1)
+    xb = xb + np.array([0.2, -0.4, 0.0])
+    pin = np.nonzero(np.isclose(xa[:, 0], 0.0))[0].astype(np.uint32)
+
+    def at(x, p):
+        return int(np.argmin(((x - np.asarray(p)) ** 2).sum(1)))
+
+    dist = []
+    for z in (0.0, 0.2):
+        for xe in (0.4,):
+            dist.append((0, 1, at(xa, (xe, 0.0, z)), at(xb, (0.4, -0.2, z))))
+            dist.append((0, 1, at(xa, (xe - 0.2, 0.0, z)), at(xb, (0.2, -0.2, z))))
+    for x0 in (0.0, 0.2):
+        dist.append((0, 0, at(xa, (x0, 0.2, 0.0)), at(xa, (x0 + 0.2, 0.2, 0.2))))
+        dist.append((0, 0, at(xa, (x0, 0.2, 0.2)), at(xa, (x0 + 0.2, 0.2, 0.0))))
+    a = Body(x0=xa, tets=ta, model=MODEL_STVK, young=1e5, poisson=0.45, density=1000.0, pinned=pin)
+    b = Body(x0=xb, tets=tb, model=MODEL_STVK, young=1e5, poisson=0.45, density=1000.0)
+    return Scene("hanging-block-springs", [a, b], 1.0 / 60.0, 1, iterations, frames,
+                 distance=np.array(dist, np.uint32), distance_compliance=alpha, distance_damping=beta,
+                 ground=((0.0, 1.0, 0.0), 2.0))
+
+
 def big_block(nx: int = 128, ny: int = 64, nz: int = 64, h: float = 0.02,
               frames: int = 200, substeps: int = 4, iterations: int = 30,
               drop: float = 0.5) -> Scene:
     """Large SNH block (default 2,621,440 tets / 545,025 vertices), E 5e5,
-    nu 0.48, dropped onto the ground from ``drop`` metres."""
+    nu 0.48, dropped onto the ground from ``drop`` metres, with self contacts
+    (vertex against the block's own surface triangles, spatial hash)."""
     x0, tets = bar_5tet(nx + 1, ny + 1, nz + 1, h)
     x0 = x0 + np.array([0.0, drop, 0.0])
     b = Body(x0=x0, tets=tets, model=MODEL_SNH, young=5e5, poisson=0.48,
              density=1000.0, x_init=x0.copy())
     return Scene(f"block-{len(tets)}-snh", [b], 1.0 / 60.0, substeps,
-                 iterations, frames, ground=((0.0, 1.0, 0.0), 0.0))
+                 iterations, frames, ground=((0.0, 1.0, 0.0), 0.0), body_contacts=2)
 
 
 def body_force_field(x0: np.ndarray, seed: int, length: float,

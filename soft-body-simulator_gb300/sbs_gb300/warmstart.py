@@ -37,10 +37,12 @@ def batch_scene(seeds, iterations: int = 30) -> scenes.Scene:
                         iterations, 60, ground=((0.0, 1.0, 0.0), 1.0))
 
 
-def generate(seeds, frames: int = 60, iterations: int = 30, every: int = 1, exec_mode: int = 1):
+def generate(seeds, frames: int = 60, iterations: int = 30, exec_mode: int = 1):
     """Runs the plain solver on the trajectories `seeds` and returns
     (features [N,16], targets [N,3]): per substep and vertex, the features at
-    the predicted state and the displacement the 30-iteration solve applied."""
+    the predicted state and the part of the displacement the 30-iteration
+    solve applied that the previous substep's displacement (features 3:6)
+    does not already give."""
     sc = batch_scene(seeds, iterations)
     g = capi.Solver(sc, exec_mode=exec_mode)
     dt = sc.frame_dt
@@ -48,13 +50,11 @@ def generate(seeds, frames: int = 60, iterations: int = 30, every: int = 1, exec
     for f in range(frames):
         g.detect_contacts()
         g.predict(dt)
-        if f % every == 0:
-            feat = g.features()
-            xp = g.predicted_all()
+        feat = g.features()
+        xp = g.predicted_all()
         g.solve(dt, iterations)
-        if f % every == 0:
-            X.append(feat)
-            Y.append(g.predicted_all() - xp)
+        X.append(feat)
+        Y.append(g.predicted_all() - xp - feat[:, 3:6])
         g.update_velocities(dt)
     g.close()
     return np.concatenate(X).astype(np.float32), np.concatenate(Y).astype(np.float32)
@@ -83,48 +83,62 @@ def residual_after(g, dt):
     return g.residual(dt)[0]
 
 
-def evaluate(mlp, seeds, frame: int = 20, iterations: int = 30, max_iters: int = 60, exec_mode: int = 1):
-    """For each held-out trajectory, advance `frame` plain frames, then from
-    that same state compare the plain solver (residual r_plain[k] after k
-    sweeps) with the warm-started one (fit sweep, then sweeps continuing from
-    the fitted multipliers).  The warm start is discarded, and the plain start
-    used, when its residual after the fit sweep exceeds r_plain[1]; otherwise
-    `iterations` is the number of sweeps (fit sweep included) it needs to reach
-    r_plain[iterations].  Returns a list of dicts."""
+def _plain_frame(g, dt, iterations):
+    """One frame of the plain solver that also records the prediction, so
+    the next substep knows its previous solve displacement."""
+    g.detect_contacts()
+    g.predict(dt)
+    g.features()
+    g.solve(dt, iterations)
+    g.update_velocities(dt)
+
+
+def evaluate(mlp, seeds, frame: int = 20, iterations: int = 30, max_iters: int = 60, exec_mode: int = 1,
+             fit_sweeps: int = 1):
+    """For each held-out trajectory, two handles advance `frame` plain frames
+    in lockstep (identical states); then one runs plain sweeps (residual
+    r_plain[k] after k sweeps) and the other the warm start (fit sweeps, then
+    sweeps continuing from the fitted multipliers).  The warm start is
+    discarded, and the plain start used, when its residual after the fit
+    exceeds r_plain[1]; otherwise `iterations` is the number of sweeps (fit
+    sweeps included) it needs to reach r_plain[iterations].  Returns a list of
+    dicts."""
     out = []
     for s in seeds:
         sc = batch_scene([s], iterations)
-        g = capi.Solver(sc, exec_mode=exec_mode)
+        a = capi.Solver(sc, exec_mode=exec_mode)
+        b = capi.Solver(sc, exec_mode=exec_mode)
         dt = sc.frame_dt
-        g.step(frame)
-        x, v = g.get_state(0)
-        # plain: residual after every sweep
-        g.detect_contacts()
-        g.predict(dt)
+        for _ in range(frame):
+            _plain_frame(a, dt, iterations)
+            _plain_frame(b, dt, iterations)
+        same = bool(np.array_equal(a.get_state(0)[0], b.get_state(0)[0]))
+        a.detect_contacts()
+        a.predict(dt)
+        a.features()
         r_plain = [None]
         for k in range(1, iterations + 1):
-            g.solve_ex(dt, 1, k == 1)
-            r_plain.append(residual_after(g, dt))
+            a.solve_ex(dt, 1, k == 1)
+            r_plain.append(residual_after(a, dt))
         target = r_plain[iterations]
-        # warm start from the same state
-        g.set_state(0, x, v)
-        g.detect_contacts()
-        g.predict(dt)
-        g.set_warm_start(mlp)
-        g.warm_start_init(dt)
-        r_fit = residual_after(g, dt)
+        b.detect_contacts()
+        b.predict(dt)
+        b.set_warm_start(mlp, fit_sweeps)
+        b.warm_start_init(dt)
+        r_fit = residual_after(b, dt)
         used, fallback, r_end = iterations, True, target
         if r_fit <= r_plain[1]:
-            k, r = 1, r_fit
+            k, r = fit_sweeps, r_fit
             while r > target and k < max_iters:
-                g.solve_ex(dt, 1, False)
+                b.solve_ex(dt, 1, False)
                 k += 1
-                r = residual_after(g, dt)
+                r = residual_after(b, dt)
             if r <= target and k <= iterations:
                 used, fallback, r_end = k, False, r
-        g.set_warm_start(None)
-        out.append({"seed": int(s), "r_plain": float(target), "r_plain_1": float(r_plain[1]),
+        b.set_warm_start(None)
+        out.append({"seed": int(s), "same_start": same, "r_plain": float(target), "r_plain_1": float(r_plain[1]),
                     "r_fit": float(r_fit), "iterations": int(used), "fallback": bool(fallback),
                     "r_end": float(r_end)})
-        g.close()
+        a.close()
+        b.close()
     return out

@@ -34,4 +34,7 @@ def make_pair(scene, capi, oracle, **kw):
     order, off = g.tet_order()
     o = oracle.Oracle(scene)
     o.set_order(order, off)
+    if getattr(scene, "distance", None) is not None and len(scene.distance):
+        eo, eoff = g.distance_order()
+        o.set_edge_order(eo, eoff)
     return g, o

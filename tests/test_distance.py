@@ -1,0 +1,177 @@
+"""Distance constraints (distance_constraint_t, src/physics/xpbd/distance_constraint.cpp:8-53):
+oracle known answers on the CPU, GPU against the oracle running the same
+sweep order (tets, then the distance constraints in their colour order)."""
+import numpy as np
+import pytest
+
+from conftest import make_pair
+from sbs_gb300 import scenes
+
+SWEEP_TOL = 2e-5   # one sweep from an identical state, fraction of the bbox diagonal
+
+
+def two_tets_on_a_spring(stretch=0.1, alpha=0.0, beta=0.0):
+    """Two unit-mass-scale single-tet bodies, vertex 0 of each joined by a
+    spring of rest length 1; body 1 starts moved by `stretch` along x (a pure
+    translation: its tet stays at rest).  No gravity, no ground."""
+    x = np.array([[0.0, 0.0, 0.0], [0.3, 0.0, 0.0], [0.0, 0.3, 0.0], [0.0, 0.0, 0.3]])
+    t = np.array([[0, 1, 2, 3]], np.uint32)
+    a = scenes.Body(x0=x, tets=t, model=scenes.MODEL_STVK, young=1e5, poisson=0.3, density=1000.0)
+    b = scenes.Body(x0=x + [1.0, 0.0, 0.0], tets=t, model=scenes.MODEL_STVK, young=1e5, poisson=0.3,
+                    density=1000.0, x_init=x + [1.0 + stretch, 0.0, 0.0])
+    return scenes.Scene("spring-pair", [a, b], 1.0 / 60.0, 1, 1, 1, gravity=(0.0, 0.0, 0.0), ground=None,
+                        distance=np.array([[0, 1, 0, 0]], np.uint32), distance_compliance=alpha,
+                        distance_damping=beta)
+
+
+def spring_length(x):
+    return np.linalg.norm(x[0] - x[4])
+
+
+def xpbd_spring_step(x1, x2, w1, w2, d, alpha, dt):
+    """distance_constraint.cpp:24-53 for one projection from lambda = 0, beta = 0."""
+    diff = x1 - x2
+    L = np.linalg.norm(diff)
+    n = diff / L
+    at = alpha / dt ** 2
+    dl = -(L - d) / (w1 + w2 + at)
+    return x1 + w1 * n * dl, x2 - w2 * n * dl, dl
+
+
+@pytest.mark.parametrize("alpha", [0.0, 1e-3])
+def test_oracle_spring_known_answer(oracle_mod, alpha):
+    sc = two_tets_on_a_spring(alpha=alpha)
+    o = oracle_mod.Oracle(sc)
+    w = 1.0 / o.masses()
+    x = o.get()
+    dt = sc.frame_dt
+    o.L.orc_predict(o.h, dt)
+    o.L.orc_solve(o.h, dt, 1)
+    xi = o.get(oracle_mod.FIELD_XI)
+    e1, e2, dl = xpbd_spring_step(x[0], x[4], w[0], w[4], 1.0, alpha, dt)
+    assert np.abs(xi[0] - e1).max() < 1e-12 and np.abs(xi[4] - e2).max() < 1e-12
+    assert abs(o.distance_lambdas()[0] - dl) < 1e-12 * max(1.0, abs(dl))
+    if alpha == 0.0:
+        assert abs(spring_length(xi) - 1.0) < 1e-12
+    # the tets moved only with their spring end
+    assert np.abs(xi[1:4] - x[1:4]).max() == 0.0
+
+
+def test_oracle_springs_at_rest(oracle_mod):
+    sc = scenes.hanging_block()
+    sc.gravity = (0.0, 0.0, 0.0)
+    o = oracle_mod.Oracle(sc)
+    x0 = o.get()
+    o.step(3)
+    assert np.abs(o.get() - x0).max() < 1e-12
+    assert np.abs(o.distance_lambdas()).max() < 1e-12
+
+
+def test_scene_distance_rows_are_valid():
+    sc = scenes.hanging_block()
+    ends = []
+    offs = np.cumsum([0] + [len(b.x0) for b in sc.bodies])
+    for b1, b2, v1, v2 in sc.distance:
+        ends.append((offs[b1] + v1, offs[b2] + v2))
+    # the library's colouring is checked on the GPU tests; here the rows are valid
+    assert all(a != b for a, b in ends)
+
+
+def sync_from_oracle(g, o, oracle):
+    x = o.get().astype(np.float32).astype(np.float64)
+    v = o.get(oracle.FIELD_V).astype(np.float32).astype(np.float64)
+    o.set(oracle.FIELD_X, x)
+    o.set(oracle.FIELD_V, v)
+    g.set_state(-1, x, v)
+
+
+@pytest.mark.gpu
+def test_gpu_edge_colours_vertex_disjoint(capi_mod):
+    sc = scenes.hanging_block()
+    g = capi_mod.Solver(sc)
+    order, off = g.distance_order()
+    assert np.array_equal(np.sort(order), np.arange(len(sc.distance)))
+    offs = np.cumsum([0] + [len(b.x0) for b in sc.bodies])
+    for c in range(len(off) - 1):
+        rows = sc.distance[order[off[c]:off[c + 1]]]
+        ends = np.concatenate([offs[rows[:, 0]] + rows[:, 2], offs[rows[:, 1]] + rows[:, 3]])
+        assert len(np.unique(ends)) == len(ends)
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("alpha", [0.0, 1e-3])
+def test_gpu_spring_known_answer(capi_mod, oracle_mod, alpha):
+    sc = two_tets_on_a_spring(alpha=alpha)
+    g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=1)
+    dt = sc.frame_dt
+    g.predict(dt)
+    g.solve(dt, 1)
+    o.L.orc_predict(o.h, dt)
+    o.L.orc_solve(o.h, dt, 1)
+    xg = g.get_predicted(-1).astype(np.float64)
+    xo = o.get(oracle_mod.FIELD_XI)
+    assert np.abs(xg - xo).max() < 1e-6
+    assert abs(g.distance_lambdas()[0] - o.distance_lambdas()[0]) <= 1e-5 * abs(o.distance_lambdas()[0]) + 1e-9
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,beta", [(1, 0.0), (2, 0.0), (1, 1e-2)])
+def test_gpu_springs_one_sweep(capi_mod, oracle_mod, mode, beta):
+    sc = scenes.hanging_block(beta=beta)
+    g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=mode)
+    g.step(5)
+    o.step(5)
+    sync_from_oracle(g, o, oracle_mod)
+    dt = sc.frame_dt
+    o.L.orc_detect_contacts(o.h)
+    o.L.orc_predict(o.h, dt)
+    o.L.orc_solve(o.h, dt, 1)
+    g.detect_contacts()
+    g.predict(dt)
+    g.solve(dt, 1)
+    xg = g.get_predicted(-1).astype(np.float64)
+    xo = o.get(oracle_mod.FIELD_XI)
+    assert np.abs(xg - xo).max() / sc.bbox_diag() < SWEEP_TOL
+    lg, lo = g.distance_lambdas(), o.distance_lambdas()
+    assert np.abs(lg - lo).max() <= 1e-2 * np.abs(lo).max() + 1e-12
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [1, 2])
+def test_gpu_springs_hold_the_block(capi_mod, oracle_mod, mode):
+    sc = scenes.hanging_block(alpha=1e-7)
+    g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=mode)
+    g.step(30)
+    o.step(30)
+    x = g.positions()
+    assert np.isfinite(x).all()
+    offs = np.cumsum([0] + [len(b.x0) for b in sc.bodies])
+    rows = sc.distance
+    p1 = x[offs[rows[:, 0]] + rows[:, 2]]
+    p2 = x[offs[rows[:, 1]] + rows[:, 3]]
+    x0 = np.concatenate([b.x0 for b in sc.bodies])
+    d = np.linalg.norm(x0[offs[rows[:, 0]] + rows[:, 2]] - x0[offs[rows[:, 1]] + rows[:, 3]], axis=1)
+    # the hanging block stays on its springs (no fall to the ground)
+    assert np.abs(np.linalg.norm(p1 - p2, axis=1) - d).max() < 0.05
+    assert x[offs[1]:, 1].min() > -0.8
+    # same physics as the oracle: the block's centre within 1 cm after 30 frames
+    c_g = x[offs[1]:].mean(0)
+    c_o = o.get()[offs[1]:].mean(0)
+    assert np.abs(c_g - c_o).max() < 1e-2
+    r, _ = g.residual(sc.frame_dt)
+    assert np.isfinite(r)
+    g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_distance_rejects_bad_input(capi_mod):
+    sc = scenes.hanging_block()
+    sc.distance = np.array([[0, 5, 0, 0]], np.uint32)   # no body 5
+    with pytest.raises(capi_mod.SbsError):
+        capi_mod.Solver(sc)
+    sc = scenes.hanging_block()
+    with pytest.raises(capi_mod.SbsError):
+        capi_mod.Solver(sc, exec_mode=3)   # cluster-resident mode runs no distance constraints

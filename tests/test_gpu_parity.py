@@ -203,6 +203,46 @@ def test_graph_and_persistent_agree(capi_mod, oracle_mod):
     assert np.abs(a.positions() - b.positions()).max() < 20 * floor + 1e-7
 
 
+@pytest.mark.parametrize("make,frames", [(scenes.beam_c1, 1), (lambda: scenes.beam_twist(16, 4, 4, 0.05), 1)])
+def test_wavefront_matches_oracle(capi_mod, oracle_mod, make, frames):
+    sc = make()
+    g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=capi_mod.EXEC_WAVEFRONT)
+    assert g.stats().exec_mode == capi_mod.EXEC_WAVEFRONT
+    g.step(frames)
+    o.step(frames)
+    floor = noise_floor(sc, oracle_mod, frames)
+    assert np.abs(g.positions() - o.get()).max() < 20 * floor + 1e-7
+
+
+def test_wavefront_with_contacts_and_springs(capi_mod, oracle_mod):
+    # ground contacts (beam on a raised plane) and distance constraints take
+    # the wavefront kernel's grid-barrier paths
+    sc = scenes.beam_c1()
+    sc.ground = ((0.0, 1.0, 0.0), -0.05)
+    a = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_WAVEFRONT)
+    b = capi_mod.Solver(sc, exec_mode=1)
+    a.step(3)
+    b.step(3)
+    floor = noise_floor(sc, oracle_mod, 3)
+    assert a.stats().n_contacts > 0
+    assert np.abs(a.positions() - b.positions()).max() < 20 * floor + 1e-7
+    hb = scenes.hanging_block()
+    a = capi_mod.Solver(hb, exec_mode=capi_mod.EXEC_WAVEFRONT)
+    b = capi_mod.Solver(hb, exec_mode=1)
+    a.step(5)
+    b.step(5)
+    assert np.abs(a.positions() - b.positions()).max() < 1e-3
+
+
+def test_wavefront_deterministic(capi_mod):
+    sc = scenes.beam_twist(16, 4, 4, 0.05)
+    a = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_WAVEFRONT)
+    b = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_WAVEFRONT)
+    a.step(5)
+    b.step(5)
+    assert np.array_equal(a.positions(), b.positions())
+
+
 def test_residual_matches_oracle(capi_mod, oracle_mod):
     for sc in (scenes.beam_c1(), scenes.beam_twist(16, 4, 4, 0.05)):
         g, o = make_pair(sc, capi_mod, oracle_mod)
