@@ -56,6 +56,15 @@ MATERIALS = {
 }
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum per launch (one launch = one
+# frame for these kernels), from profiles/k_cluster_frame_beam98k.md and
+# profiles/k_frame_block2m.md
+TRAFFIC = {
+    ("beam-98304-snh-twist", "k_cluster_frame"): 7.09e6,
+    ("block-2621440-snh", "k_frame_t<false>"): 22.856e9 + 2.567e9,
+}
+
+
 def workload(name: str):
     from sbs_gb300 import scenes
     if name == "beam98k":
@@ -214,6 +223,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="beam98k")
     ap.add_argument("--exec-mode", type=int, default=0)
+    ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: the library's choice)")
     ap.add_argument("--cpu-budget", type=int, default=25_000_000,
                     help="tet projections in the single-thread CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -235,7 +245,7 @@ def main():
 
     from sbs_gb300 import capi
     scene = workload(args.workload)
-    solver = capi.Solver(scene, device=device, exec_mode=args.exec_mode)
+    solver = capi.Solver(scene, device=device, exec_mode=args.exec_mode, block_size=args.block)
     per_frame = scene.substeps * scene.iterations * scene.n_tets
 
     for _ in range(max(3, args.warmup)):
@@ -310,13 +320,6 @@ def main():
         peak, peak_src = float(peaks["hbm_gbs"]), "measured"
     except Exception:
         peak, peak_src = 6800.0, "fallback"
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get(scene.name)
-        except Exception:
-            traffic = None
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -330,6 +333,9 @@ def main():
     resident = footprint < 100 * 1024 * 1024
     kernel = {capi.EXEC_PERSISTENT: "k_frame_t<false>", capi.EXEC_CLUSTER: "k_cluster_frame",
               capi.EXEC_WAVEFRONT: "k_frame_t<true>"}.get(st.exec_mode, "k_colour")
+    # DRAM bytes (read + write) per launch of the dominant kernel from one ncu
+    # capture of the same workload and mode (summaries under profiles/)
+    traffic = TRAFFIC.get((scene.name, kernel))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_frame, "higher_is_better": True,

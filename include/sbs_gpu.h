@@ -144,6 +144,57 @@ sbs_status sbs_gpu_set_external_acceleration(sbs_gpu* h, int32_t body, const flo
  * environment_body_t in main.cpp:60-72. */
 sbs_status sbs_gpu_add_ground_plane(sbs_gpu* h, const double n[3], double d);
 
+/* Initial velocity of every vertex of a body (physics_body_info::velocity of
+ * a scene object, load_scene.cpp:246-250).  Before finalize. */
+sbs_status sbs_gpu_set_body_velocity(sbs_gpu* h, int32_t body, const double v[3]);
+
+/* read_ply (src/io/ply.cpp): vertex x y z (kept as float, as geometry_t does),
+ * `face` elements with 3 indices -> triangles, `tet` elements with 4 -> tets;
+ * ascii, binary_little_endian or binary_big_endian.  Any output may be NULL
+ * (counts only); capacities are in vertices / triangles / tets.  Host only. */
+sbs_status sbs_io_read_ply(const char* path, float* positions, uint32_t cap_verts, uint32_t* n_verts,
+                           uint32_t* tris, uint32_t cap_tris, uint32_t* n_tris, uint32_t* tets, uint32_t cap_tets,
+                           uint32_t* n_tets);
+/* load_scene (src/io/load_scene.cpp:83-365) into a handle before finalize:
+ * every "environment" entry that is a collideable PLY triangle mesh becomes
+ * an environment SDF (sbs_gpu_add_environment_mesh over the mesh's bounds
+ * grown by env_margin metres on every side - the depth below a floor in which
+ * contacts are found - with env_cells cells per axis); every "objects" entry
+ * with a PLY tet mesh becomes
+ * a body with `material` (its density replaced by "physics"."mass", the
+ * reference's mass density) and initial velocity "physics"."velocity".  Both
+ * are first rescaled into their "box" and moved by their "translation" as the
+ * reference does.  Paths are relative to the JSON file.  Lights, colours and
+ * non-PLY assets are skipped.  *first_body / *n_bodies: the bodies added. */
+sbs_status sbs_gpu_load_scene(sbs_gpu* h, const char* json_path, const sbs_gpu_material* material,
+                              const uint32_t env_cells[3], double env_margin, int32_t* first_body,
+                              int32_t* n_bodies);
+
+/* Signed-distance grid of an environment body: node values [nx * ny * nz],
+ * index (k * ny + j) * nx + i at origin + (i, j, k) * spacing, evaluated by
+ * trilinear interpolation with the interpolant's gradient.  Surface vertices
+ * with sd < 0 get the contact of bvh_model.cpp:72-94 (n = normalised
+ * gradient, q = p + |sd| n); outside the grid there is no contact.  Stands in
+ * for the Discregrid cubic Lagrange grid of sdf_model_t
+ * (src/physics/collision/sdf_model.cpp:66-75).  Up to 2 grids; planes and
+ * grids together at most 4, planes first.  Before finalize; not with
+ * SBS_EXEC_CLUSTER. */
+sbs_status sbs_gpu_add_sdf_grid(sbs_gpu* h, const float* values, const uint32_t nodes[3], const double origin[3],
+                                const double spacing[3]);
+/* environment_body_t's constructor (src/physics/environment_body.cpp:12-78) for
+ * a triangle mesh (outward winding): the domain grown over the mesh vertices
+ * and padded as that constructor does, `cells` cells per axis, node values from
+ * sbs_gpu_sdf_from_mesh, added with sbs_gpu_add_sdf_grid. */
+sbs_status sbs_gpu_add_environment_mesh(sbs_gpu* h, const double* verts, uint32_t n_verts, const uint32_t* tris,
+                                        uint32_t n_tris, const double domain_lo[3], const double domain_hi[3],
+                                        const uint32_t cells[3]);
+/* Host only (no handle, no GPU): signed distance of a triangle mesh at the
+ * (cells + 1)^3 nodes of the box [lo, hi], into values (layout as above).
+ * Closest point per triangle (Ericson 2005, 5.1.5), sign from the angle-weighted
+ * pseudonormal (Baerentzen & Aanaes 2005); brute force over triangles. */
+sbs_status sbs_gpu_sdf_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris, uint32_t n_tris,
+                                 const double lo[3], const double hi[3], const uint32_t cells[3], float* values);
+
 /* Distance constraints: n rows of ids [4n] = (b1, b2, v1, v2) - body and
  * body-local vertex of each end, the order of distance_constraint_t's
  * constructor (src/physics/xpbd/distance_constraint.cpp:8-22) - with

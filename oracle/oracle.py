@@ -49,6 +49,7 @@ def lib():
         L.orc_add_kinematic_rotation.argtypes = [P, I, up, U32, dp, dp, D]
         L.orc_set_external_acceleration.argtypes = [P, I, dp]
         L.orc_add_ground_plane.argtypes = [P, dp, D]
+        L.orc_add_sdf_grid.argtypes = [P, C.c_void_p, up, dp, dp]
         L.orc_set_tet_order.restype = I
         L.orc_set_tet_order.argtypes = [P, up, U32, C.c_void_p, U32]
         L.orc_step.argtypes = [P, D, U32, U32]
@@ -149,6 +150,12 @@ class Oracle:
         if scene.ground is not None:
             n, d = scene.ground
             L.orc_add_ground_plane(self.h, np.asarray(n, np.float64), d)
+        self._grids = []
+        for values, nodes, origin, spacing in getattr(scene, "sdf_grids", None) or []:
+            v = np.ascontiguousarray(values, np.float32).ravel()
+            self._grids.append(v)
+            L.orc_add_sdf_grid(self.h, v.ctypes.data, np.ascontiguousarray(nodes, np.uint32),
+                               np.asarray(origin, np.float64), np.asarray(spacing, np.float64))
         if getattr(scene, "body_contacts", 0):
             cell = scene.hash_cell if scene.hash_cell > 0 else mean_edge_cell(scene)
             self.hash_cell = cell

@@ -214,6 +214,46 @@ struct kinematic_t {
 
 struct plane_t { vec3 n; double d; };
 
+// Signed-distance grid of an environment body (addition: the reference
+// samples a Discregrid cubic Lagrange grid, sdf_model.cpp:66-75; here node
+// values with trilinear interpolation and the interpolant's gradient).
+struct grid_t {
+    std::vector<double> v;
+    uint32_t n[3];
+    double o[3], h[3];
+    // false outside the grid (no contact there)
+    bool eval(vec3 p, double& sd, vec3& g) const {
+        const double u[3] = {(p.x - o[0]) / h[0], (p.y - o[1]) / h[1], (p.z - o[2]) / h[2]};
+        uint32_t c[3];
+        double f[3];
+        for (int k = 0; k < 3; ++k) {
+            if (!(u[k] >= 0.0 && u[k] <= (double)(n[k] - 1))) return false;
+            c[k] = std::min((uint32_t)u[k], n[k] - 2);
+            f[k] = u[k] - c[k];
+        }
+        auto at = [&](uint32_t i, uint32_t j, uint32_t k) {
+            return v[((size_t)(c[2] + k) * n[1] + (c[1] + j)) * n[0] + (c[0] + i)];
+        };
+        double w[2][2][2];
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) w[i][j][k] = at(i, j, k);
+        const double fx = f[0], fy = f[1], fz = f[2];
+        sd = 0.0;
+        g = {0.0, 0.0, 0.0};
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) {
+                    const double bx = i ? fx : 1 - fx, by = j ? fy : 1 - fy, bz = k ? fz : 1 - fz;
+                    sd += w[i][j][k] * bx * by * bz;
+                    g.x += w[i][j][k] * (i ? 1.0 : -1.0) * by * bz / h[0];
+                    g.y += w[i][j][k] * bx * (j ? 1.0 : -1.0) * bz / h[1];
+                    g.z += w[i][j][k] * bx * by * (k ? 1.0 : -1.0) / h[2];
+                }
+        return true;
+    }
+};
+
 struct body_t {
     uint32_t v0, nv, t0, nt;
     std::vector<uint32_t> surface;   // global vertex ids, ascending
@@ -283,6 +323,7 @@ struct sim_t {
     std::vector<uint32_t> ground_end;                                  // ground contacts per plane
     std::vector<kinematic_t> kinematics;
     std::vector<plane_t> planes;
+    std::vector<grid_t> grids;              // environment slots after the planes
     std::vector<tet_topo_t> topo;          // global tet order
     std::vector<uint32_t> vbody;           // per particle
     std::vector<uint8_t> vsurf;            // per particle: surface vertex
@@ -530,6 +571,24 @@ static void detect_ground(sim_t& sim) {
                 vec3 q = p + pl.n * std::fabs(sd);
                 sim.collision_constraints.push_back(std::make_unique<collision_constraint_t>(
                     sim.prm.collision_alpha, 0.0, vi, q, pl.n));
+            }
+        }
+        sim.ground_end.push_back((uint32_t)sim.collision_constraints.size());
+    }
+    // signed-distance grids: bvh_model.cpp:72-94, n = normalised gradient,
+    // q = p + |sd| n
+    for (const grid_t& gr : sim.grids) {
+        for (const body_t& b : sim.bodies) {
+            for (uint32_t vi : b.surface) {
+                const vec3 p = sim.particles[vi].x;
+                double sd;
+                vec3 g;
+                if (!gr.eval(p, sd, g) || !(sd < 0.0)) continue;
+                const double l = norm(g);
+                if (!(l > 0.0)) continue;
+                const vec3 n = g / l;
+                sim.collision_constraints.push_back(std::make_unique<collision_constraint_t>(
+                    sim.prm.collision_alpha, 0.0, vi, p + n * std::fabs(sd), n));
             }
         }
         sim.ground_end.push_back((uint32_t)sim.collision_constraints.size());
@@ -901,6 +960,21 @@ void orc_set_external_acceleration(void* h, int body, const double* acc) {
     const body_t& b = s.bodies[body];
     for (uint32_t i = 0; i < b.nv; ++i)
         s.particles[b.v0 + i].ext_acc = {acc[3 * i], acc[3 * i + 1], acc[3 * i + 2]};
+}
+
+void orc_add_sdf_grid(void* h, const float* values, const uint32_t* nodes, const double* origin,
+                      const double* spacing) {
+    sim_t& s = *(sim_t*)h;
+    grid_t g;
+    size_t n = 1;
+    for (int k = 0; k < 3; ++k) {
+        g.n[k] = nodes[k];
+        g.o[k] = origin[k];
+        g.h[k] = spacing[k];
+        n *= nodes[k];
+    }
+    g.v.assign(values, values + n);
+    s.grids.push_back(std::move(g));
 }
 
 void orc_add_ground_plane(void* h, const double* n, double d) {

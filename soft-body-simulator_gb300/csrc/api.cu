@@ -57,6 +57,7 @@ struct sbs_gpu {
 
     // scene as added (global "old" vertex ids = body offset + local id)
     std::vector<double> x0, xinit, mass;
+    std::vector<float> vinit;            // initial velocities, 3 per vertex
     std::vector<uint8_t> user_mass;
     std::vector<uint32_t> tets;          // 4 per tet, old global ids
     std::vector<int32_t> tet_model;
@@ -67,6 +68,14 @@ struct sbs_gpu {
     std::vector<float> acc;
     bool has_acc = false;
     std::vector<Plane> planes;
+    // signed-distance grids of environment bodies (after the planes)
+    struct GridHost {
+        std::vector<float> v;
+        uint32_t n[3];
+        double o[3], h[3];
+    };
+    std::vector<GridHost> grids;
+    std::vector<float*> grid_dev;
 
     // after finalize
     uint32_t n_verts = 0, n_tets = 0;
@@ -219,31 +228,146 @@ static int colour_tets(const std::vector<uint32_t>& tets, uint32_t n_verts, cons
             else vm[tets[4 * t + k]][1] |= 1ull << (c - 64);
         }
     };
-    int K = 0;
-    for (uint32_t t : order) {
-        int c = pick(t, nullptr, 0);
-        if (c < 0) return -1;
-        colour[t] = c;
-        mark(t, c);
-        K = std::max(K, c + 1);
+    auto greedy = [&](const std::vector<uint32_t>& ord, std::vector<int32_t>& col) -> int {
+        for (auto& m : vm) m = {0ull, 0ull};
+        int k = 0;
+        for (uint32_t t : ord) {
+            const int c = pick(t, nullptr, 0);
+            if (c < 0) return -1;
+            col[t] = c;
+            mark(t, c);
+            k = std::max(k, c + 1);
+        }
+        return k;
+    };
+    int K = greedy(order, colour);
+    if (K < 0) return -1;
+    // DSATUR (Brelaz 1979): colour next the uncoloured tet whose neighbours
+    // (tets sharing a vertex) already use the most distinct colours, with
+    // the smallest colour free at its vertices; kept when it needs fewer
+    // colours than first-fit.  Saturations come from the vertex colour masks.
+    if (T <= 4000000) {
+        const uint32_t NV = n_verts;
+        std::vector<uint32_t> inc_start(NV + 1, 0), inc;
+        for (uint32_t t : order)
+            for (int k = 0; k < 4; ++k) inc_start[tets[4 * t + k] + 1]++;
+        for (uint32_t v = 0; v < NV; ++v) inc_start[v + 1] += inc_start[v];
+        inc.resize(inc_start[NV]);
+        {
+            std::vector<uint32_t> fill(inc_start.begin(), inc_start.end() - 1);
+            for (uint32_t t : order)
+                for (int k = 0; k < 4; ++k) inc[fill[tets[4 * t + k]]++] = t;
+        }
+        for (auto& m : vm) m = {0ull, 0ull};
+        std::vector<int32_t> cd(colour.size(), -1);
+        std::vector<uint8_t> sat(colour.size(), 0);
+        std::vector<std::vector<uint32_t>> bucket(kMaxColours + 1);
+        auto saturation = [&](uint32_t t) {
+            uint64_t f0 = 0, f1 = 0;
+            for (int k = 0; k < 4; ++k) {
+                f0 |= vm[tets[4 * t + k]][0];
+                f1 |= vm[tets[4 * t + k]][1];
+            }
+            return (uint8_t)(__builtin_popcountll(f0) + __builtin_popcountll(f1));
+        };
+        // seed in reverse Morton order so the LIFO bucket starts at the first tet
+        for (size_t i = order.size(); i-- > 0;) bucket[0].push_back(order[i]);
+        int top = 0, Kd = 0;
+        bool ok = true;
+        for (size_t done = 0; done < T && ok;) {
+            while (top > 0 && bucket[top].empty()) --top;
+            if (bucket[top].empty()) break;
+            const uint32_t t = bucket[top].back();
+            bucket[top].pop_back();
+            if (cd[t] >= 0 || sat[t] != top) continue;   // stale entry
+            const int c = pick(t, nullptr, 0);
+            if (c < 0) { ok = false; break; }
+            cd[t] = c;
+            mark(t, c);
+            Kd = std::max(Kd, c + 1);
+            ++done;
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t v = tets[4 * t + k];
+                for (uint32_t j = inc_start[v]; j < inc_start[v + 1]; ++j) {
+                    const uint32_t u = inc[j];
+                    if (cd[u] >= 0) continue;
+                    const uint8_t su = saturation(u);
+                    if (su != sat[u]) {
+                        sat[u] = su;
+                        bucket[su].push_back(u);
+                        top = std::max(top, (int)su);
+                    }
+                }
+            }
+        }
+        if (ok && Kd > 0 && Kd < K) {
+            bool all = true;
+            for (uint32_t t : order) all &= cd[t] >= 0;
+            if (all) {
+                colour.swap(cd);
+                K = Kd;
+            }
+        }
     }
-    // balanced pass
-    std::vector<uint32_t> size(kMaxColours, 0);
+    // iterated greedy (Culberson): first-fit again over the tets listed class
+    // by class never needs more colours and often needs fewer; the class
+    // order varies between passes (reverse, largest first, smallest first)
+    {
+        const int passes = T <= 500000 ? 24 : T <= 4000000 ? 8 : 0;
+        std::vector<int32_t> c2(colour.size(), -1);
+        std::vector<uint32_t> ord(T);
+        for (int pass = 0; pass < passes && K > 1; ++pass) {
+            std::vector<uint32_t> size(K, 0);
+            for (uint32_t t : order) size[colour[t]]++;
+            std::vector<int> rank(K);
+            for (int c = 0; c < K; ++c) rank[c] = c;
+            if (pass % 3 == 0) std::reverse(rank.begin(), rank.end());
+            else if (pass % 3 == 1) std::stable_sort(rank.begin(), rank.end(), [&](int a, int b) { return size[a] > size[b]; });
+            else std::stable_sort(rank.begin(), rank.end(), [&](int a, int b) { return size[a] < size[b]; });
+            std::vector<uint32_t> start(K + 1, 0);
+            std::vector<int> pos(K);
+            for (int r = 0; r < K; ++r) pos[rank[r]] = r;
+            for (int c = 0; c < K; ++c) start[pos[c] + 1] = size[c];
+            for (int r = 0; r < K; ++r) start[r + 1] += start[r];
+            for (uint32_t t : order) ord[start[pos[colour[t]]]++] = t;   // Morton order kept inside a class
+            const int K2 = greedy(ord, c2);
+            if (K2 < 0 || K2 > K) break;
+            colour.swap(c2);
+            K = K2;
+        }
+    }
+    // balance the classes: move tets of oversized classes into the smallest
+    // class they fit (no shared vertex); the colour count does not change
+    std::vector<uint32_t> size(K, 0);
+    for (uint32_t t : order) size[colour[t]]++;
     const uint32_t cap = (uint32_t)std::ceil((double)T / K * 1.02) + 1;
     for (auto& m : vm) m = {0ull, 0ull};
-    std::vector<int32_t> c2(colour.size(), -1);
-    int K2 = 0;
+    for (uint32_t t : order) mark(t, colour[t]);
     for (uint32_t t : order) {
-        int c = pick(t, &size, cap);
-        if (c < 0) return K;  // keep the first-fit colouring
-        c2[t] = c;
-        mark(t, c);
-        size[c]++;
-        K2 = std::max(K2, c + 1);
-    }
-    if (K2 <= K + 2) {
-        colour.swap(c2);
-        return K2;
+        const int c = colour[t];
+        if (size[c] <= cap) continue;
+        uint64_t f0 = 0, f1 = 0;
+        for (int k = 0; k < 4; ++k) {
+            f0 |= vm[tets[4 * t + k]][0];
+            f1 |= vm[tets[4 * t + k]][1];
+        }
+        int best = -1;
+        for (int d = 0; d < K; ++d) {
+            const bool used = d < 64 ? ((f0 >> d) & 1ull) : ((f1 >> (d - 64)) & 1ull);
+            if (used || size[d] >= cap) continue;
+            if (best < 0 || size[d] < size[best]) best = d;
+        }
+        if (best < 0) continue;
+        // bit c stays set at t's vertices: conservative, as c is oversized
+        // and takes no tets
+        colour[t] = best;
+        size[c]--;
+        size[best]++;
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t v = tets[4 * t + k];
+            if (best < 64) vm[v][0] |= 1ull << best;
+            else vm[v][1] |= 1ull << (best - 64);
+        }
     }
     return K;
 }
@@ -417,6 +541,7 @@ sbs_status sbs_gpu_add_body(sbs_gpu* h, const double* x0, const double* x_init, 
     h->x0.insert(h->x0.end(), x0, x0 + 3ull * n_verts);
     if (x_init) h->xinit.insert(h->xinit.end(), x_init, x_init + 3ull * n_verts);
     else h->xinit.insert(h->xinit.end(), x0, x0 + 3ull * n_verts);
+    h->vinit.resize(h->xinit.size(), 0.0f);
     // lumped masses: density * |V0| / 4 per incident tet
     std::vector<double> m(n_verts, 0.0);
     for (uint32_t t = 0; t < n_tets; ++t) {
@@ -497,7 +622,8 @@ sbs_status sbs_gpu_set_external_acceleration(sbs_gpu* h, int32_t body, const flo
 sbs_status sbs_gpu_add_ground_plane(sbs_gpu* h, const double n[3], double d) {
     if (!h || !n) return fail(h, SBS_EINVAL, "plane: null");
     if (h->finalized) return fail(h, SBS_ESTATE, "plane after finalize");
-    if (h->planes.size() >= (size_t)kMaxPlanes) return fail(h, SBS_EINVAL, "too many planes");
+    if (h->planes.size() + h->grids.size() >= (size_t)kMaxPlanes) return fail(h, SBS_EINVAL, "too many planes");
+    if (!h->grids.empty()) return fail(h, SBS_ESTATE, "add planes before sdf grids");
     double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
     if (!(l > 0) || !std::isfinite(d)) return fail(h, SBS_EINVAL, "plane normal");
     h->planes.push_back(Plane{(float)(n[0] / l), (float)(n[1] / l), (float)(n[2] / l), (float)(d / l)});
@@ -567,6 +693,76 @@ static int colour_edges(const std::vector<uint32_t>& ends, uint32_t V, std::vect
     return K;
 }
 
+sbs_status sbs_gpu_set_body_velocity(sbs_gpu* h, int32_t body, const double v[3]) {
+    if (!h || !v) return fail(h, SBS_EINVAL, "velocity: null");
+    if (h->finalized) return fail(h, SBS_ESTATE, "initial velocity after finalize (use sbs_gpu_set_state)");
+    if (body < 0 || body >= (int32_t)h->bodies.size()) return fail(h, SBS_EINVAL, "body id");
+    if (!std::isfinite(v[0]) || !std::isfinite(v[1]) || !std::isfinite(v[2])) return fail(h, SBS_EINVAL, "velocity");
+    const BodyHost& b = h->bodies[body];
+    for (uint32_t i = 0; i < b.nv; ++i)
+        for (int k = 0; k < 3; ++k) h->vinit[3ull * (b.v0 + i) + k] = (float)v[k];
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_add_sdf_grid(sbs_gpu* h, const float* values, const uint32_t nodes[3], const double origin[3],
+                                const double spacing[3]) {
+    if (!h || !values || !nodes || !origin || !spacing) return fail(h, SBS_EINVAL, "sdf grid: null");
+    if (h->finalized) return fail(h, SBS_ESTATE, "sdf grid after finalize");
+    if (h->grids.size() >= (size_t)kMaxGrids) return fail(h, SBS_EINVAL, "too many sdf grids");
+    if (h->planes.size() + h->grids.size() >= (size_t)kMaxPlanes)
+        return fail(h, SBS_EINVAL, "too many environment bodies (planes + grids)");
+    sbs_gpu::GridHost g;
+    size_t n = 1;
+    for (int k = 0; k < 3; ++k) {
+        if (nodes[k] < 2 || nodes[k] > 4096) return fail(h, SBS_EINVAL, "sdf grid: 2..4096 nodes per axis");
+        if (!(spacing[k] > 0) || !std::isfinite(origin[k])) return fail(h, SBS_EINVAL, "sdf grid: spacing/origin");
+        g.n[k] = nodes[k];
+        g.o[k] = origin[k];
+        g.h[k] = spacing[k];
+        n *= nodes[k];
+    }
+    g.v.assign(values, values + n);
+    for (float f : g.v)
+        if (!std::isfinite(f)) return fail(h, SBS_EINVAL, "sdf grid: non-finite value");
+    h->grids.push_back(std::move(g));
+    return SBS_OK;
+}
+
+extern "C" sbs_status sbs_gpu_sdf_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris,
+                                            uint32_t n_tris, const double lo[3], const double hi[3],
+                                            const uint32_t cells[3], float* values);
+
+sbs_status sbs_gpu_add_environment_mesh(sbs_gpu* h, const double* verts, uint32_t n_verts, const uint32_t* tris,
+                                        uint32_t n_tris, const double domain_lo[3], const double domain_hi[3],
+                                        const uint32_t cells[3]) {
+    if (!h || !verts || !tris || !domain_lo || !domain_hi || !cells) return fail(h, SBS_EINVAL, "environment: null");
+    // the domain as environment_body_t extends it (environment_body.cpp:53-63):
+    // for every mesh vertex, grow the box over all vertices and pad both
+    // corners by 1e-3 of the current diagonal
+    double lo[3] = {domain_lo[0], domain_lo[1], domain_lo[2]}, hi[3] = {domain_hi[0], domain_hi[1], domain_hi[2]};
+    for (uint32_t a = 0; a < n_verts; ++a) {
+        for (uint32_t b = 0; b < n_verts; ++b)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], verts[3ull * b + k]);
+                hi[k] = std::max(hi[k], verts[3ull * b + k]);
+            }
+        const double dg = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                    (hi[2] - lo[2]) * (hi[2] - lo[2]));
+        for (int k = 0; k < 3; ++k) {
+            hi[k] += 1e-3 * dg;
+            lo[k] -= 1e-3 * dg;
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+        if (cells[k] == 0 || cells[k] > 4095) return fail(h, SBS_EINVAL, "environment: 1..4095 cells per axis");
+    std::vector<float> v((size_t)(cells[0] + 1) * (cells[1] + 1) * (cells[2] + 1));
+    const sbs_status s = sbs_gpu_sdf_from_mesh(verts, n_verts, tris, n_tris, lo, hi, cells, v.data());
+    if (s) return fail(h, s, "environment: bad mesh or domain");
+    const uint32_t nodes[3] = {cells[0] + 1, cells[1] + 1, cells[2] + 1};
+    const double sp[3] = {(hi[0] - lo[0]) / cells[0], (hi[1] - lo[1]) / cells[1], (hi[2] - lo[2]) / cells[2]};
+    return sbs_gpu_add_sdf_grid(h, v.data(), nodes, lo, sp);
+}
+
 static sbs_status upload(sbs_gpu* h, void* dst, const void* src, size_t bytes) {
     if (bytes == 0) return SBS_OK;
     CU(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->st));
@@ -588,25 +784,39 @@ static void fill_params(sbs_gpu* h, StepParams& p, double dt, uint32_t substeps,
     p.iterations = (int)iterations;
 }
 
-// Wavefront mode: CTA b of G owns the slice [c0 + b n / G, c0 + (b+1) n / G)
-// of every colour (c0, n: colour start and size).  Two CTAs are neighbours
-// when some vertex is touched by tets of both.  Returns the CSR lists.
-static void wave_neighbours(const std::vector<uint4>& tid, const std::vector<uint32_t>& offsets, int K, int G,
-                            std::vector<uint32_t>& start, std::vector<uint32_t>& list) {
-    std::vector<uint64_t> pairs;   // vertex * G + cta
-    pairs.reserve(tid.size() * 4);
+// Wavefront mode.  The vertex slots (per-body Morton order) are cut into G
+// equal ranges, one per CTA; a tet belongs to the CTA of its lowest vertex
+// slot, so a CTA covers the same region of the mesh in every colour.  Outputs
+// per (colour c, CTA b) the tet slots b projects in c (CSR: start[c * (G+1) + b]
+// into idx) and, per CTA, the CTAs whose tets share a vertex with its own.
+static void wave_partition(const std::vector<uint4>& tid, const std::vector<uint32_t>& offsets, int K, int G,
+                           uint32_t V, std::vector<uint32_t>& wstart, std::vector<uint32_t>& widx,
+                           std::vector<uint32_t>& nstart, std::vector<uint32_t>& nlist) {
+    const size_t T = tid.size();
+    std::vector<uint32_t> owner(T);
+    for (size_t k = 0; k < T; ++k) {
+        const uint4 q = tid[k];
+        const uint32_t m = std::min(std::min(q.x, q.y), std::min(q.z, q.w));
+        owner[k] = (uint32_t)((uint64_t)m * G / V);
+    }
+    wstart.assign((size_t)K * (G + 1), 0);
+    widx.resize(T);
     for (int c = 0; c < K; ++c) {
-        const uint64_t c0 = offsets[c], n = offsets[c + 1] - offsets[c];
-        for (int b = 0; b < G; ++b) {
-            const uint64_t lo = c0 + n * b / G, hi = c0 + n * (b + 1) / G;
-            for (uint64_t k = lo; k < hi; ++k) {
-                const uint4 q = tid[k];
-                pairs.push_back((uint64_t)q.x * G + b);
-                pairs.push_back((uint64_t)q.y * G + b);
-                pairs.push_back((uint64_t)q.z * G + b);
-                pairs.push_back((uint64_t)q.w * G + b);
-            }
-        }
+        uint32_t* st = &wstart[(size_t)c * (G + 1)];
+        for (uint32_t k = offsets[c]; k < offsets[c + 1]; ++k) st[owner[k] + 1]++;
+        st[0] = offsets[c];
+        for (int b = 0; b < G; ++b) st[b + 1] += st[b];
+        std::vector<uint32_t> fill(st, st + G);
+        for (uint32_t k = offsets[c]; k < offsets[c + 1]; ++k) widx[fill[owner[k]]++] = k;
+    }
+    std::vector<uint64_t> pairs;   // vertex * G + cta
+    pairs.reserve(T * 4);
+    for (size_t k = 0; k < T; ++k) {
+        const uint4 q = tid[k];
+        pairs.push_back((uint64_t)q.x * G + owner[k]);
+        pairs.push_back((uint64_t)q.y * G + owner[k]);
+        pairs.push_back((uint64_t)q.z * G + owner[k]);
+        pairs.push_back((uint64_t)q.w * G + owner[k]);
     }
     std::sort(pairs.begin(), pairs.end());
     pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
@@ -621,12 +831,12 @@ static void wave_neighbours(const std::vector<uint4>& tid, const std::vector<uin
             for (uint32_t b : ctas)
                 if (a != b) bits[(size_t)a * words + b / 64] |= 1ull << (b % 64);
     }
-    start.assign(G + 1, 0);
-    list.clear();
+    nstart.assign(G + 1, 0);
+    nlist.clear();
     for (int a = 0; a < G; ++a) {
         for (int b = 0; b < G; ++b)
-            if (bits[(size_t)a * words + b / 64] >> (b % 64) & 1ull) list.push_back((uint32_t)b);
-        start[a + 1] = (uint32_t)list.size();
+            if (bits[(size_t)a * words + b / 64] >> (b % 64) & 1ull) nlist.push_back((uint32_t)b);
+        nstart[a + 1] = (uint32_t)nlist.size();
     }
 }
 
@@ -683,7 +893,9 @@ sbs_status sbs_gpu_finalize(sbs_gpu* h) {
     // shared memory, else (or after a few tries) with the cluster mode excluded
     // distance constraints may join any two bodies: they run in the global modes only
     bool allow_cluster = h->prm.exec_mode != SBS_EXEC_GRAPH && h->prm.exec_mode != SBS_EXEC_PERSISTENT &&
-                         h->dist_p.empty();
+                         h->prm.exec_mode != SBS_EXEC_WAVEFRONT && h->dist_p.empty() && h->grids.empty();
+    if (!h->grids.empty() && h->prm.exec_mode == SBS_EXEC_CLUSTER)
+        return fail(h, SBS_EINVAL, "sdf grids do not run in the cluster-resident mode");
     if (!h->dist_p.empty() && h->prm.exec_mode == SBS_EXEC_CLUSTER)
         return fail(h, SBS_EINVAL, "distance constraints do not run in the cluster-resident mode");
 plan_again:
@@ -863,7 +1075,7 @@ plan_again:
         float w = m > 0.0 ? (float)(1.0 / m) : 0.0f;
         h->inv_mass[n] = w;
         xw[n] = make_float4((float)h->xinit[3ull * o], (float)h->xinit[3ull * o + 1], (float)h->xinit[3ull * o + 2], w);
-        vel[n] = make_float4(0, 0, 0, 0);
+        vel[n] = make_float4(h->vinit[3ull * o], h->vinit[3ull * o + 1], h->vinit[3ull * o + 2], 0.0f);
         if (h->kin_group[o] >= 0) {
             const KinGroup& g = h->groups[h->kin_group[o]];
             vel[n].w = (float)(1 + h->kin_group[o]);
@@ -1178,8 +1390,20 @@ plan_again:
     p.gravity_mode = h->prm.gravity_mode;
     p.n_colours = K;
     p.first_tail = (int)h->first_tail;
-    p.n_planes = (int)h->planes.size();
+    p.n_analytic = (int)h->planes.size();
+    p.n_planes = (int)(h->planes.size() + h->grids.size());
     for (size_t i = 0; i < h->planes.size(); ++i) p.planes[i] = h->planes[i];
+    h->grid_dev.assign(h->grids.size(), nullptr);
+    for (size_t g = 0; g < h->grids.size(); ++g) {
+        const auto& gh = h->grids[g];
+        if ((s = dalloc(h, &h->grid_dev[g], gh.v.size())) != SBS_OK) return s;
+        if ((s = upload(h, h->grid_dev[g], gh.v.data(), gh.v.size() * sizeof(float))) != SBS_OK) return s;
+        SdfGrid& dg = p.grids[g];
+        dg.v = h->grid_dev[g];
+        dg.nx = gh.n[0]; dg.ny = gh.n[1]; dg.nz = gh.n[2];
+        dg.ox = (float)gh.o[0]; dg.oy = (float)gh.o[1]; dg.oz = (float)gh.o[2];
+        dg.hx = (float)gh.h[0]; dg.hy = (float)gh.h[1]; dg.hz = (float)gh.h[2];
+    }
     p.n_kin_groups = (int)h->groups.size();
     p.has_acc = h->has_acc ? 1 : 0;
     p.body_contacts = h->body_on ? 1 : 0;
@@ -1216,17 +1440,25 @@ plan_again:
             h->cl_grid = std::max(1, std::min(active, (int)h->cd.n_groups));
         }
     }
-    // wavefront mode: one CTA slice of every colour per CTA, neighbour waits
+    // wavefront mode (only when asked for: measured slower than the grid
+    // barrier on every workload - 22 vs 9.4 ms on the 98k-tet beam, 40 vs
+    // 24.5 ms on the 2.6M-tet block - as each CTA has ~100 neighbours to poll)
     h->d.prog = nullptr;
     h->d.nb_start = nullptr;
     h->d.nb = nullptr;
+    h->d.wave_start = nullptr;
+    h->d.wave_idx = nullptr;
     h->wave_grid = 0;
-    if (h->global_modes && h->prm.exec_mode != SBS_EXEC_CLUSTER) {
+    if (h->global_modes && h->prm.exec_mode == SBS_EXEC_WAVEFRONT) {
         int wocc = 0;
         if (wavefront_occupancy(256, &wocc) == cudaSuccess && wocc > 0) {
             const int G = wocc * h->n_sm;
-            std::vector<uint32_t> st_, nb_;
-            wave_neighbours(tid, h->colour_offsets, K, G, st_, nb_);
+            std::vector<uint32_t> st_, nb_, ws_, wi_;
+            wave_partition(tid, h->colour_offsets, K, G, V, ws_, wi_, st_, nb_);
+            if ((s = dalloc(h, &h->d.wave_start, ws_.size())) != SBS_OK) return s;
+            if ((s = dalloc(h, &h->d.wave_idx, wi_.size())) != SBS_OK) return s;
+            if ((s = upload(h, h->d.wave_start, ws_.data(), ws_.size() * 4)) != SBS_OK) return s;
+            if ((s = upload(h, h->d.wave_idx, wi_.data(), wi_.size() * 4)) != SBS_OK) return s;
             if ((s = dalloc(h, &h->d.prog, G)) != SBS_OK) return s;
             if ((s = dalloc(h, &h->d.nb_start, G + 1)) != SBS_OK) return s;
             if ((s = dalloc(h, &h->d.nb, nb_.size())) != SBS_OK) return s;
@@ -1402,7 +1634,6 @@ static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t it
         }
     }
     if (h->global_modes) cands.push_back({SBS_EXEC_GRAPH, 256, h->grid});
-    if (h->wave_grid) cands.push_back({SBS_EXEC_WAVEFRONT, 256, h->wave_grid});
     const int saved_mode = h->exec_mode, saved_pb = h->pers_block, saved_pg = h->pers_grid;
     const uint64_t saved_frames = h->frames, saved_proj = h->projections;
     const double saved_time = h->sim_time;
@@ -1730,7 +1961,7 @@ sbs_status sbs_gpu_get_contacts(sbs_gpu* h, uint32_t* verts, float* qn, uint32_t
     const uint32_t* c = h->contacts_live ? cnt : cnt + kMaxPlanes + 1;
     std::vector<std::pair<std::pair<uint32_t, uint32_t>, std::array<float, 6>>> all;
     // ground planes in order, then the body-body segment (ordered after them)
-    const size_t P = h->planes.size();
+    const size_t P = h->planes.size() + h->grids.size();   // environment slots
     for (size_t seg = 0; seg <= P; ++seg) {
         const size_t src = seg < P ? seg : (size_t)kMaxPlanes;
         if (seg == P && !h->body_on) break;
@@ -1977,7 +2208,7 @@ sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st) {
     st->n_tets = h->n_tets;
     st->n_colours = h->n_colours;
     st->n_tail_colours = h->n_colours - h->first_tail;
-    for (size_t pl = 0; pl < h->planes.size(); ++pl) st->n_contacts += c[pl];
+    for (size_t pl = 0; pl < h->planes.size() + h->grids.size(); ++pl) st->n_contacts += c[pl];
     st->n_body_contacts = c[kMaxPlanes];
     st->exec_mode = h->exec_mode;
     st->grid_ctas = h->exec_mode == SBS_EXEC_WAVEFRONT     ? h->wave_grid

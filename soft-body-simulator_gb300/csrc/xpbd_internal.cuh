@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "sdf_eval.cuh"
+
 namespace sbs {
 
 constexpr int kMaxColours = 128;  // colour masks are two 64-bit words per vertex
@@ -62,6 +64,8 @@ struct SceneDev {
     uint32_t* prog;
     uint32_t* nb_start;
     uint32_t* nb;
+    uint32_t* wave_start;  // [colour * (G + 1) + cta]: first entry of the CTA's tets in wave_idx
+    uint32_t* wave_idx;    // tet slots, grouped by (colour, owning CTA)
     // reductions
     double* red_out;       // [4]: residual^2 (elastic), energy, residual^2 (contacts), spare
     float* partials;       // per-CTA partial sums for the residual kernel
@@ -88,13 +92,15 @@ struct StepParams {
     int gravity_mode;
     int n_colours;
     int first_tail;              // colours [first_tail, n_colours) run in one CTA
-    int n_planes;
+    int n_planes;                // environment slots: analytic planes, then SDF grids
+    int n_analytic;              // slots [0, n_analytic) are planes
     int n_kin_groups;
     int substeps, iterations;
     int body_contacts;
     int has_acc;                 // 1 when an external acceleration field is set
     double dt_d;
     Plane planes[kMaxPlanes];
+    SdfGrid grids[kMaxGrids];    // slot n_analytic + g
     KinGroup kin[kMaxKinGroups];
     uint32_t colour_start[kMaxColours + 1];
     uint32_t colour_split[kMaxColours];  // first SNH tet of each colour
@@ -118,10 +124,10 @@ cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st);
 cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
                                     cudaStream_t st);
 cudaError_t persistent_occupancy(int block, int* ctas_per_sm);
-// Wavefront variant of the frame kernel: every CTA owns the contiguous slice
-// [start + b n / G, start + (b + 1) n / G) of each colour and, instead of a
-// grid barrier per colour, waits until the CTAs it shares vertices with have
-// finished the previous colour.  Needs s.prog zeroed before the launch.
+// Wavefront variant of the frame kernel: every CTA owns the tets of one
+// region of the mesh (s.wave_start / s.wave_idx) in every colour and, instead
+// of a grid barrier per colour, waits until the CTAs it shares vertices with
+// have finished the previous colour.  Needs s.prog zeroed before the launch.
 cudaError_t wavefront_occupancy(int block, int* ctas_per_sm);
 cudaError_t launch_wavefront_frame(const SceneDev& s, const StepParams& p, int block, int grid, cudaStream_t st);
 cudaError_t launch_set_error(int* err, int code, cudaStream_t st);

@@ -166,16 +166,34 @@ __device__ __forceinline__ void finalize_vertex(const SceneDev& s, const StepPar
     s.xn[i] = a;
 }
 
-// Ground contact detection for item k of (planes x surface vertices):
-// bvh_model.cpp:72-94 with the plane SDF of sdf_model.cpp:52-64.
+// Environment contact detection for item k of (environment slots x surface
+// vertices): bvh_model.cpp:72-94 - a surface vertex with signed distance
+// sd < 0 gets the contact n = normalised gradient, q = p + |sd| n - with the
+// plane SDF of sdf_model.cpp:52-64 or a signed-distance grid.
 __device__ __forceinline__ void detect_item(const SceneDev& s, const StepParams& p, uint32_t k) {
     const uint32_t plane = k / s.n_surf;
     const uint32_t vi = s.surf[k - plane * s.n_surf];
     const float4 x = s.xn[vi];
-    const Plane pl = p.planes[plane];
-    const float sd = pl.nx * x.x + pl.ny * x.y + pl.nz * x.z + pl.d;
-    const bool hit = sd < 0.0f;
-    const unsigned mask = __ballot_sync(__activemask(), hit);
+    float sd = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    bool hit;
+    if ((int)plane < p.n_analytic) {
+        const Plane pl = p.planes[plane];
+        sd = pl.nx * x.x + pl.ny * x.y + pl.nz * x.z + pl.d;
+        nx = pl.nx; ny = pl.ny; nz = pl.nz;
+        hit = sd < 0.0f;
+    } else {
+        float gx, gy, gz;
+        hit = sdf_eval(p.grids[plane - p.n_analytic], x.x, x.y, x.z, sd, gx, gy, gz) && sd < 0.0f;
+        if (hit) {
+            const float l = sqrtf(gx * gx + gy * gy + gz * gz);
+            hit = l > 0.0f;
+            if (hit) { nx = gx / l; ny = gy / l; nz = gz / l; }
+        }
+    }
+    // one atomic per (warp, slot): a warp may straddle two slots
+    const unsigned act = __activemask();
+    const unsigned same = __match_any_sync(act, plane);
+    const unsigned mask = __ballot_sync(act, hit) & same;
     if (!hit) return;
     const unsigned lane = threadIdx.x & 31u;
     const int leader = __ffs(mask) - 1;
@@ -186,8 +204,8 @@ __device__ __forceinline__ void detect_item(const SceneDev& s, const StepParams&
     if (base + rank >= s.n_surf) return;  // cannot happen with reset counters; never write past the segment
     const float ad = fabsf(sd);
     Contact c;
-    c.q = make_float4(x.x + pl.nx * ad, x.y + pl.ny * ad, x.z + pl.nz * ad, __uint_as_float(vi));
-    c.n = make_float4(pl.nx, pl.ny, pl.nz, 0.0f);
+    c.q = make_float4(x.x + nx * ad, x.y + ny * ad, x.z + nz * ad, __uint_as_float(vi));
+    c.n = make_float4(nx, ny, nz, 0.0f);
     s.contacts[(size_t)plane * s.n_surf + base + rank] = c;
 }
 
@@ -439,41 +457,44 @@ __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ unsigned ld_relaxed_u(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 // Wavefront wait: warp 0 polls the progress counters of this CTA's
-// neighbours until each has finished `need` colour phases (bounded by
-// kBarrierLimitNs, then SBS_ETIMEOUT); the CTA then passes a CTA barrier.
+// neighbours (relaxed loads, all of a lane's in flight at once) until each
+// has finished `need` colour phases, then one acquire fence; bounded by
+// kBarrierLimitNs (then SBS_ETIMEOUT).  The CTA then passes a CTA barrier.
 __device__ __forceinline__ bool wave_wait(const SceneDev& s, uint32_t need) {
     __shared__ int s_ok;
     if (threadIdx.x < 32) {
         int ok = 1;
         const uint32_t b = s.nb_start[blockIdx.x], e = s.nb_start[blockIdx.x + 1];
         const unsigned long long t0 = global_ns();
-        for (uint32_t k = b + threadIdx.x; k < e && ok; k += 32) {
-            const unsigned* c = s.prog + s.nb[k];
-            unsigned spins = 0;
-            while (ld_acquire(c) < need) {
-                if ((++spins & 63u) == 0) {
-                    if (ld_relaxed(s.err) != 0) { ok = 0; break; }
-                    if (global_ns() - t0 > kBarrierLimitNs) {
+        unsigned spins = 0;
+        for (;;) {
+            bool mine = true;
+            for (uint32_t k = b + threadIdx.x; k < e; k += 32) mine &= ld_relaxed_u(s.prog + s.nb[k]) >= need;
+            if (__all_sync(0xffffffffu, mine)) break;
+            if ((++spins & 15u) == 0) {
+                int stop = 0;
+                if (threadIdx.x == 0) {
+                    if (ld_relaxed(s.err) != 0) stop = 1;
+                    else if (global_ns() - t0 > kBarrierLimitNs) {
                         atomicCAS(s.err, 0, kErrTimeout);
-                        ok = 0;
-                        break;
+                        stop = 1;
                     }
                 }
+                if (__shfl_sync(0xffffffffu, stop, 0)) { ok = 0; break; }
             }
         }
-        ok = __all_sync(0xffffffffu, ok);
+        __threadfence();   // acquire: the neighbours' released writes are visible after this
         if (threadIdx.x == 0) s_ok = ok;
     }
     __syncthreads();
     return s_ok != 0;
-}
-
-// This CTA's slice of colour `col` in the wavefront mapping.
-__device__ __forceinline__ void wave_range(const StepParams& p, int col, uint32_t& b, uint32_t& e) {
-    const uint32_t c0 = p.colour_start[col], n = p.colour_start[col + 1] - c0;
-    b = c0 + (uint32_t)(((uint64_t)n * blockIdx.x) / gridDim.x);
-    e = c0 + (uint32_t)(((uint64_t)n * (blockIdx.x + 1)) / gridDim.x);
 }
 
 template <bool kWave>
@@ -521,14 +542,18 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
                 // every vertex-sharing tet of colours < c has finished, and
                 // before any of colours > c starts)
                 for (int col = 0; col < p.n_colours; ++col) {
-                    uint32_t b, e;
-                    wave_range(p, col, b, e);
-                    const uint32_t t0 = b + threadIdx.x;
+                    const uint32_t* ws = s.wave_start + (size_t)col * (gridDim.x + 1) + blockIdx.x;
+                    const uint32_t b = ws[0], e = ws[1];
+                    const uint32_t k0 = b + threadIdx.x;
+                    uint32_t t0 = 0;
                     TetRec r;
-                    if (t0 < e) r = load_tet(s, t0);
+                    if (k0 < e) {
+                        t0 = s.wave_idx[k0];
+                        r = load_tet(s, t0);
+                    }
                     if (!wave_wait(s, done)) return;
-                    if (t0 < e) project_tet_rec(s, p, t0, r, first);
-                    for (uint32_t u = t0 + blockDim.x; u < e; u += blockDim.x) project_tet(s, p, u, first);
+                    if (k0 < e) project_tet_rec(s, p, t0, r, first);
+                    for (uint32_t k = k0 + blockDim.x; k < e; k += blockDim.x) project_tet(s, p, s.wave_idx[k], first);
                     __syncthreads();
                     ++done;
                     if (threadIdx.x == 0) {

@@ -97,6 +97,14 @@ def load(build: bool = True):
         "sbs_gpu_get_contacts": [P, C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
         "sbs_gpu_get_masses": [P, f32],
         "sbs_gpu_get_surface": [P, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_set_body_velocity": [P, C.c_int32, f64],
+        "sbs_io_read_ply": [C.c_char_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_void_p, C.c_uint32,
+                            C.POINTER(C.c_uint32), C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_load_scene": [P, C.c_char_p, C.POINTER(Material), u32, C.c_double, C.POINTER(C.c_int32),
+                               C.POINTER(C.c_int32)],
+        "sbs_gpu_add_sdf_grid": [P, C.c_void_p, u32, f64, f64],
+        "sbs_gpu_add_environment_mesh": [P, f64, C.c_uint32, u32, C.c_uint32, f64, f64, u32],
+        "sbs_gpu_sdf_from_mesh": [f64, C.c_uint32, u32, C.c_uint32, f64, f64, u32, C.c_void_p],
         "sbs_gpu_add_distance_constraints": [P, C.c_void_p, C.c_uint32, C.c_double, C.c_double],
         "sbs_gpu_get_distance_order": [P, C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
         "sbs_gpu_get_distance_lambdas": [P, C.c_void_p],
@@ -158,6 +166,38 @@ def default_params(**kw) -> Params:
 
 def _ptr(a):
     return None if a is None else a.ctypes.data
+
+
+def read_ply(path):
+    """(positions float32 [V,3], triangles [F,3], tets [T,4]) of a PLY file."""
+    L = load()
+    nv, nf, nt = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    st = L.sbs_io_read_ply(str(path).encode(), None, 0, C.byref(nv), None, 0, C.byref(nf), None, 0, C.byref(nt))
+    if st != SBS_OK:
+        raise SbsError(st, f"cannot read {path}")
+    x = np.zeros((nv.value, 3), np.float32)
+    f = np.zeros((nf.value, 3), np.uint32)
+    t = np.zeros((nt.value, 4), np.uint32)
+    st = L.sbs_io_read_ply(str(path).encode(), x.ctypes.data, nv.value, C.byref(nv), f.ctypes.data, nf.value,
+                           C.byref(nf), t.ctypes.data, nt.value, C.byref(nt))
+    if st != SBS_OK:
+        raise SbsError(st, f"cannot read {path}")
+    return x, f, t
+
+
+def sdf_from_mesh(verts, tris, lo, hi, cells) -> np.ndarray:
+    """Host-only signed distance of a triangle mesh at the (cells+1) nodes per
+    axis of the box [lo, hi]; returns float32 [nz, ny, nx]."""
+    L = load()
+    v = np.ascontiguousarray(verts, np.float64).ravel()
+    t = np.ascontiguousarray(tris, np.uint32).ravel()
+    c = np.ascontiguousarray(cells, np.uint32)
+    out = np.zeros((int(c[2]) + 1) * (int(c[1]) + 1) * (int(c[0]) + 1), np.float32)
+    st = L.sbs_gpu_sdf_from_mesh(v, len(v) // 3, t, len(t) // 3, np.asarray(lo, np.float64),
+                                 np.asarray(hi, np.float64), c, out.ctypes.data)
+    if st != SBS_OK:
+        raise SbsError(st, "sbs_gpu_sdf_from_mesh failed")
+    return out.reshape(int(c[2]) + 1, int(c[1]) + 1, int(c[0]) + 1)
 
 
 def plan_sweep(scene):
@@ -229,6 +269,10 @@ class Solver:
         if scene.ground is not None:
             n, d = scene.ground
             self._check(L.sbs_gpu_add_ground_plane(h, np.asarray(n, np.float64), d))
+        for values, nodes, origin, spacing in getattr(scene, "sdf_grids", None) or []:
+            v = np.ascontiguousarray(values, np.float32).ravel()
+            self._check(L.sbs_gpu_add_sdf_grid(h, v.ctypes.data, np.ascontiguousarray(nodes, np.uint32),
+                                               np.asarray(origin, np.float64), np.asarray(spacing, np.float64)))
         self._check(L.sbs_gpu_finalize(h))
         if any(b.v_init is not None for b in scene.bodies):
             for i, b in enumerate(scene.bodies):

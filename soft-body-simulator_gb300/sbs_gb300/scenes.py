@@ -200,6 +200,9 @@ class Scene:
     distance_compliance: float = 0.0
     distance_damping: float = 0.0
     ground: tuple | None = ((0.0, 1.0, 0.0), 1.0)  # (n, d): n.x + d = 0
+    # signed-distance grids of environment bodies: (values [nz, ny, nx] float32,
+    # nodes (nx, ny, nz), origin, spacing)
+    sdf_grids: list | None = None
     body_contacts: bool = False
     hash_cell: float = 0.0
 

@@ -6,9 +6,14 @@ only fixtures the reference ships; element `tet` with `property list uchar int
 indices`, parsed as src/io/ply.cpp:616-640 does) and stores, per mesh:
   <name>_x0     rest positions (float64)
   <name>_tets   tets (uint32)
+  <name>_order  the Gauss-Seidel sweep order used (tet ids, colour-major, from
+                the library's host planner when the file was made),
+  <name>_offsets its colour offsets,
   <name>_x1     FP64 oracle positions after one frame of the golden scenario
-                (sweep order from the library's host planner), and
-  <name>_x10    after ten frames.
+                in that order, and
+  <name>_x10    after ten frames;
+and the reference's floor triangle mesh (data/meshes/xz_plane.ply, the
+environment of data/scenes/scene1.json) as xz_plane_verts / xz_plane_tris.
 Golden scenario: positions scaled by 0.1, vertices with minimal x pinned,
 StVK E 1e5 / nu 0.3 / rho 1000, compliance 1e-4, gravity -9.81 (acceleration),
 ground plane y = -0.05, dt 1/60, 1 substep, 10 iterations.
@@ -50,6 +55,29 @@ def read_ply_tets(path: Path):
     return x, np.array(tets, np.uint32)
 
 
+def read_ply_faces(path: Path):
+    """Vertices and triangle faces of an ascii PLY (element face, list uchar int)."""
+    lines = path.read_text().splitlines()
+    nv = nf = 0
+    i = 0
+    while lines[i].strip() != "end_header":
+        tok = lines[i].split()
+        if tok[:2] == ["element", "vertex"]:
+            nv = int(tok[2])
+        if tok[:2] == ["element", "face"]:
+            nf = int(tok[2])
+        i += 1
+    i += 1
+    x = np.array([[float(t) for t in lines[i + k].split()[:3]] for k in range(nv)])
+    i += nv
+    f = []
+    for k in range(nf):
+        tok = [int(t) for t in lines[i + k].split()]
+        assert tok[0] == 3
+        f.append(tok[1:4])
+    return x, np.array(f, np.uint32)
+
+
 def golden_scene(x0, tets):
     from sbs_gb300 import scenes
     x0 = x0 * 0.1
@@ -75,8 +103,13 @@ def main(meshdir: Path):
         o.step(9)
         out[f"{name}_x0"] = x0
         out[f"{name}_tets"] = tets
+        out[f"{name}_order"] = np.asarray(order, np.uint32)
+        out[f"{name}_offsets"] = np.asarray(off, np.uint32)
         out[f"{name}_x1"] = x1
         out[f"{name}_x10"] = o.get().copy()
+    fx, ff = read_ply_faces(meshdir / "xz_plane.ply")
+    out["xz_plane_verts"] = fx
+    out["xz_plane_tris"] = ff
     np.savez_compressed(HERE / "ref_meshes.npz", **out)
     print("wrote", HERE / "ref_meshes.npz")
 

@@ -77,9 +77,8 @@ def test_golden_fixtures_reproduce(oracle_mod):
     d = np.load(Path(__file__).parent / "golden" / "ref_meshes.npz")
     for name in NAMES:
         sc = golden_scene(d[f"{name}_x0"], d[f"{name}_tets"])
-        order, off = capi.plan_sweep(sc)
         o = oracle_mod.Oracle(sc)
-        o.set_order(order, off)
+        o.set_order(d[f"{name}_order"], d[f"{name}_offsets"])
         o.step(1)
         assert np.array_equal(o.get(), d[f"{name}_x1"])
         o.step(9)
