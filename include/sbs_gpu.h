@@ -356,6 +356,14 @@ sbs_status sbs_mlp_set_params(sbs_mlp* m, const float* params);
 sbs_status sbs_mlp_set_normalization(sbs_mlp* m, const float* in_mean, const float* in_std, const float* out_scale);
 /* Host buffers: x [n*16] raw features -> y [n*3] raw outputs. */
 sbs_status sbs_mlp_forward(sbs_mlp* m, const float* x, uint32_t n, float* y);
+/* As sbs_mlp_forward with the implementation chosen: 0 the fused tcgen05
+ * kernel (the default; weights resident in shared memory, accumulators in
+ * tensor memory), 1 the per-layer mma.sync GEMMs that training uses. */
+sbs_status sbs_mlp_forward_path(sbs_mlp* m, const float* x, uint32_t n, float* y, int32_t path);
+/* The same on device buffers of the network's device (x [n*16], y [n*3]);
+ * with ms != NULL the kernels' device time in milliseconds (CUDA events on
+ * the network's stream).  Returns when y is written. */
+sbs_status sbs_mlp_forward_device(sbs_mlp* m, const float* x, uint32_t n, float* y, int32_t path, float* ms);
 /* Host buffers: loss = mean over rows of ||(y - t) / out_scale||^2 and its
  * gradient w.r.t. all parameters (for gradient checks). */
 sbs_status sbs_mlp_loss_grad(sbs_mlp* m, const float* x, const float* t, uint32_t n, float* loss, float* grad);

@@ -2056,7 +2056,8 @@ sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps) {
 static sbs_status enqueue_warm_init(sbs_gpu* h, const StepParams& p) {
     CU(h, launch_features(h->d, h->wd, p, h->xpred_valid ? 1 : 0, h->st));
     h->xpred_valid = true;
-    CU(h, mlp_forward_dev(h->mlp->d, h->wd.feat, (int)h->n_verts, h->wd.delta, h->st));
+    CU(h, mlp_infer_tc(h->mlp->d, h->wd.feat, (int)h->n_verts, h->wd.delta, h->d.err, (int)SBS_ETIMEOUT, h->n_sm,
+                       h->st));
     for (uint32_t k = 0; k < h->fit_sweeps; ++k)
         for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c)
             CU(h, launch_fit_segment(h->d, h->wd, p, h->colour_offsets[c], h->colour_offsets[c + 1], k == 0 ? 1 : 0,

@@ -120,6 +120,9 @@ sbs_status sbs_mlp_create(int32_t device, uint64_t seed, sbs_mlp** out) {
     A((void**)&d.inv_std, kIn * sizeof(float));
     A((void**)&d.out_scale, kOut * sizeof(float));
     A((void**)&d.loss, sizeof(float));
+    A((void**)&d.tc_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d.tc_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&d.n_sm, cudaDevAttrMultiProcessorCount, d.device);
     if (e == cudaSuccess) e = cudaMemcpy(d.w, w.data(), kParams * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(d.m1, 0, kParams * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(d.m2, 0, kParams * sizeof(float));
@@ -191,18 +194,56 @@ sbs_status sbs_mlp_set_normalization(sbs_mlp* m, const float* in_mean, const flo
 }
 
 sbs_status sbs_mlp_forward(sbs_mlp* m, const float* x, uint32_t n, float* y) {
-    if (!m || !x || !y || n == 0 || n > (1u << 26)) return SBS_EINVAL;
+    return sbs_mlp_forward_path(m, x, n, y, 0);
+}
+
+sbs_status sbs_mlp_forward_path(sbs_mlp* m, const float* x, uint32_t n, float* y, int32_t path) {
+    if (!m || !x || !y || n == 0 || n > (1u << 26) || (path != 0 && path != 1)) return SBS_EINVAL;
     MCU(m, cudaSetDevice(m->d.device));
     float *dx = nullptr, *dy = nullptr;
     MCU(m, cudaMalloc((void**)&dx, (size_t)n * kIn * sizeof(float)));
     cudaError_t e = cudaMalloc((void**)&dy, (size_t)n * kOut * sizeof(float));
     if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice, m->st);
-    if (e == cudaSuccess) e = mlp_forward_dev(m->d, dx, (int)n, dy, m->st);
+    if (e == cudaSuccess)
+        e = path == 0 ? mlp_infer_tc(m->d, dx, (int)n, dy, m->d.tc_err, 3, m->d.n_sm, m->st)
+                      : mlp_forward_dev(m->d, dx, (int)n, dy, m->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, (size_t)n * kOut * sizeof(float), cudaMemcpyDeviceToHost, m->st);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, m->d.tc_err, sizeof(int), cudaMemcpyDeviceToHost, m->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->st);
     cudaFree(dx);
     if (dy) cudaFree(dy);
     if (e != cudaSuccess) return mfail(m, SBS_ECUDA, cudaGetErrorString(e));
+    if (flag) {
+        cudaMemsetAsync(m->d.tc_err, 0, sizeof(int), m->st);
+        return mfail(m, SBS_ETIMEOUT, "tensor-core inference: a wait timed out");
+    }
+    return SBS_OK;
+}
+
+sbs_status sbs_mlp_forward_device(sbs_mlp* m, const float* x, uint32_t n, float* y, int32_t path, float* ms) {
+    if (!m || !x || !y || n == 0 || n > (1u << 26) || (path != 0 && path != 1)) return SBS_EINVAL;
+    MCU(m, cudaSetDevice(m->d.device));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ms) {
+        MCU(m, cudaEventCreate(&e0));
+        MCU(m, cudaEventCreate(&e1));
+        MCU(m, cudaEventRecord(e0, m->st));
+    }
+    cudaError_t e = path == 0 ? mlp_infer_tc(m->d, x, (int)n, y, m->d.tc_err, 3, m->d.n_sm, m->st)
+                              : mlp_forward_dev(m->d, x, (int)n, y, m->st);
+    if (e == cudaSuccess && ms) e = cudaEventRecord(e1, m->st);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, m->d.tc_err, sizeof(int), cudaMemcpyDeviceToHost, m->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->st);
+    if (e == cudaSuccess && ms) e = cudaEventElapsedTime(ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (e != cudaSuccess) return mfail(m, SBS_ECUDA, cudaGetErrorString(e));
+    if (flag) {
+        cudaMemsetAsync(m->d.tc_err, 0, sizeof(int), m->st);
+        return mfail(m, SBS_ETIMEOUT, "tensor-core inference: a wait timed out");
+    }
     return SBS_OK;
 }
 

@@ -45,10 +45,16 @@ struct MlpDev {
     float* data_x = nullptr;
     float* data_t = nullptr;
     uint32_t n_data = 0;
+    int* tc_err = nullptr;     // error flag of the fused inference kernel
+    int n_sm = 0;
 };
 
 cudaError_t mlp_reserve(MlpDev& d, int n);
 cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cudaStream_t st);
+// Inference only (no activations kept): the fused tcgen05 kernel of
+// mlp_tc.cu.  A wait that times out stores err_code into *err (if 0).
+cudaError_t mlp_infer_tc(const MlpDev& d, const float* x, int n, float* y, int* err, int err_code, int n_sm,
+                         cudaStream_t st);
 cudaError_t mlp_backward_dev(MlpDev& d, const float* x, const float* t, int n, cudaStream_t st);
 cudaError_t mlp_adam_dev(MlpDev& d, float lr, cudaStream_t st);
 cudaError_t mlp_sync_bf16(MlpDev& d, cudaStream_t st);

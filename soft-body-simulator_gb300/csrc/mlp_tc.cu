@@ -1,0 +1,290 @@
+// Fused inference of the warm-start MLP (16 -> 128 -> 128 -> 128 -> 3, SiLU)
+// on the 5th-generation tensor cores of sm_100-class GPUs.
+//
+// One CTA of 128 threads takes 128-row tiles (rows = vertices).  The four
+// weight matrices stay in shared memory for the CTA's lifetime, in the
+// canonical K-major layout without swizzle that tcgen05.mma reads through
+// shared-memory descriptors: core matrices of 8 rows x 16 bytes, element
+// (r, k) at (r / 8) * SBO + (k / 8) * LBO + (r % 8) * 16 + (k % 8) * 2 with
+// LBO = 128 B and SBO = (K / 8) * 128 B.  Per layer one elected thread issues
+// K / 16 MMAs (M = 128, N = 128 - or 16 for the 3-wide output, zero-padded -
+// K = 16 each, BF16 inputs, FP32 accumulators in tensor memory), commits
+// them to an mbarrier, and the four warps read the accumulators back with
+// tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = rows of the tile), add the
+// bias, apply SiLU, round to BF16 and write the next layer's A operand.
+// Waits on the mbarrier are bounded in time; on expiry the kernel records an
+// error, frees its tensor memory and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "launch_count.cuh"
+#include "mlp_internal.cuh"
+
+namespace sbs {
+
+namespace {
+
+constexpr int kTileRows = 128;                    // UMMA M
+constexpr int kOutPad = 16;                       // layer-4 N, padded
+constexpr uint32_t kTmemCols = 128;               // accumulator columns
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
+// shared memory carve-up (bytes, 1024-aligned pieces)
+constexpr uint32_t kW1 = 0;                                   // 128 x 16
+constexpr uint32_t kW2 = kW1 + kHid * kIn * 2;                // 128 x 128
+constexpr uint32_t kW3 = kW2 + kHid * kHid * 2;               // 128 x 128
+constexpr uint32_t kW4 = kW3 + kHid * kHid * 2;               // 16 x 128
+constexpr uint32_t kA1 = kW4 + kOutPad * kHid * 2;            // 128 x 16
+constexpr uint32_t kAct = kA1 + kTileRows * kIn * 2;          // 128 x 128
+constexpr uint32_t kSmemBytes = kAct + kTileRows * kHid * 2;  // 110,592
+
+struct TcArgs {
+    const float* x;            // [n][16] raw features
+    int n;
+    const float* mean;         // [16]
+    const float* inv_std;      // [16]
+    const __nv_bfloat16* w[4]; // row-major [out][in]
+    const float* b[4];
+    const float* out_scale;    // [3]
+    float* y;                  // [n][3]
+    int* err;                  // set to err_code on a wait that timed out
+    int err_code;
+};
+
+__device__ __forceinline__ uint32_t canon(uint32_t r, uint32_t k, uint32_t K) {
+    return (r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t K) {
+    const uint64_t lbo = 128, sbo = (uint64_t)(K / 8) * 128;
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46);
+}
+
+__host__ __device__ constexpr uint32_t instr_desc(uint32_t N) {
+    // D f32 (bits 4-5 = 1), A bf16 (7-9 = 1), B bf16 (10-12 = 1), both
+    // K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((uint32_t)(kTileRows >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+// bounded wait for the mbarrier phase `parity` to complete
+__device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity) {
+    const unsigned long long t0 = now_ns();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (now_ns() - t0 > kWaitLimitNs) return false;
+    }
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 32 consecutive accumulator columns of this thread's row
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + __expf(-z)); }
+
+// accumulators + bias -> SiLU -> BF16 into the next layer's A operand
+__device__ __forceinline__ void hidden_epilogue(uint32_t tmem_row, const float* bias, uint8_t* act) {
+    const uint32_t r = threadIdx.x;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kHid; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem_row + (uint32_t)c0, v);
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) h[j] = __float2bfloat16(silu_f(v[g * 8 + j] + __ldg(&bias[c0 + g * 8 + j])));
+            *reinterpret_cast<uint4*>(act + canon(r, (uint32_t)(c0 + g * 8), kHid)) =
+                *reinterpret_cast<const uint4*>(h);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(TcArgs a) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_fail;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+
+    // weights -> canonical layouts (W4 zero-padded to 16 rows)
+    for (uint32_t i = tid; i < (uint32_t)(kHid * kIn); i += blockDim.x) {
+        const uint32_t r = i / kIn, k = i % kIn;
+        *reinterpret_cast<__nv_bfloat16*>(sm + kW1 + canon(r, k, kIn)) = a.w[0][i];
+    }
+    for (uint32_t i = tid; i < (uint32_t)(kHid * kHid); i += blockDim.x) {
+        const uint32_t r = i / kHid, k = i % kHid;
+        *reinterpret_cast<__nv_bfloat16*>(sm + kW2 + canon(r, k, kHid)) = a.w[1][i];
+        *reinterpret_cast<__nv_bfloat16*>(sm + kW3 + canon(r, k, kHid)) = a.w[2][i];
+    }
+    for (uint32_t i = tid; i < (uint32_t)(kOutPad * kHid); i += blockDim.x) {
+        const uint32_t r = i / kHid, k = i % kHid;
+        *reinterpret_cast<__nv_bfloat16*>(sm + kW4 + canon(r, k, kHid)) =
+            r < (uint32_t)kOut ? a.w[3][r * kHid + k] : __float2bfloat16(0.0f);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t tmem_row = tmem + ((warp * 32u) << 16);   // this warp's 32 lanes
+    const uint32_t mb = smem_u32(&mbar);
+    const uint32_t base = smem_u32(sm);
+    uint32_t parity = 0;
+    const int tiles = (a.n + kTileRows - 1) / kTileRows;
+
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int row = tile * kTileRows + (int)tid;
+        const bool valid = row < a.n;
+        // layer-1 A operand: normalised features
+        {
+            __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+            for (int k = 0; k < kIn; ++k) {
+                const float f = valid ? (__ldg(&a.x[(size_t)row * kIn + k]) - __ldg(&a.mean[k])) * __ldg(&a.inv_std[k])
+                                      : 0.0f;
+                h[k] = __float2bfloat16(f);
+            }
+            *reinterpret_cast<uint4*>(sm + kA1 + canon(tid, 0, kIn)) = *reinterpret_cast<const uint4*>(&h[0]);
+            *reinterpret_cast<uint4*>(sm + kA1 + canon(tid, 8, kIn)) = *reinterpret_cast<const uint4*>(&h[8]);
+        }
+        for (int layer = 0; layer < 4; ++layer) {
+            const uint32_t K = layer == 0 ? kIn : kHid;
+            const uint32_t aop = base + (layer == 0 ? kA1 : kAct);
+            const uint32_t bop = base + (layer == 0 ? kW1 : layer == 1 ? kW2 : layer == 2 ? kW3 : kW4);
+            const uint32_t idesc = instr_desc(layer == 3 ? kOutPad : kHid);
+            fence_async_smem();
+            fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                fence_after();
+                for (uint32_t s = 0; s < K / 16; ++s)
+                    mma(tmem, smem_desc(aop + 256 * s, K), smem_desc(bop + 256 * s, K), idesc, s > 0 ? 1u : 0u);
+                commit(mb);
+            }
+            const bool ok = wait_phase(mb, parity);
+            parity ^= 1u;
+            if (!ok) s_fail = 1;
+            __syncthreads();
+            if (s_fail) break;
+            fence_after();
+            if (layer < 3) {
+                hidden_epilogue(tmem_row, a.b[layer], sm + kAct);
+            } else {
+                float v[16];
+                tmem_ld16(tmem_row, v);
+                if (valid)
+                    for (int j = 0; j < kOut; ++j)
+                        a.y[(size_t)row * kOut + j] = (v[j] + __ldg(&a.b[3][j])) * __ldg(&a.out_scale[j]);
+            }
+        }
+        if (s_fail) break;
+    }
+    if (s_fail && tid == 0) atomicCAS(a.err, 0, a.err_code);
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+}  // namespace
+
+cudaError_t mlp_infer_tc(const MlpDev& d, const float* x, int n, float* y, int* err, int err_code, int n_sm,
+                         cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    TcArgs a;
+    a.x = x;
+    a.n = n;
+    a.mean = d.mean;
+    a.inv_std = d.inv_std;
+    for (int l = 0; l < 4; ++l) {
+        a.w[l] = d.wb[l];
+        a.b[l] = d.b[l];
+    }
+    a.out_scale = d.out_scale;
+    a.y = y;
+    a.err = err;
+    a.err_code = err_code;
+    const int tiles = (n + kTileRows - 1) / kTileRows;
+    const int grid = tiles < 2 * n_sm ? tiles : 2 * n_sm;
+    k_mlp_infer_tc<<<grid, 128, kSmemBytes, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace sbs

@@ -133,6 +133,8 @@ def load(build: bool = True):
         "sbs_mlp_set_params": [P, f32p],
         "sbs_mlp_set_normalization": [P, f32p, f32p, f32p],
         "sbs_mlp_forward": [P, f32p, C.c_uint32, f32p],
+        "sbs_mlp_forward_path": [P, f32p, C.c_uint32, f32p, C.c_int32],
+        "sbs_mlp_forward_device": [P, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32, C.POINTER(C.c_float)],
         "sbs_mlp_loss_grad": [P, f32p, f32p, C.c_uint32, C.POINTER(C.c_float), C.c_void_p],
         "sbs_mlp_set_dataset": [P, f32p, f32p, C.c_uint32],
         "sbs_mlp_train": [P, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64, C.POINTER(C.c_float)],
@@ -510,11 +512,19 @@ class Mlp:
             self.h, np.ascontiguousarray(mean, np.float32), np.ascontiguousarray(std, np.float32),
             np.ascontiguousarray(scale, np.float32)))
 
-    def forward(self, x) -> np.ndarray:
+    def forward(self, x, path: int = 0) -> np.ndarray:
+        """Network output for rows x; path 0 = fused tcgen05 kernel, 1 = per-layer GEMMs."""
         x = np.ascontiguousarray(x, np.float32)
         y = np.zeros((len(x), 3), np.float32)
-        self._check(self.L.sbs_mlp_forward(self.h, x.ravel(), len(x), y.ravel()))
+        self._check(self.L.sbs_mlp_forward_path(self.h, x.ravel(), len(x), y.ravel(), path))
         return y
+
+    def forward_device(self, x_ptr: int, n: int, y_ptr: int, path: int = 0) -> float:
+        """Forward on device buffers (pointers of the network's device);
+        returns the kernels' device time in ms."""
+        ms = C.c_float()
+        self._check(self.L.sbs_mlp_forward_device(self.h, x_ptr, n, y_ptr, path, C.byref(ms)))
+        return ms.value
 
     def loss_grad(self, x, t):
         x = np.ascontiguousarray(x, np.float32)

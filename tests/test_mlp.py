@@ -62,6 +62,26 @@ def test_gpu_forward_and_gradients_match_fp64(capi_mod):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 4096, 300001])
+def test_tcgen05_inference_matches_fp64_and_gemm_path(capi_mod, n):
+    """The fused tcgen05 kernel (path 0) against the FP64 network and the
+    per-layer mma.sync path (path 1): same BF16 rounding points, so the two
+    GPU paths agree to FP32 accumulation-order noise; ragged last tiles."""
+    m = capi_mod.Mlp(seed=9)
+    x, t = data(n, seed=11)
+    mean, std, scale = norm_of(x, t) if n > 1 else (np.zeros(16), np.ones(16), np.ones(3))
+    m.set_normalization(mean, std, scale)
+    p = m.params().astype(np.float64)
+    y_tc = m.forward(x, path=0)
+    y_mm = m.forward(x, path=1)
+    assert np.isfinite(y_tc).all()
+    k = min(n, 4096)
+    y_ref = mlp_oracle.forward(p, x[:k], mean, std, scale)
+    assert np.linalg.norm(y_tc[:k] - y_ref) <= 3e-2 * np.linalg.norm(y_ref) + 1e-6
+    assert np.abs(y_tc - y_mm).max() <= 2e-2 * np.abs(y_mm).max() + 1e-6
+
+
+@pytest.mark.gpu
 def test_gpu_adam_training_reduces_loss(capi_mod):
     m = capi_mod.Mlp(seed=4)
     x, t = data(50000, seed=5)
