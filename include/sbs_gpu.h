@@ -101,6 +101,7 @@ typedef struct sbs_gpu_stats {
     double last_frame_ms;     /* device time of the last timed frame (sbs_gpu_step_timed) */
     uint64_t kernel_launches; /* kernels run by sbs_gpu_step / step_timed since finalize
                                  (counted by the host as it enqueues them or their graph) */
+    uint32_t cluster_phase_max_tets; /* cluster mode: most tets one CTA projects in one colour */
 } sbs_gpu_stats;
 
 typedef struct sbs_gpu sbs_gpu;

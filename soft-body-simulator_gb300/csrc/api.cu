@@ -95,6 +95,7 @@ struct sbs_gpu {
     int pers_block = 256, pers_grid = 0;
     int wave_grid = 0;                 // CTAs of the wavefront mode (0: unavailable)
     uint32_t wave_max_nb = 0;          // largest neighbour list
+    uint32_t cl_phase_max = 0;         // cluster mode: most tets one CTA projects in one colour
     bool tuned = false;
     bool contacts_live = false;
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -1007,6 +1008,7 @@ plan_again:
         for (const GroupDesc& g : gdesc) slice = std::max(slice, (g.nv + C - 1) / C);
         h->cl_slice = slice;
         h->cl_lcap = 1;
+        h->cl_phase_max = 0;
         std::vector<uint32_t> tmp;
         for (GroupDesc& g : gdesc) {
             const uint32_t crs_base = (uint32_t)crs.size(), lb_base = (uint32_t)lbs.size();
@@ -1030,6 +1032,7 @@ plan_again:
                     crs.push_back(k);
                     lbs.push_back(owned[rr]);
                     owned[rr] += (uint32_t)by[rr].size();
+                    h->cl_phase_max = std::max(h->cl_phase_max, (uint32_t)by[rr].size());
                     for (uint32_t t : by[rr]) h->tet_order[k++] = t;
                 }
             }
@@ -2224,6 +2227,7 @@ sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st) {
     st->energy = h->energy;
     st->last_frame_ms = h->last_frame_ms;
     st->kernel_launches = h->kernel_launches;
+    st->cluster_phase_max_tets = h->exec_mode == SBS_EXEC_CLUSTER ? h->cl_phase_max : 0;
     return check_err(h);
 }
 

@@ -1,8 +1,10 @@
 // Fused inference of the warm-start MLP (16 -> 128 -> 128 -> 128 -> 3, SiLU)
 // on the 5th-generation tensor cores of sm_100-class GPUs.
 //
-// One CTA of 128 threads takes 128-row tiles (rows = vertices).  The four
-// weight matrices stay in shared memory for the CTA's lifetime, in the
+// One CTA of four warpgroups per SM; each warpgroup takes 128-row tiles
+// (rows = vertices) on its own, so one warpgroup's epilogue overlaps another's
+// MMAs.  The four weight matrices stay in shared memory for the CTA's
+// lifetime (shared by the warpgroups), in the
 // canonical K-major layout without swizzle that tcgen05.mma reads through
 // shared-memory descriptors: core matrices of 8 rows x 16 bytes, element
 // (r, k) at (r / 8) * SBO + (k / 8) * LBO + (r % 8) * 16 + (k % 8) * 2 with
@@ -27,16 +29,19 @@ namespace {
 
 constexpr int kTileRows = 128;                    // UMMA M
 constexpr int kOutPad = 16;                       // layer-4 N, padded
-constexpr uint32_t kTmemCols = 128;               // accumulator columns
+constexpr int kGroups = 4;                        // warpgroups per CTA
+constexpr uint32_t kTmemCols = 128;               // accumulator columns per warpgroup
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
 // shared memory carve-up (bytes, 1024-aligned pieces)
 constexpr uint32_t kW1 = 0;                                   // 128 x 16
 constexpr uint32_t kW2 = kW1 + kHid * kIn * 2;                // 128 x 128
 constexpr uint32_t kW3 = kW2 + kHid * kHid * 2;               // 128 x 128
 constexpr uint32_t kW4 = kW3 + kHid * kHid * 2;               // 16 x 128
-constexpr uint32_t kA1 = kW4 + kOutPad * kHid * 2;            // 128 x 16
+constexpr uint32_t kGroupBase = kW4 + kOutPad * kHid * 2;     // per-warpgroup operands from here
+constexpr uint32_t kA1 = 0;                                   // 128 x 16 (offset in a group's block)
 constexpr uint32_t kAct = kA1 + kTileRows * kIn * 2;          // 128 x 128
-constexpr uint32_t kSmemBytes = kAct + kTileRows * kHid * 2;  // 110,592
+constexpr uint32_t kGroupBytes = kAct + kTileRows * kHid * 2; // 36,864
+constexpr uint32_t kSmemBytes = kGroupBase + kGroups * kGroupBytes;  // 221,184
 
 struct TcArgs {
     const float* x;            // [n][16] raw features
@@ -136,11 +141,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU with the fast reciprocal: the result is rounded to BF16 next
+__device__ __forceinline__ float silu_f(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+
+__device__ __forceinline__ void group_sync(uint32_t g) {
+    asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(128) : "memory");
+}
 
 // accumulators + bias -> SiLU -> BF16 into the next layer's A operand
 __device__ __forceinline__ void hidden_epilogue(uint32_t tmem_row, const float* bias, uint8_t* act) {
-    const uint32_t r = threadIdx.x;
+    const uint32_t r = threadIdx.x & 127u;
 #pragma unroll 1
     for (int c0 = 0; c0 < kHid; c0 += 32) {
         float v[32];
@@ -156,52 +166,55 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem_row, const float* 
     }
 }
 
-__global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(TcArgs a) {
+__global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_infer_tc(TcArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[kGroups];
     __shared__ uint32_t tmem_slot;
-    __shared__ int s_fail;
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    __shared__ int s_fail[kGroups];
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, r = tid & 127u;
 
-    // weights -> canonical layouts (W4 zero-padded to 16 rows)
+    // weights -> canonical layouts (W4 zero-padded to 16 rows), all warpgroups
     for (uint32_t i = tid; i < (uint32_t)(kHid * kIn); i += blockDim.x) {
-        const uint32_t r = i / kIn, k = i % kIn;
-        *reinterpret_cast<__nv_bfloat16*>(sm + kW1 + canon(r, k, kIn)) = a.w[0][i];
+        const uint32_t rr = i / kIn, k = i % kIn;
+        *reinterpret_cast<__nv_bfloat16*>(sm + kW1 + canon(rr, k, kIn)) = a.w[0][i];
     }
     for (uint32_t i = tid; i < (uint32_t)(kHid * kHid); i += blockDim.x) {
-        const uint32_t r = i / kHid, k = i % kHid;
-        *reinterpret_cast<__nv_bfloat16*>(sm + kW2 + canon(r, k, kHid)) = a.w[1][i];
-        *reinterpret_cast<__nv_bfloat16*>(sm + kW3 + canon(r, k, kHid)) = a.w[2][i];
+        const uint32_t rr = i / kHid, k = i % kHid;
+        *reinterpret_cast<__nv_bfloat16*>(sm + kW2 + canon(rr, k, kHid)) = a.w[1][i];
+        *reinterpret_cast<__nv_bfloat16*>(sm + kW3 + canon(rr, k, kHid)) = a.w[2][i];
     }
     for (uint32_t i = tid; i < (uint32_t)(kOutPad * kHid); i += blockDim.x) {
-        const uint32_t r = i / kHid, k = i % kHid;
-        *reinterpret_cast<__nv_bfloat16*>(sm + kW4 + canon(r, k, kHid)) =
-            r < (uint32_t)kOut ? a.w[3][r * kHid + k] : __float2bfloat16(0.0f);
+        const uint32_t rr = i / kHid, k = i % kHid;
+        *reinterpret_cast<__nv_bfloat16*>(sm + kW4 + canon(rr, k, kHid)) =
+            rr < (uint32_t)kOut ? a.w[3][rr * kHid + k] : __float2bfloat16(0.0f);
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                     "r"(kTmemCols)
+                     "r"(kTmemCols * kGroups)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid == 0) {
-        s_fail = 0;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+    if (r == 0) {
+        s_fail[g] = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[g])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = tmem_slot;
-    const uint32_t tmem_row = tmem + ((warp * 32u) << 16);   // this warp's 32 lanes
-    const uint32_t mb = smem_u32(&mbar);
+    // this warpgroup's accumulator columns; warp w of a warpgroup reads TMEM lanes 32 (w % 4)...
+    const uint32_t tmem = tmem_slot + g * kTmemCols;
+    const uint32_t tmem_row = tmem + (((warp & 3u) * 32u) << 16);
+    const uint32_t mb = smem_u32(&mbar[g]);
     const uint32_t base = smem_u32(sm);
+    uint8_t* gsm = sm + kGroupBase + g * kGroupBytes;
+    const uint32_t gbase = base + kGroupBase + g * kGroupBytes;
     uint32_t parity = 0;
     const int tiles = (a.n + kTileRows - 1) / kTileRows;
 
-    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int row = tile * kTileRows + (int)tid;
+    for (int tile = blockIdx.x * kGroups + (int)g; tile < tiles; tile += gridDim.x * kGroups) {
+        const int row = tile * kTileRows + (int)r;
         const bool valid = row < a.n;
         // layer-1 A operand: normalised features
         {
@@ -212,18 +225,18 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(TcArgs a) {
                                       : 0.0f;
                 h[k] = __float2bfloat16(f);
             }
-            *reinterpret_cast<uint4*>(sm + kA1 + canon(tid, 0, kIn)) = *reinterpret_cast<const uint4*>(&h[0]);
-            *reinterpret_cast<uint4*>(sm + kA1 + canon(tid, 8, kIn)) = *reinterpret_cast<const uint4*>(&h[8]);
+            *reinterpret_cast<uint4*>(gsm + kA1 + canon(r, 0, kIn)) = *reinterpret_cast<const uint4*>(&h[0]);
+            *reinterpret_cast<uint4*>(gsm + kA1 + canon(r, 8, kIn)) = *reinterpret_cast<const uint4*>(&h[8]);
         }
         for (int layer = 0; layer < 4; ++layer) {
             const uint32_t K = layer == 0 ? kIn : kHid;
-            const uint32_t aop = base + (layer == 0 ? kA1 : kAct);
+            const uint32_t aop = gbase + (layer == 0 ? kA1 : kAct);
             const uint32_t bop = base + (layer == 0 ? kW1 : layer == 1 ? kW2 : layer == 2 ? kW3 : kW4);
             const uint32_t idesc = instr_desc(layer == 3 ? kOutPad : kHid);
             fence_async_smem();
             fence_before();
-            __syncthreads();
-            if (tid == 0) {
+            group_sync(g);
+            if (r == 0) {
                 fence_after();
                 for (uint32_t s = 0; s < K / 16; ++s)
                     mma(tmem, smem_desc(aop + 256 * s, K), smem_desc(bop + 256 * s, K), idesc, s > 0 ? 1u : 0u);
@@ -231,12 +244,12 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(TcArgs a) {
             }
             const bool ok = wait_phase(mb, parity);
             parity ^= 1u;
-            if (!ok) s_fail = 1;
-            __syncthreads();
-            if (s_fail) break;
+            if (!ok) s_fail[g] = 1;
+            group_sync(g);
+            if (s_fail[g]) break;
             fence_after();
             if (layer < 3) {
-                hidden_epilogue(tmem_row, a.b[layer], sm + kAct);
+                hidden_epilogue(tmem_row, a.b[layer], gsm + kAct);
             } else {
                 float v[16];
                 tmem_ld16(tmem_row, v);
@@ -245,14 +258,16 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(TcArgs a) {
                         a.y[(size_t)row * kOut + j] = (v[j] + __ldg(&a.b[3][j])) * __ldg(&a.out_scale[j]);
             }
         }
-        if (s_fail) break;
+        if (s_fail[g]) break;
     }
-    if (s_fail && tid == 0) atomicCAS(a.err, 0, a.err_code);
+    if (s_fail[g] && r == 0) atomicCAS(a.err, 0, a.err_code);
     fence_before();
     __syncthreads();
     if (warp == 0) {
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot),
+                     "r"(kTmemCols * kGroups)
+                     : "memory");
     }
 }
 
@@ -281,8 +296,10 @@ cudaError_t mlp_infer_tc(const MlpDev& d, const float* x, int n, float* y, int* 
     a.err = err;
     a.err_code = err_code;
     const int tiles = (n + kTileRows - 1) / kTileRows;
-    const int grid = tiles < 2 * n_sm ? tiles : 2 * n_sm;
-    k_mlp_infer_tc<<<grid, 128, kSmemBytes, st>>>(a);
+    const int per_cta = kGroups;
+    const int want = (tiles + per_cta - 1) / per_cta;
+    const int grid = want < n_sm ? want : n_sm;   // one CTA (4 warpgroups, 216 KB) per SM
+    k_mlp_infer_tc<<<grid, 128 * kGroups, kSmemBytes, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }

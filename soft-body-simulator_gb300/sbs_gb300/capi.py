@@ -48,7 +48,7 @@ class Stats(C.Structure):
                 ("n_body_contacts", C.c_uint32), ("body_contact_overflow", C.c_uint32),
                 ("exec_mode", C.c_int32), ("grid_ctas", C.c_int32), ("block_size", C.c_int32),
                 ("residual", C.c_double), ("energy", C.c_double), ("last_frame_ms", C.c_double),
-                ("kernel_launches", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("cluster_phase_max_tets", C.c_uint32)]
 
 
 _lib = None
