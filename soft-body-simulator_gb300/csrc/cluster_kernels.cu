@@ -167,6 +167,9 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
     uint32_t* clist = gidx + (size_t)slice * S;
     float* lam_s = reinterpret_cast<float*>(clist + slice);   // [2 * lcap] multipliers of this CTA's tets
     __shared__ uint32_t s_ncont;
+    // this CTA's tet range and multiplier base per colour of the current
+    // group, kept on chip: they head every colour phase's dependency chain
+    __shared__ uint32_t s_cb[kMaxColours], s_ce[kMaxColours], s_lb[kMaxColours];
     const uint32_t xi_base = smem_addr(xi);
 
     for (uint32_t g = cl_id(); g < c.n_groups; g += cl_count()) {
@@ -175,6 +178,12 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
         const uint32_t own1 = min(gd.v0 + (rank + 1) * slice, gd.v0 + gd.nv);
         const uint32_t nown = own1 > own0 ? own1 - own0 : 0;
         if (threadIdx.x == 0) s_ncont = 0;
+        for (uint32_t col = threadIdx.x; col < gd.n_col; col += blockDim.x) {
+            const uint32_t k = gd.col_base + col * C + rank;
+            s_cb[col] = c.col_start[k];
+            s_ce[col] = c.col_start[k + 1];
+            s_lb[col] = c.lam_base[gd.lb_base + col * C + rank];
+        }
         __syncthreads();
         // load own slice; ground contacts of own surface vertices from the
         // frame-start positions (bvh_model.cpp:72-94 with the plane SDF)
@@ -260,11 +269,6 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
             for (int it = 0; it < p.iterations; ++it) {
                 const bool first = it == 0;
                 // this CTA's tets of colour `col`: those owning most of their vertices here
-                auto col_range = [&](uint32_t col, uint32_t& b, uint32_t& e) {
-                    const uint32_t k = gd.col_base + col * C + rank;
-                    b = c.col_start[k];
-                    e = c.col_start[k + 1];
-                };
                 // contacts: own vertices only (collision_constraint.cpp:21-41)
                 for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
                     const uint32_t i = clist[k];
@@ -295,9 +299,8 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                 }
                 if (S > 0) cluster_sync();  // cluster-uniform condition
                 for (uint32_t col = 0; col < gd.n_col; ++col) {
-                    uint32_t b, e;
-                    col_range(col, b, e);
-                    float* lb = lam_s + c.lam_base[gd.lb_base + col * C + rank] - b;
+                    const uint32_t b = s_cb[col], e = s_ce[col];
+                    float* lb = lam_s + s_lb[col] - b;
                     for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
                         project_tet_dsmem(c, p, cl_load_tet(s, c, tt, xi_base), first, lb + tt, c.lcap);
                     cluster_sync();

@@ -71,6 +71,40 @@ def test_plan_sweep_rejects_bad_indices():
     assert L.sbs_gpu_plan_sweep(x0, 4, tets, 1, None, None, None, 0, C.byref(n)) == capi.SBS_EINVAL
 
 
+def test_plan_sweep_reports_colour_overflow():
+    """130 tets sharing one vertex need 130 colours; the planner allows 128."""
+    n = 130
+    ang = np.linspace(0, 2 * np.pi, n, endpoint=False)
+    x0 = [[0.0, 0.0, 0.0]]
+    tets = []
+    for i, a in enumerate(ang):
+        c, s_ = np.cos(a), np.sin(a)
+        base = len(x0)
+        x0 += [[c, s_, 0.0], [c * 1.1, s_ * 1.1, 0.1], [c, s_, 0.2]]
+        tets.append([0, base, base + 1, base + 2])
+    x0 = np.array(x0).ravel()
+    tets = np.array(tets, np.uint32).ravel()
+    L = capi.load()
+    cnt = C.c_uint32()
+    order = np.zeros(n, np.uint32)
+    off = np.zeros(129, np.uint32)
+    st = L.sbs_gpu_plan_sweep(x0, len(x0) // 3, tets, n, None, order.ctypes.data, off.ctypes.data, len(off),
+                              C.byref(cnt))
+    assert st == capi.SBS_ECOLOUR
+
+
+def test_plan_sweep_multibody_scene_is_valid():
+    sc = scenes.box_drop(n_bodies=12, min_cells=2, max_cells=6, arena=4.0)
+    order, off = capi.plan_sweep(sc)
+    t = np.concatenate([b.tets + o for b, o in zip(sc.bodies, np.cumsum([0] + [len(b.x0) for b in sc.bodies]))])
+    assert np.array_equal(np.sort(order), np.arange(len(t)))
+    for c in range(len(off) - 1):
+        v = t[order[off[c]:off[c + 1]]].ravel()
+        assert len(np.unique(v)) == len(v)
+    # 5-tet cubes: at most 32 tets meet at a vertex; the planner stays close
+    assert len(off) - 1 <= 40
+
+
 def test_golden_fixtures_reproduce(oracle_mod):
     from pathlib import Path
     from golden.make_golden import golden_scene, NAMES
