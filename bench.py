@@ -158,6 +158,24 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+def max_over_ranks(x: float, pg, device: int = 0) -> float:
+    """MAX of x over the ranks of the process group `pg` (the
+    torch.distributed module, or None for one process)."""
+    if pg is None:
+        return x
+    import torch
+    dev = f"cuda:{device}" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world: int, units_per_step: int, steps: int, seconds: float) -> float:
+    """Whole-job throughput: every rank runs its own replica of the workload
+    (weak scaling), timed by the slowest rank."""
+    return world * units_per_step * steps / seconds
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -189,6 +207,8 @@ def run_reference(args):
     from sbs_gb300 import capi
     # each step: one frame, or a bounded part of one for the large workloads
     sub, _, desc = bounded_sample(scene, 40_000_000)
+    if sub is scene:
+        desc = f"one frame of {scene.name}"
     per_step = sub.substeps * sub.iterations * sub.n_tets
     order, offsets = capi.plan_sweep(sub)
     o = oracle.Oracle(sub, threads=threads)
@@ -208,7 +228,7 @@ def run_reference(args):
         "config": {"workload": scene.name, "tets": scene.n_tets, "vertices": scene.n_verts,
                    "substeps": scene.substeps, "iterations": scene.iterations},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} steps, each {desc.replace('1 frame(s)', 'one frame')}, "
+                         "sample": f"{args.steps} steps, each {desc}, "
                                    f"colour-parallel sweep (bit-identical to the sequential reference order)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -273,13 +293,9 @@ def main():
     t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
     timed_launches = solver.stats().kernel_launches - launches0
-    total_ms = float(sum(frame_ms))
-    if pg:
-        t = torch.tensor([total_ms], device=f"cuda:{device}")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(sum(frame_ms)), pg, device)
     ms_per_frame = total_ms / args.steps
-    value = world * per_frame * args.steps / (total_ms * 1e-3)
+    value = job_throughput(world, per_frame, args.steps, total_ms * 1e-3)
 
     # end to end through the C ABI with host buffers
     x, v = solver.get_state(-1)   # the whole scene, every body
@@ -297,11 +313,7 @@ def main():
         xo, vo = solver.get_state(-1)
         hx[:] = xo.ravel()
         hv[:] = vo.ravel()
-    e2e_s = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([e2e_s], device=f"cuda:{device}")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, pg, device)
     V = scene.n_verts
     h2d = V * 16 * 3   # float4 staging: x -> xi and xn, v
     d2h = V * 16 * 2   # float4 staging: x, v
@@ -353,7 +365,7 @@ def main():
         "ms_per_frame": ms_per_frame,
         "frame_ms_samples": frame_ms,
         "wall_s": t_wall,
-        "e2e": {"value": world * per_frame * e2e_steps / e2e_s, "unit": UNIT,
+        "e2e": {"value": job_throughput(world, per_frame, e2e_steps, e2e_s), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * e2e_s / e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
