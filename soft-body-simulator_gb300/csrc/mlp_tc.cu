@@ -141,8 +141,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// SiLU with the fast reciprocal: the result is rounded to BF16 next
-__device__ __forceinline__ float silu_f(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+// SiLU as z * sigmoid(z) = z (1 + tanh(z / 2)) / 2 with the hardware tanh
+// approximation (tanh.approx.f32, relative error about 2^-11); the result is
+// rounded to BF16 (2^-8) next
+__device__ __forceinline__ float silu_f(float z) {
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+    return 0.5f * z * (1.0f + t);
+}
 
 __device__ __forceinline__ void group_sync(uint32_t g) {
     asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(128) : "memory");
@@ -276,12 +282,9 @@ __global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_infer_tc(TcArgs a) {
 cudaError_t mlp_infer_tc(const MlpDev& d, const float* x, int n, float* y, int* err, int err_code, int n_sm,
                          cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    // per device and cheap: set on every call (the caller may switch devices)
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+    if (e != cudaSuccess) return e;
     TcArgs a;
     a.x = x;
     a.n = n;
