@@ -56,6 +56,11 @@ __device__ __forceinline__ float4 ld_dsmem(uint32_t addr) {
                  : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr) : "memory");
     return v;
 }
+__device__ __forceinline__ uint32_t ld_dsmem_u32(uint32_t addr) {
+    uint32_t v;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
 __device__ __forceinline__ void st_dsmem(uint32_t addr, float4 v) {
     asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};"
                  :: "r"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w) : "memory");
@@ -167,6 +172,7 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
     uint32_t* clist = gidx + (size_t)slice * S;
     float* lam_s = reinterpret_cast<float*>(clist + slice);   // [2 * lcap] multipliers of this CTA's tets
     __shared__ uint32_t s_ncont;
+    __shared__ uint32_t s_any_contact;
     // this CTA's tet range and multiplier base per colour of the current
     // group, kept on chip: they head every colour phase's dependency chain
     __shared__ uint32_t s_cb[kMaxColours], s_ce[kMaxColours], s_lb[kMaxColours];
@@ -232,6 +238,16 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
         }
         cluster_sync();
         const uint32_t ncont = s_ncont;
+        // does any CTA of the cluster hold a contact this frame?  (the same
+        // answer everywhere, so the contact phase and its barrier are skipped
+        // cluster-wide when none does)
+        if (threadIdx.x == 0) {
+            uint32_t any = 0;
+            for (uint32_t r = 0; r < C; ++r) any |= ld_dsmem_u32(map_rank(smem_addr(&s_ncont), r));
+            s_any_contact = any;
+        }
+        __syncthreads();
+        const bool group_contacts = s_any_contact != 0;
         double t = t0;
         for (int sub = 0; sub < p.substeps; ++sub) {
             const double t_next = t + p.dt_d;
@@ -268,7 +284,6 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
             cluster_sync();
             for (int it = 0; it < p.iterations; ++it) {
                 const bool first = it == 0;
-                // this CTA's tets of colour `col`: those owning most of their vertices here
                 // contacts: own vertices only (collision_constraint.cpp:21-41)
                 for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
                     const uint32_t i = clist[k];
@@ -297,8 +312,9 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                     }
                     xi[i] = x;
                 }
-                if (S > 0) cluster_sync();  // cluster-uniform condition
+                if (S > 0 && group_contacts) cluster_sync();  // cluster-uniform condition
                 for (uint32_t col = 0; col < gd.n_col; ++col) {
+                    // this CTA's tets of the colour: those owning most of their vertices here
                     const uint32_t b = s_cb[col], e = s_ce[col];
                     float* lb = lam_s + s_lb[col] - b;
                     for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
