@@ -315,8 +315,8 @@ def main():
         hv[:] = vo.ravel()
     e2e_s = max_over_ranks(time.perf_counter() - t0, pg, device)
     V = scene.n_verts
-    h2d = V * 16 * 3   # float4 staging: x -> xi and xn, v
-    d2h = V * 16 * 2   # float4 staging: x, v
+    h2d = V * 12 * 2   # x and v, 3 floats per vertex (permuted on the device)
+    d2h = V * 12 * 2   # x and v
 
     if rank != 0:
         solver.close()

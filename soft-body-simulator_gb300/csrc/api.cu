@@ -87,8 +87,6 @@ struct sbs_gpu {
     uint32_t n_colours = 0, first_tail = 0;
     SceneDev d{};
     StepParams base{};
-    float4* h_stage = nullptr;           // pinned staging, n_verts float4
-    float4* h_stage2 = nullptr;
     int* d_err = nullptr;
     int exec_mode = SBS_EXEC_GRAPH;
     int block = 256, grid = 0;
@@ -102,6 +100,10 @@ struct sbs_gpu {
     std::map<GraphKey, uint64_t> graph_kernels;   // kernel nodes of each graph
     uint64_t kernel_launches = 0;                 // kernels run by frames since finalize
     BodyHost all_bodies;                          // the whole scene as one range (state transfer)
+    uint32_t* d_o2n = nullptr;                    // global input vertex id -> library slot
+    float* d_stage_x = nullptr;                   // [3V] transfer staging (positions)
+    float* d_stage_v = nullptr;                   // [3V] transfer staging (velocities)
+    int* d_bad = nullptr;                         // non-finite flag of a transfer
     // distance constraints: ends as global input vertex ids, parameters
     std::vector<uint32_t> dist_v;                 // 2 per constraint
     std::vector<float4> dist_p;                   // rest length, alpha, beta, 0
@@ -1279,8 +1281,11 @@ plan_again:
     CU(h, cudaMemsetAsync(d.time, 0, sizeof(double), h->st));
     CU(h, cudaMemsetAsync(d.err, 0, sizeof(int), h->st));
     CU(h, cudaMemsetAsync(d.bar, 0, 2 * sizeof(unsigned), h->st));
-    CU(h, cudaMallocHost((void**)&h->h_stage, V * sizeof(float4)));
-    CU(h, cudaMallocHost((void**)&h->h_stage2, V * sizeof(float4)));
+    if ((s = dalloc(h, &h->d_o2n, V)) != SBS_OK) return s;
+    if ((s = dalloc(h, &h->d_stage_x, 3ull * V)) != SBS_OK) return s;
+    if ((s = dalloc(h, &h->d_stage_v, 3ull * V)) != SBS_OK) return s;
+    if ((s = dalloc(h, &h->d_bad, 1)) != SBS_OK) return s;
+    if ((s = upload(h, h->d_o2n, old_to_new.data(), V * sizeof(uint32_t))) != SBS_OK) return s;
     // spatial hash for body-body contacts
     if (h->prm.body_contacts && d.n_surf > 0) {
         HashDev& hd = h->hd;
@@ -1808,83 +1813,77 @@ static sbs_status state_range(sbs_gpu* h, int32_t body, const BodyHost** b) {
     return SBS_OK;
 }
 
-static sbs_status read_field(sbs_gpu* h, int32_t body, const float4* dsrc, float* out, bool check) {
+// Device -> caller: gather in input order on the device, one copy back.
+static sbs_status read_fields(sbs_gpu* h, int32_t body, const float4* xsrc, float* xout, const float4* vsrc,
+                              float* vout) {
     const BodyHost* b;
     sbs_status s = state_range(h, body, &b);
     if (s) return s;
-    CU(h, cudaMemcpyAsync(h->h_stage, dsrc + b->v0, b->nv * sizeof(float4), cudaMemcpyDeviceToHost, h->st));
+    const size_t bytes = 3ull * b->nv * sizeof(float);
+    int bad = 0;
+    CU(h, cudaMemsetAsync(h->d_bad, 0, sizeof(int), h->st));
+    if (vout) {
+        CU(h, launch_gather_xyz(vsrc, h->d_o2n, b->v0, b->nv, h->d_stage_v, 0, h->d_bad, h->st));
+        CU(h, cudaMemcpyAsync(vout, h->d_stage_v, bytes, cudaMemcpyDeviceToHost, h->st));
+    }
+    if (xout) {
+        CU(h, launch_gather_xyz(xsrc, h->d_o2n, b->v0, b->nv, h->d_stage_x, 1, h->d_bad, h->st));
+        CU(h, cudaMemcpyAsync(xout, h->d_stage_x, bytes, cudaMemcpyDeviceToHost, h->st));
+    }
+    CU(h, cudaMemcpyAsync(&bad, h->d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CU(h, cudaStreamSynchronize(h->st));
     s = check_err(h);
     if (s) return s;
-    bool finite = true;
-    for (uint32_t o = 0; o < b->nv; ++o) {
-        const float4 q = h->h_stage[b->old_to_new[o]];
-        out[3ull * o] = q.x;
-        out[3ull * o + 1] = q.y;
-        out[3ull * o + 2] = q.z;
-        finite &= std::isfinite(q.x) && std::isfinite(q.y) && std::isfinite(q.z);
-    }
-    if (check && h->prm.check_finite && !finite) return fail(h, SBS_ENAN, "non-finite positions");
+    if (bad && h->prm.check_finite) return fail(h, SBS_ENAN, "non-finite positions");
     return SBS_OK;
 }
 
 sbs_status sbs_gpu_get_state(sbs_gpu* h, int32_t body, float* x, float* v) {
     if (!h) return SBS_EINVAL;
-    sbs_status s;
-    if (v && (s = read_field(h, body, h->d.v, v, false)) != SBS_OK) return s;
-    if (x && (s = read_field(h, body, h->d.xn, x, true)) != SBS_OK) return s;
-    return SBS_OK;
+    return read_fields(h, body, h->d.xn, x, h->d.v, v);
 }
 
 sbs_status sbs_gpu_get_predicted(sbs_gpu* h, int32_t body, float* xi) {
     if (!h || !xi) return fail(h, SBS_EINVAL, "null");
-    return read_field(h, body, h->d.xi, xi, true);
+    return read_fields(h, body, h->d.xi, xi, nullptr, nullptr);
 }
 
-static sbs_status write_positions(sbs_gpu* h, int32_t body, const float* x, bool all) {
+// Caller -> device: one copy in, checked for finite positions on the device,
+// scattered into the library's layout (.w of each record kept).
+static sbs_status write_fields(sbs_gpu* h, int32_t body, const float* x, bool both, const float* v) {
     const BodyHost* b;
     sbs_status s = state_range(h, body, &b);
     if (s) return s;
-    CU(h, cudaStreamSynchronize(h->st));  // staging buffer reuse
-    for (uint32_t o = 0; o < b->nv; ++o) {
-        if (!std::isfinite(x[3ull * o]) || !std::isfinite(x[3ull * o + 1]) || !std::isfinite(x[3ull * o + 2]))
-            return fail(h, SBS_EINVAL, "non-finite input position");
-        const uint32_t n = b->old_to_new[o];
-        h->h_stage[n] = make_float4(x[3ull * o], x[3ull * o + 1], x[3ull * o + 2], h->inv_mass[b->v0 + n]);
+    const size_t bytes = 3ull * b->nv * sizeof(float);
+    CU(h, cudaStreamSynchronize(h->st));   // staging reuse
+    if (x) {
+        int bad = 0;
+        CU(h, cudaMemcpyAsync(h->d_stage_x, x, bytes, cudaMemcpyHostToDevice, h->st));
+        CU(h, cudaMemsetAsync(h->d_bad, 0, sizeof(int), h->st));
+        CU(h, launch_check_finite(h->d_stage_x, 3ull * b->nv, h->d_bad, h->st));
+        CU(h, cudaMemcpyAsync(&bad, h->d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        CU(h, cudaStreamSynchronize(h->st));
+        if (bad) return fail(h, SBS_EINVAL, "non-finite input position");
+        CU(h, launch_scatter_xyz(h->d.xi, both ? h->d.xn : nullptr, h->d_o2n, b->v0, b->nv, h->d_stage_x, h->st));
     }
-    const size_t bytes = b->nv * sizeof(float4);
-    CU(h, cudaMemcpyAsync(h->d.xi + b->v0, h->h_stage, bytes, cudaMemcpyHostToDevice, h->st));
-    if (all) CU(h, cudaMemcpyAsync(h->d.xn + b->v0, h->h_stage, bytes, cudaMemcpyHostToDevice, h->st));
+    if (v) {
+        CU(h, cudaMemcpyAsync(h->d_stage_v, v, bytes, cudaMemcpyHostToDevice, h->st));
+        CU(h, launch_scatter_xyz(h->d.v, nullptr, h->d_o2n, b->v0, b->nv, h->d_stage_v, h->st));
+    }
+    CU(h, cudaStreamSynchronize(h->st));
     return SBS_OK;
 }
 
 sbs_status sbs_gpu_set_state(sbs_gpu* h, int32_t body, const float* x, const float* v) {
     if (!h) return SBS_EINVAL;
     h->xpred_valid = false;
-    sbs_status s;
-    if (x && (s = write_positions(h, body, x, true)) != SBS_OK) return s;
-    if (v) {
-        const BodyHost* b;
-        if ((s = state_range(h, body, &b)) != SBS_OK) return s;
-        for (uint32_t o = 0; o < b->nv; ++o) {
-            const uint32_t n = b->old_to_new[o];
-            float flag = 0.0f;
-            if (h->is_kin[b->v0 + n]) flag = (float)(1 + h->kin_group[b->v0 + o]);
-            h->h_stage2[n] = make_float4(v[3ull * o], v[3ull * o + 1], v[3ull * o + 2], flag);
-        }
-        CU(h, cudaMemcpyAsync(h->d.v + b->v0, h->h_stage2, b->nv * sizeof(float4), cudaMemcpyHostToDevice, h->st));
-    }
-    CU(h, cudaStreamSynchronize(h->st));
-    return SBS_OK;
+    return write_fields(h, body, x, true, v);
 }
 
 sbs_status sbs_gpu_set_predicted(sbs_gpu* h, int32_t body, const float* xi) {
     if (!h || !xi) return fail(h, SBS_EINVAL, "null");
     h->xpred_valid = false;
-    sbs_status s = write_positions(h, body, xi, false);
-    if (s) return s;
-    CU(h, cudaStreamSynchronize(h->st));
-    return SBS_OK;
+    return write_fields(h, body, xi, false, nullptr);
 }
 
 sbs_status sbs_gpu_get_tet_order(sbs_gpu* h, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
@@ -2237,8 +2236,6 @@ sbs_status sbs_gpu_destroy(sbs_gpu* h) {
     if (h->st) cudaStreamSynchronize(h->st);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     for (void* p : h->allocations) cudaFree(p);
-    if (h->h_stage) cudaFreeHost(h->h_stage);
-    if (h->h_stage2) cudaFreeHost(h->h_stage2);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->st) cudaStreamDestroy(h->st);

@@ -124,6 +124,13 @@ cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st);
 cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
                                     cudaStream_t st);
 cudaError_t persistent_occupancy(int block, int* ctas_per_sm);
+// State transfer (transfer_kernels.cu): o2n maps a global input vertex id to
+// its library slot.
+cudaError_t launch_gather_xyz(const float4* src, const uint32_t* o2n, uint32_t v0, uint32_t nv, float* out,
+                              int check, int* bad, cudaStream_t st);
+cudaError_t launch_check_finite(const float* in, uint64_t n, int* bad, cudaStream_t st);
+cudaError_t launch_scatter_xyz(float4* dst, float4* dst2, const uint32_t* o2n, uint32_t v0, uint32_t nv,
+                               const float* in, cudaStream_t st);
 // Wavefront variant of the frame kernel: every CTA owns the tets of one
 // region of the mesh (s.wave_start / s.wave_idx) in every colour and, instead
 // of a grid barrier per colour, waits until the CTAs it shares vertices with

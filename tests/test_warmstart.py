@@ -64,3 +64,29 @@ def test_warm_start_saves_sweeps(capi_mod):
     for r in res:
         if not r["fallback"]:
             assert r["r_end"] <= r["r_plain"]
+
+
+def test_warm_start_with_springs_and_grid_environment(capi_mod):
+    """The warm-start path runs distance constraints and grid contacts too."""
+    from sbs_gb300 import scenes
+    sc = scenes.hanging_block(alpha=1e-6)
+    lo = np.array([-1.0, -1.5, -1.0])
+    sp = np.array([0.25, 0.25, 0.25])
+    nodes = (9, 9, 9)
+    y = lo[1] + sp[1] * np.arange(nodes[1])
+    vals = np.broadcast_to((y + 0.3)[None, :, None], (nodes[2], nodes[1], nodes[0])).astype(np.float32).copy()
+    sc.ground = None
+    sc.sdf_grids = [(vals, nodes, lo, sp)]          # a floor at y = -0.3 under the hanging block
+    g = capi_mod.Solver(sc, exec_mode=1)
+    m = capi_mod.Mlp(device=0, seed=0)
+    m.set_params(np.zeros(m.n_params, np.float32))
+    g.set_warm_start(m, 2)
+    g.step(1)
+    assert g.stats().n_contacts > 0                   # the block starts 0.1 m into the floor
+    g.step(39)
+    x = g.positions()
+    assert np.isfinite(x).all()
+    offs = np.cumsum([0] + [len(b.x0) for b in sc.bodies])
+    assert x[offs[1]:, 1].min() > -0.35               # pushed out of the grid floor
+    g.set_warm_start(None)
+    g.close()
