@@ -179,19 +179,24 @@ __device__ __forceinline__ float stvk_dlambda(const TetEval& e, const float (&w)
 // deviatoric C_D = ||F||_F (compliance 1/(mu|V0|)) and hydrostatic
 // C_H = det F - (1 + mu/lam) (compliance 1/(lam|V0|)) constraints.
 // Computes the position deltas dx[i] (already weighted by w_i) and the two
-// multiplier increments.  Returns false when the step is skipped.
+// multiplier increments.  Returns false when the step is skipped.  1/|F| by
+// rsqrt and the other quotients by the fast reciprocal (a few ulp; the
+// one-sweep parity against the FP64 oracle is unchanged at ~1e-6 of the
+// scene diagonal): they sit on the per-phase latency chain, and the change
+// took 9% off a frame of the 98k-tet beam.
 __device__ __forceinline__ bool snh_step(f3 x0, f3 x1, f3 x2, f3 x3, f3 r0, f3 r1, f3 r2,
                                          float aV0, float mu, float lam, float inv_dt2,
                                          const float (&w)[4], float lamD, float lamH,
                                          f3 (&dx)[4], float& dlD, float& dlH) {
     const f3 d1 = x0 - x3, d2 = x1 - x3, d3 = x2 - x3;
     const m3 F = deformation(d1, d2, d3, r0, r1, r2);
-    const float cD = sqrtf(dot(F.c0, F.c0) + dot(F.c1, F.c1) + dot(F.c2, F.c2));
-    if (!(cD > 1e-12f)) return false;
+    const float cD2 = dot(F.c0, F.c0) + dot(F.c1, F.c1) + dot(F.c2, F.c2);
+    if (!(cD2 > 1e-24f)) return false;
+    const float icD = rsqrtf(cD2);
+    const float cD = cD2 * icD;
     const float J = det3(F);
-    const float cH = J - (1.0f + mu / lam);
-    const float atD = inv_dt2 / (mu * aV0), atH = inv_dt2 / (lam * aV0);
-    const float icD = 1.0f / cD;
+    const float cH = J - (1.0f + __fdividef(mu, lam));
+    const float atD = __fdividef(inv_dt2, mu * aV0), atH = __fdividef(inv_dt2, lam * aV0);
     // dC_D/dF = F / cD ; dC_H/dF = cof(F) = [f1 x f2 ... ] columns (f2 x f3, f3 x f1, f1 x f2)
     const f3 h0 = cross(F.c1, F.c2), h1 = cross(F.c2, F.c0), h2 = cross(F.c0, F.c1);
     // gradient wrt vertex j (j<3) = (dC/dF) r_j ; vertex 3 = -sum
@@ -214,7 +219,7 @@ __device__ __forceinline__ bool snh_step(f3 x0, f3 x1, f3 x2, f3 x3, f3 r0, f3 r
     const float b1 = -(cD + atD * lamD), b2 = -(cH + atH * lamH);
     const float det = a11 * a22 - a12 * a12;
     if (!(det > 1e-30f * a11 * a22)) return false;
-    const float idet = 1.0f / det;
+    const float idet = __fdividef(1.0f, det);
     dlD = (b1 * a22 - b2 * a12) * idet;
     dlH = (b2 * a11 - b1 * a12) * idet;
 #pragma unroll
