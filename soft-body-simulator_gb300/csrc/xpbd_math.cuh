@@ -96,13 +96,17 @@ __device__ __forceinline__ void svd3(const m3& F, f3 (&U)[3], float (&s)[3], f3 
     // B = F V
     auto mulF = [&](f3 v) { return F.c0 * v.x + F.c1 * v.y + F.c2 * v.z; };
     f3 b0 = mulF(V[0]), b1 = mulF(V[1]), b2 = mulF(V[2]);
-    float n0 = sqrtf(dot(b0, b0));
-    f3 u0 = n0 > 1e-30f ? b0 * (1.0f / n0) : mk(1.f, 0.f, 0.f);
+    const float q0 = dot(b0, b0);
+    const float i0 = q0 > 1e-36f ? rsqrtf(q0) : 0.0f;
+    float n0 = q0 * i0;
+    f3 u0 = q0 > 1e-36f ? b0 * i0 : mk(1.f, 0.f, 0.f);
     f3 b1p = b1 - u0 * dot(u0, b1);
-    float n1 = sqrtf(dot(b1p, b1p));
+    const float q1 = dot(b1p, b1p);
+    const float i1 = q1 > 1e-36f ? rsqrtf(q1) : 0.0f;
+    float n1 = q1 * i1;
     f3 u1;
-    if (n1 > 1e-7f * n0 && n1 > 1e-30f) {
-        u1 = b1p * (1.0f / n1);
+    if (n1 > 1e-7f * n0 && q1 > 1e-36f) {
+        u1 = b1p * i1;
     } else {
         f3 e = fabsf(u0.x) < 0.9f ? mk(1.f, 0.f, 0.f) : mk(0.f, 1.f, 0.f);
         f3 wv = e - u0 * dot(e, u0);
@@ -164,7 +168,8 @@ __device__ __forceinline__ void stvk_eval(f3 x0, f3 x1, f3 x2, f3 x3, f3 r0, f3 
 }
 
 // XPBD multiplier update of the StVK constraint (green_constraint.cpp:122-157).
-// Returns dlambda (0 when the weighted gradient norm is below 1e-20).
+// Returns dlambda (0 when the weighted gradient norm is below 1e-20); the
+// quotient by the fast reciprocal, as it ends the per-tet latency chain.
 __device__ __forceinline__ float stvk_dlambda(const TetEval& e, const float (&w)[4], float lam_acc,
                                               float alpha_tilde, float gamma, float gd) {
     const float S = w[0] * dot(e.g[0], e.g[0]) + w[1] * dot(e.g[1], e.g[1]) +
@@ -172,7 +177,7 @@ __device__ __forceinline__ float stvk_dlambda(const TetEval& e, const float (&w)
     if (S < 1e-20f) return 0.0f;
     const float num = -(e.C + alpha_tilde * lam_acc) + gamma * gd;
     const float den = (1.0f + gamma) * S + alpha_tilde;
-    return num / den;
+    return __fdividef(num, den);
 }
 
 // Stable Neo-Hookean (Macklin & Mueller 2021), coupled 2x2 solve of the
