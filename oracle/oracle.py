@@ -1,7 +1,8 @@
 """ctypes front end of the FP64 CPU oracle (oracle/xpbd_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
-baseline legs of bench.py as the checker.  The CUDA library never imports it.
+baseline legs of bench.py to check and time against.  The CUDA library never
+imports it.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 // FP64 CPU oracle for the XPBD substep loop.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library:
-// it is loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU
+// TEST INFRASTRUCTURE ONLY.  The CUDA library's results are checked against
+// it: it is loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU
 // baseline arm, never by the product path.
 //
 // It restates, in plain C++17 with no dependencies, the reference's
