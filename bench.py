@@ -244,6 +244,8 @@ def main():
     ap.add_argument("--workload", default="beam98k")
     ap.add_argument("--exec-mode", type=int, default=0)
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: the library's choice)")
+    ap.add_argument("--stage-records", type=int, default=1, choices=[0, 1],
+                    help="cluster mode: stage each colour's tet records in shared memory one phase ahead")
     ap.add_argument("--cpu-budget", type=int, default=25_000_000,
                     help="tet projections in the single-thread CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -265,7 +267,8 @@ def main():
 
     from sbs_gb300 import capi
     scene = workload(args.workload)
-    solver = capi.Solver(scene, device=device, exec_mode=args.exec_mode, block_size=args.block)
+    solver = capi.Solver(scene, device=device, exec_mode=args.exec_mode, block_size=args.block,
+                         stage_records=args.stage_records)
     per_frame = scene.substeps * scene.iterations * scene.n_tets
 
     for _ in range(max(3, args.warmup)):
@@ -358,6 +361,8 @@ def main():
                    "bodies": len(scene.bodies),
                    "exec_mode": ["auto", "graph", "persistent", "cluster", "wavefront"][st.exec_mode],
                    "grid_ctas": st.grid_ctas, "block": st.block_size, "colours": st.n_colours,
+                   **({"max_tets_per_cta_colour": st.cluster_phase_max_tets,
+                       "stage_records": args.stage_records} if st.exec_mode == capi.EXEC_CLUSTER else {}),
                    "l2": (f"flushed (256 MB write) before every timed frame; the "
                           f"{footprint / 2**20:.0f} MB solver state is "
                           + ("L2-resident within a frame" if resident else "larger than L2")),

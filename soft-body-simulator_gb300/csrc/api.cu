@@ -488,6 +488,7 @@ sbs_status sbs_gpu_params_default(sbs_gpu_params* p) {
     p->hash_cell = 0.0f;
     p->candidate_capacity = 0;
     p->check_finite = 1;
+    p->stage_records = 1;
     return SBS_OK;
 }
 
@@ -1361,6 +1362,20 @@ plan_again:
         c.xn_minus_xi = slice * 16u;
         c.n_groups = (uint32_t)gdesc.size();
         h->cl_smem = cluster_smem_bytes(slice, P, h->body_on ? 1 : 0, h->cl_lcap);
+        c.stage = 0;
+        if (h->prm.stage_records) {
+            // staging buffers for the largest (colour, CTA) tet set, when the
+            // cluster still launches with them
+            const size_t staged = cluster_smem_bytes(slice, P, h->body_on ? 1 : 0, h->cl_lcap, h->cl_phase_max);
+            const int blk = h->prm.block_size ? std::min(h->prm.block_size, kClusterMaxBlock) : 256;
+            int active = 0;
+            if (staged + 2048 <= (size_t)smem_optin && cluster_configure(blk, staged) == cudaSuccess &&
+                cluster_max_active(h->cl_size, blk, staged, &active) == cudaSuccess && active >= 1) {
+                c.stage = h->cl_phase_max;
+                h->cl_smem = staged;
+            }
+            cudaGetLastError();
+        }
         c.lcap = h->cl_lcap;
         c.body = h->body_on ? 1 : 0;
         c.bc_q = h->hd.bc_q;
@@ -1373,7 +1388,10 @@ plan_again:
             return ((local / slice) << 24) | (local % slice);
         };
         std::vector<uint4> tp(T);
-        for (uint32_t k = 0; k < T; ++k) tp[k] = make_uint4(pack(tid[k].x), pack(tid[k].y), pack(tid[k].z), pack(tid[k].w));
+        for (uint32_t k = 0; k < T; ++k) {
+            tp[k] = make_uint4(pack(tid[k].x), pack(tid[k].y), pack(tid[k].z), pack(tid[k].w));
+            if (h->tet_model[h->tet_order[k]] != SBS_MODEL_STVK) tp[k].x |= 0x80000000u;
+        }
         std::vector<uint8_t> vf(V, 0);
         for (uint32_t n : h->surf) vf[n] = 1;
         if ((s = dalloc(h, &c.tet_packed, T)) != SBS_OK) return s;

@@ -26,7 +26,10 @@ struct ClusterDev {
     uint32_t* col_start;
     uint32_t* lam_base;    // per group: n_col * C offsets into the CTA's multiplier array
     uint32_t lcap;         // multipliers per CTA (max tets owned by one CTA)
-    uint4* tet_packed;     // per tet slot: vertex as (cluster rank << 24) | slice offset
+    uint4* tet_packed;     // per tet slot: vertex as (cluster rank << 24) | slice offset;
+                           // bit 31 of .x set for a stable Neo-Hookean tet
+    uint32_t stage;        // tet records per staging buffer (most tets one CTA has in one
+                           // colour), 0: records are read from global memory in the phase
     uint8_t* vflags;       // per vertex: bit 0 = surface vertex
     uint32_t cluster_size;
     uint32_t slice;        // vertices per CTA slice
@@ -37,11 +40,14 @@ struct ClusterDev {
 };
 
 // Dynamic shared memory of one CTA for `slice` vertices, `planes` planes and
-// an optional body-contact slot: xi, xn, v, contact records and body normals
-// (float4), global contact slots and the contact vertex list (uint32).
-inline size_t cluster_smem_bytes(uint32_t slice, int planes, int body, uint32_t lcap) {
+// an optional body-contact slot: two staging buffers of `stage` tet records
+// (packed ids and the three DmInv rows, 64 bytes per tet), xi, xn, v, contact
+// records and body normals (float4), global contact slots and the contact
+// vertex list (uint32), the multipliers of the CTA's tets.
+inline size_t cluster_smem_bytes(uint32_t slice, int planes, int body, uint32_t lcap, uint32_t stage = 0) {
     const size_t S = (size_t)planes + (body ? 1 : 0);
-    return (size_t)slice * (3 * 16 + S * 16 + (body ? 16 : 0) + S * 4 + 4) + 2 * sizeof(float) * (size_t)lcap;
+    return 2 * 64 * (size_t)stage + (size_t)slice * (3 * 16 + S * 16 + (body ? 16 : 0) + S * 4 + 4) +
+           2 * sizeof(float) * (size_t)lcap;
 }
 
 cudaError_t cluster_configure(int block, size_t smem);

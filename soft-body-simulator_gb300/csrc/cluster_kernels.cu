@@ -68,31 +68,95 @@ __device__ __forceinline__ void st_dsmem(uint32_t addr, float4 v) {
 
 // Address of packed vertex (rank << 24 | local) in the cluster's xi slices.
 __device__ __forceinline__ uint32_t vaddr(uint32_t packed, uint32_t xi_base) {
-    return map_rank(xi_base + ((packed & 0xFFFFFFu) << 4), packed >> 24);
+    return map_rank(xi_base + ((packed & 0xFFFFFFu) << 4), (packed >> 24) & 0x7Fu);
 }
 
 // The read-only part of a tet's record: the DSMEM addresses of its corners'
-// xi and its rest data.  (Loading the next colour's record across the
-// cluster barrier was measured slower: 6.9 against 6.3 ms per frame of the
-// 98k-tet beam.)
+// xi and its rest data.  (Loading the next colour's record into registers
+// across the cluster barrier was measured slower: 6.9 against 6.3 ms per
+// frame of the 98k-tet beam; the records are staged in shared memory by
+// bulk copies instead, see k_cluster_frame.)
 struct ClTet {
     uint32_t a0, a1, a2, a3;
     float4 a, b, c;   // DmInv rows; w: V0, mu, lambda
     uint32_t snh;
 };
 
-__device__ __forceinline__ ClTet cl_load_tet(const SceneDev& s, const ClusterDev& c, uint32_t t, uint32_t xi_base) {
+__device__ __forceinline__ ClTet cl_make_tet(uint4 id, float4 a, float4 b, float4 c, uint32_t xi_base) {
     ClTet r;
-    const uint4 id = __ldg(&c.tet_packed[t]);
     r.a0 = vaddr(id.x, xi_base);
     r.a1 = vaddr(id.y, xi_base);
     r.a2 = vaddr(id.z, xi_base);
     r.a3 = vaddr(id.w, xi_base);
-    r.a = __ldg(&s.dm0[t]);
-    r.b = __ldg(&s.dm1[t]);
-    r.c = __ldg(&s.dm2[t]);
-    r.snh = s.model[t] != 0;
+    r.a = a;
+    r.b = b;
+    r.c = c;
+    r.snh = id.x >> 31;
     return r;
+}
+
+__device__ __forceinline__ ClTet cl_load_tet(const SceneDev& s, const ClusterDev& c, uint32_t t, uint32_t xi_base) {
+    return cl_make_tet(__ldg(&c.tet_packed[t]), __ldg(&s.dm0[t]), __ldg(&s.dm1[t]), __ldg(&s.dm2[t]), xi_base);
+}
+
+// ---- staging of tet records: bulk asynchronous copies (TMA) completing on an
+// mbarrier.  A copy is issued one colour phase ahead by one thread; the bulk
+// copy engine works outside the threads' memory order, so the release at the
+// cluster barrier does not wait for it.
+constexpr unsigned long long kStageLimitNs = 2000000000ull;   // 2 s
+constexpr int kErrTimeoutCl = 3;                              // SBS_ETIMEOUT
+
+__device__ __forceinline__ unsigned long long cl_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mb_init(uint32_t mb) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+}
+__device__ __forceinline__ void mb_arrive_tx(uint32_t mb, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mb_arrive(uint32_t mb) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mb) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mb) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(mb) : "memory");
+}
+// Bounded wait for phase `parity` of the mbarrier; false after kStageLimitNs.
+__device__ __forceinline__ bool mb_wait(uint32_t mb, uint32_t parity) {
+    unsigned long long t0 = 0;
+    for (uint32_t spins = 0;; ++spins) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mb), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (spins == 0) t0 = cl_ns();
+        else if ((spins & 15u) == 0 && cl_ns() - t0 > kStageLimitNs) return false;
+    }
+}
+
+// Stage the records of tets [b, e) (at most c.stage) into buffer `buf`:
+// packed ids, then the three DmInv rows, each an array of c.stage float4.
+// Elements are 16 bytes, so every source and destination is 16-byte aligned.
+__device__ __forceinline__ void stage_issue(const SceneDev& s, const ClusterDev& c, uint32_t b, uint32_t e,
+                                            uint32_t buf_addr, uint32_t mb) {
+    const uint32_t n = e - b;
+    if (n == 0) {
+        mb_arrive(mb);
+        return;
+    }
+    const uint32_t bytes = n * 16u, arr = c.stage * 16u;
+    mb_arrive_tx(mb, 4u * bytes);
+    bulk_g2s(buf_addr, c.tet_packed + b, bytes, mb);
+    bulk_g2s(buf_addr + arr, s.dm0 + b, bytes, mb);
+    bulk_g2s(buf_addr + 2u * arr, s.dm1 + b, bytes, mb);
+    bulk_g2s(buf_addr + 3u * arr, s.dm2 + b, bytes, mb);
 }
 
 // lam: this tet's multipliers in the CTA's shared memory (lam[0]; SNH's
@@ -152,7 +216,10 @@ __device__ __forceinline__ void project_tet_dsmem(const ClusterDev& c, const Ste
     }
 }
 
-// Shared memory per CTA: xi[slice], xn[slice], v[slice] (float4 each),
+// Shared memory per CTA: two staging buffers for the tet records of one
+// colour phase (4 * c.stage float4 each: packed ids, DmInv rows; filled one
+// phase ahead while the current phase projects), xi[slice], xn[slice],
+// v[slice] (float4 each),
 // contact records rec[slice * n_planes] (q.xyz, lambda; q.x = NaN when the
 // vertex has no contact with that plane), their slots in the global contact
 // list gidx[slice * n_planes], and the CTA's contact vertex list clist[slice].
@@ -162,11 +229,12 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
     const uint32_t rank = cl_rank();
     const uint32_t C = c.cluster_size;
     const uint32_t slice = c.slice;
-    float4* xi = sm;
-    float4* xn = sm + slice;
-    float4* vv = sm + 2 * slice;
+    const float4* stg = sm;                        // 2 staging buffers of 4 * c.stage float4
+    float4* xi = sm + 8 * (size_t)c.stage;
+    float4* xn = xi + slice;
+    float4* vv = xi + 2 * slice;
     const int S = p.n_planes + (c.body ? 1 : 0);   // contact slots per vertex: planes, then body
-    float4* rec = sm + 3 * slice;
+    float4* rec = xi + 3 * slice;
     float4* bn = rec + (size_t)slice * S;          // body contact normals (when c.body)
     uint32_t* gidx = reinterpret_cast<uint32_t*>(bn + (c.body ? slice : 0));
     uint32_t* clist = gidx + (size_t)slice * S;
@@ -176,7 +244,19 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
     // this CTA's tet range and multiplier base per colour of the current
     // group, kept on chip: they head every colour phase's dependency chain
     __shared__ uint32_t s_cb[kMaxColours], s_ce[kMaxColours], s_lb[kMaxColours];
+    __shared__ __align__(8) unsigned long long s_mb[2];   // one mbarrier per staging buffer
     const uint32_t xi_base = smem_addr(xi);
+    const uint32_t stg_base = smem_addr(stg), stg_bytes = c.stage * 64u, mb_base = smem_addr(s_mb);
+    // colour phases run so far (all groups): staging buffer ph & 1, whose
+    // mbarrier is then in its (ph >> 1)-th phase
+    uint32_t ph = 0;
+    bool stage_bad = false;   // a staging wait expired: this thread projects nothing more
+    if (c.stage && threadIdx.x == 0) {
+        mb_init(mb_base);
+        mb_init(mb_base + 8);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
 
     for (uint32_t g = cl_id(); g < c.n_groups; g += cl_count()) {
         const GroupDesc gd = c.groups[g];
@@ -191,6 +271,9 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
             s_lb[col] = c.lam_base[gd.lb_base + col * C + rank];
         }
         __syncthreads();
+        // the group's first colour phase: its records arrive while the slice loads
+        if (c.stage && threadIdx.x == 0 && gd.n_col > 0 && p.substeps > 0 && p.iterations > 0)
+            stage_issue(s, c, s_cb[0], s_ce[0], stg_base + (ph & 1u) * stg_bytes, mb_base + (ph & 1u) * 8u);
         // load own slice; ground contacts of own surface vertices from the
         // frame-start positions (bvh_model.cpp:72-94 with the plane SDF)
         for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
@@ -317,8 +400,36 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                     // this CTA's tets of the colour: those owning most of their vertices here
                     const uint32_t b = s_cb[col], e = s_ce[col];
                     float* lb = lam_s + s_lb[col] - b;
-                    for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
-                        project_tet_dsmem(c, p, cl_load_tet(s, c, tt, xi_base), first, lb + tt, c.lcap);
+                    if (c.stage) {
+                        const uint32_t buf = ph & 1u;
+                        if (threadIdx.x == 0 &&
+                            !(sub + 1 == p.substeps && it + 1 == p.iterations && col + 1 == gd.n_col)) {
+                            // next phase's records into the other buffer, whose
+                            // readers all passed the cluster barrier behind us
+                            const uint32_t nc = col + 1 == gd.n_col ? 0u : col + 1;
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            stage_issue(s, c, s_cb[nc], s_ce[nc], stg_base + (buf ^ 1u) * stg_bytes,
+                                        mb_base + (buf ^ 1u) * 8u);
+                        }
+                        if (b + threadIdx.x < e && !stage_bad) {
+                            if (mb_wait(mb_base + buf * 8u, (ph >> 1) & 1u)) {
+                                const float4* B = stg + (size_t)buf * 4 * c.stage;
+                                const uint4* I = reinterpret_cast<const uint4*>(B);
+                                for (uint32_t k = threadIdx.x; k < e - b; k += blockDim.x)
+                                    project_tet_dsmem(c, p,
+                                                      cl_make_tet(I[k], B[c.stage + k], B[2 * c.stage + k],
+                                                                  B[3 * c.stage + k], xi_base),
+                                                      first, lb + b + k, c.lcap);
+                            } else {
+                                stage_bad = true;
+                                atomicCAS(s.err, 0, kErrTimeoutCl);
+                            }
+                        }
+                        ++ph;
+                    } else {
+                        for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
+                            project_tet_dsmem(c, p, cl_load_tet(s, c, tt, xi_base), first, lb + tt, c.lcap);
+                    }
                     cluster_sync();
                 }
             }

@@ -229,13 +229,16 @@ __device__ __forceinline__ void project_contact(const SceneDev& s, const StepPar
     s.contact_lam[ci] = lam;
 }
 
-// The read-only part of a tet's record (indices and rest data).  It does not
-// depend on positions, so the persistent kernel loads a thread's next tet
-// before the grid barrier that precedes its projection.
+// The part of a tet's record that no other tet's projection changes: indices,
+// rest data and its own multipliers (written only by this tet's projection,
+// in an earlier sweep).  None of it depends on positions, so the persistent
+// kernel loads a thread's next tet while it waits at the grid barrier that
+// precedes the projection.
 struct TetRec {
     uint4 id;
     float4 a, b, c;   // DmInv rows; w: V0, mu, lambda
     uint32_t snh;
+    float l0, l1;     // multipliers at the end of the previous sweep
 };
 
 __device__ __forceinline__ TetRec load_tet(const SceneDev& s, uint32_t t) {
@@ -245,6 +248,8 @@ __device__ __forceinline__ TetRec load_tet(const SceneDev& s, uint32_t t) {
     r.b = __ldg(&s.dm1[t]);
     r.c = __ldg(&s.dm2[t]);
     r.snh = s.model[t] != 0;
+    r.l0 = __ldcg(&s.lam0[t]);
+    r.l1 = r.snh ? __ldcg(&s.lam1[t]) : 0.0f;
     return r;
 }
 
@@ -266,7 +271,7 @@ __device__ __forceinline__ void project_tet_rec(const SceneDev& s, const StepPar
     if (!snh) {
         TetEval e;
         stvk_eval(x0, x1, x2, x3, r0, r1, r2, a.w, b.w, c.w, e);
-        const float lacc = first ? 0.0f : s.lam0[t];
+        const float lacc = first ? 0.0f : R.l0;
         float gd = 0.0f;
         if (p.stvk_damping) {
             // sum_i f_i . (xi_i - xn_i) with f = -g
@@ -282,8 +287,8 @@ __device__ __forceinline__ void project_tet_rec(const SceneDev& s, const StepPar
             for (int i = 0; i < 4; ++i) dx[i] = e.g[i] * (w[i] * dl);
         }
     } else {
-        float lD = first ? 0.0f : s.lam0[t];
-        float lH = first ? 0.0f : s.lam1[t];
+        float lD = first ? 0.0f : R.l0;
+        float lH = first ? 0.0f : R.l1;
         float dlD, dlH;
         if (snh_step(x0, x1, x2, x3, r0, r1, r2, fabsf(a.w), b.w, c.w, p.inv_dt2, w, lD, lH, dx, dlD,
                      dlH)) {
