@@ -60,7 +60,7 @@ MATERIALS = {
 # frame for these kernels), from profiles/k_cluster_frame_beam98k.md and
 # profiles/k_frame_block2m.md
 TRAFFIC = {
-    ("beam-98304-snh-twist", "k_cluster_frame"): 7.08e6,
+    ("beam-98304-snh-twist", "k_cluster_frame"): 7.01e6,
     ("block-2621440-snh", "k_frame_t<false>"): 22.876e9 + 2.582e9,
 }
 
