@@ -1467,8 +1467,10 @@ plan_again:
         }
     }
     // wavefront mode (only when asked for: measured slower than the grid
-    // barrier on every workload - 22 vs 9.4 ms on the 98k-tet beam, 40 vs
-    // 24.5 ms on the 2.6M-tet block - as each CTA has ~100 neighbours to poll)
+    // barrier on every workload - 22.1 vs 8.0 ms on the 98k-tet beam, 34.0 vs
+    // 22.1 ms on the 2.6M-tet block, 16.1 vs 13.5 ms on 512 boxes: a CTA of
+    // the block polls 22 neighbours on average (36 at most), and each phase
+    // pays the release of its stores, the polls' L2 round trips and a fence)
     h->d.prog = nullptr;
     h->d.nb_start = nullptr;
     h->d.nb = nullptr;

@@ -30,6 +30,9 @@ def test_params_default_follow_reference_parameters():
     # simulation_parameters.h:12-27
     assert p.compliance == 1e-4 and p.damping == 0.0 and p.collision_compliance == 1e-8
     assert tuple(p.gravity) == (0.0, -9.81, 0.0)
+    # library-side defaults: automatic mode, finite-state checks and staged
+    # tet records in the cluster mode
+    assert p.exec_mode == capi.EXEC_AUTO and p.check_finite == 1 and p.stage_records == 1
 
 
 def test_create_without_gpu_fails_loudly():

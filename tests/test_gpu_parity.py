@@ -356,3 +356,17 @@ def test_cluster_mode_deterministic(capi_mod):
     a.step(4)
     b.step(4)
     assert np.array_equal(a.positions(), b.positions())
+
+
+@pytest.mark.parametrize("make", [lambda: scenes.beam_twist(16, 4, 4, 0.05), lambda: _batch(24, seed=9)])
+def test_cluster_staging_is_exact(capi_mod, make):
+    """Tet records staged in shared memory one phase ahead (bulk async copies)
+    and records read from global memory in the phase give identical bits."""
+    sc = make()
+    a = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_CLUSTER, stage_records=1)
+    b = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_CLUSTER, stage_records=0)
+    assert a.stats().cluster_phase_max_tets > 0
+    a.step(3)
+    b.step(3)
+    assert np.array_equal(a.positions(), b.positions())
+    assert np.array_equal(a.velocities(), b.velocities())
