@@ -478,10 +478,23 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
     cluster_sync();
 }
 
+// The dynamic shared-memory limit is a per-function attribute shared by every
+// handle of the process, so it is raised to the most the device allows next
+// to the kernel's static shared memory rather than to this scene's need: a
+// later handle needing less must not make an earlier handle's launch invalid
+// (measured: no change in the frame time).
 cudaError_t cluster_configure(int block, size_t smem) {
+    (void)block;
     cudaError_t e = cudaFuncSetAttribute(k_cluster_frame, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_cluster_frame, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0, optin = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, k_cluster_frame)) != cudaSuccess) return e;
+    const size_t max_dyn = (size_t)optin > fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
+    if (smem > max_dyn) return cudaErrorInvalidValue;
+    return cudaFuncSetAttribute(k_cluster_frame, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dyn);
 }
 
 cudaError_t cluster_max_active(int cluster_size, int block, size_t smem, int* n) {
