@@ -293,13 +293,14 @@ def hash_candidates(o: "Oracle", xf: np.ndarray, cell: float, self_contacts: boo
     return out
 
 
-def noise_floor(scene, frames: int, order=None, offsets=None, seed: int = 0) -> float:
+def noise_floor(scene, frames: int, order=None, offsets=None, seed: int = 0, threads: int = 1) -> float:
     """Max position deviation after `frames` between the oracle and the
     oracle restarted from FP32-rounded initial positions nudged by one ulp.
     It measures how far rounding at FP32 level alone carries the sequential
-    loop, the yardstick for multi-frame FP32-vs-FP64 comparisons."""
-    a = Oracle(scene)
-    b = Oracle(scene)
+    loop, the yardstick for multi-frame FP32-vs-FP64 comparisons.  `threads`
+    > 1 runs the colour-parallel sweep, bit-identical to the sequential one."""
+    a = Oracle(scene, threads=threads)
+    b = Oracle(scene, threads=threads)
     if order is not None:
         a.set_order(order, offsets)
         b.set_order(order, offsets)
