@@ -382,8 +382,11 @@ sbs_status sbs_mlp_train(sbs_mlp* m, uint32_t steps, uint32_t batch, float lr, u
  * previous substep's solve displacement plus the network's correction) into
  * multipliers (colour order, each constraint's increment best matching the
  * displacement still missing at its vertices) -> `iterations` sweeps
- * continuing from those multipliers.  The previous substep's displacement is
- * known when its features were computed and the state was not replaced since
+ * continuing from those multipliers.  fit_sweeps = 0 is the carry start: the
+ * free vertices move by the guessed displacement and the elastic multipliers
+ * keep the values the previous substep's solve ended with (zero when there is
+ * no previous substep).  The previous substep's displacement is known when
+ * its features were computed and the state was not replaced since
  * (set_state / set_predicted / a frame without the network reset it to 0).
  * Do not train the same network while it is attached. */
 sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps);

@@ -2062,7 +2062,7 @@ static sbs_status warm_prepare(sbs_gpu* h) {
 sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps) {
     sbs_status s = check_ready(h);
     if (s) return s;
-    if (m && (fit_sweeps < 1 || fit_sweeps > 16)) return fail(h, SBS_EINVAL, "fit_sweeps must be 1..16");
+    if (m && fit_sweeps > 16) return fail(h, SBS_EINVAL, "fit_sweeps must be 0..16");
     if (m && m->d.device != h->prm.device) return fail(h, SBS_EINVAL, "MLP lives on another device");
     if (m && (s = warm_prepare(h)) != SBS_OK) return s;
     if (m) CU(h, mlp_reserve(m->d, (int)h->n_verts));
@@ -2076,10 +2076,20 @@ sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps) {
 
 // features -> MLP -> fit sweep (multipliers initialised), on the predicted state
 static sbs_status enqueue_warm_init(sbs_gpu* h, const StepParams& p) {
-    CU(h, launch_features(h->d, h->wd, p, h->xpred_valid ? 1 : 0, h->st));
+    const bool dprev_valid = h->xpred_valid;
+    CU(h, launch_features(h->d, h->wd, p, dprev_valid ? 1 : 0, h->st));
     h->xpred_valid = true;
     CU(h, mlp_infer_tc(h->mlp->d, h->wd.feat, (int)h->n_verts, h->wd.delta, h->d.err, (int)SBS_ETIMEOUT, h->n_sm,
                        h->st));
+    if (h->fit_sweeps == 0) {
+        // carry start: the multipliers stay as the previous substep left
+        // them, unless there is no previous substep of this state
+        if (!dprev_valid) {
+            CU(h, cudaMemsetAsync(h->d.lam0, 0, (size_t)h->n_tets * sizeof(float), h->st));
+            CU(h, cudaMemsetAsync(h->d.lam1, 0, (size_t)h->n_tets * sizeof(float), h->st));
+        }
+        CU(h, launch_carry(h->d, h->wd, h->st));
+    }
     for (uint32_t k = 0; k < h->fit_sweeps; ++k)
         for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c)
             CU(h, launch_fit_segment(h->d, h->wd, p, h->colour_offsets[c], h->colour_offsets[c + 1], k == 0 ? 1 : 0,

@@ -12,7 +12,9 @@
 //     dl = argmin sum_i m_i |w_i grad_i C dl - r_i|^2 + alpha~ (lambda + dl)^2,
 //     r_i = x_pred_i + d_i - x_i,
 // (2x2 normal equations for SNH), and moves its vertices accordingly.  The
-// ordinary sweeps then continue from those multipliers.  Features (per
+// ordinary sweeps then continue from those multipliers.  With no fit sweeps
+// the start "carries" the previous substep's multipliers instead (k_carry).
+// Features (per
 // vertex): x_pred - x (3), d_prev (3), Green strain of the mean deformation
 // gradient of the incident tets at x_pred (6: E00 E11 E22 E01 E02 E12),
 // external acceleration (3), pin flag (1).
@@ -175,6 +177,33 @@ __device__ __forceinline__ void fit_tet(const SceneDev& s, const WarmDev& w, con
 __global__ void k_fit_segment(SceneDev s, WarmDev w, StepParams p, uint32_t b, uint32_t e, int first) {
     for (uint32_t t = b + blockIdx.x * blockDim.x + threadIdx.x; t < e; t += gridDim.x * blockDim.x)
         fit_tet(s, w, p, t, first != 0);
+}
+
+// Carry start (no fit sweeps): every free vertex moves to x_pred + d_prev +
+// MLP correction, and the multipliers keep the values the previous substep's
+// solve ended with - the displacement d_prev came from those multipliers, so
+// the two stay consistent up to the change of the constraint gradients over
+// one substep.  For stiff bodies, whose Gauss-Seidel sweeps rebuild the
+// multipliers only slowly, that start is far closer to the solution than
+// multipliers fitted from the displacement in a few sweeps.
+__global__ void k_carry(SceneDev s, WarmDev w) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n_verts; i += gridDim.x * blockDim.x) {
+        float4 x = s.xi[i];
+        if (!(x.w > 0.0f)) continue;
+        const float* dp = w.feat + (size_t)i * 16 + 3;
+        const float* d = w.delta + (size_t)i * 3;
+        x.x += dp[0] + d[0];
+        x.y += dp[1] + d[1];
+        x.z += dp[2] + d[2];
+        s.xi[i] = x;
+    }
+}
+
+cudaError_t launch_carry(const SceneDev& s, const WarmDev& w, cudaStream_t st) {
+    const int grid = (int)std::min<uint32_t>(4096, (s.n_verts + 255) / 256);
+    k_carry<<<grid > 0 ? grid : 1, 256, 0, st>>>(s, w);
+    count_launch();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParams& p, int dprev_valid,

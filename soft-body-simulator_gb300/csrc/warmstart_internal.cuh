@@ -22,5 +22,6 @@ cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParam
                             cudaStream_t st);
 cudaError_t launch_fit_segment(const SceneDev& s, const WarmDev& w, const StepParams& p, uint32_t b, uint32_t e,
                                int first, cudaStream_t st);
+cudaError_t launch_carry(const SceneDev& s, const WarmDev& w, cudaStream_t st);
 
 }  // namespace sbs

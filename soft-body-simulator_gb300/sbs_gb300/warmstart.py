@@ -1,15 +1,22 @@
 """Learned warm start: training data from the plain solver, GPU training,
 and evaluation by Gauss-Seidel iterations to reach the plain residual.
 
-The workload is the 450-tet cantilever (10x3x3 cubes of 0.1 m, StVK E 1e5,
-nu 0.45, rho 1000), 1 substep of 1/60 s, 30 plain iterations, under seeded
-random body-force fields (three sinusoids, amplitude U(0, 50) N/kg, wave
-vectors up to 4 cycles per beam length) and a random pinned face.  Many
-trajectories run as independent bodies of one solver handle.
+Two workloads, both under seeded random body-force fields (three sinusoids,
+amplitude U(0, 50) N/kg, wave vectors up to 4 cycles per beam length) and a
+random pinned face, many trajectories running as independent bodies of one
+solver handle:
+
+* ``CANTILEVER``: the 450-tet beam (10x3x3 cubes of 0.1 m, 5 tets each,
+  StVK E 1e5, nu 0.45, rho 1000), 1 substep of 1/60 s, 30 plain iterations;
+* ``BEAM98K``: the 98,304-tet beam (64x16x16 cubes of 0.05 m, 6 tets each,
+  stable Neo-Hookean E 1e6, nu 0.49, rho 1000), 4 substeps x 30 plain
+  iterations per 1/60 s frame.
 """
 from __future__ import annotations
 
 import math
+from dataclasses import dataclass
+from typing import Callable
 
 import numpy as np
 
@@ -18,46 +25,80 @@ from . import capi, scenes
 FACES = ("x0", "x1", "y0", "y1", "z0", "z1")
 
 
-def beam_trajectory_body(seed: int):
-    """One C1 beam with its own force field and pinned face."""
-    x0, tets = scenes.bar_5tet(11, 4, 4, 0.1)
+def _trajectory_body(seed: int, x0, tets, model: int, young: float, poisson: float, length: float,
+                     jitter: float):
+    """A beam with its own force field and pinned face."""
     rng = np.random.default_rng(seed)
     face = FACES[rng.integers(0, 6)]
     ax = "xyz".index(face[0])
     val = x0[:, ax].min() if face[1] == "0" else x0[:, ax].max()
     pinned = np.nonzero(np.isclose(x0[:, ax], val))[0].astype(np.uint32)
-    acc = scenes.body_force_field(x0, seed + 7919, length=1.0, amp_max=50.0, max_cycles=4.0)
-    xi = scenes.jitter(x0, 1e-3, seed + 104729, pinned)
-    return scenes.Body(x0=x0, tets=tets, model=scenes.MODEL_STVK, young=1e5, poisson=0.45,
+    acc = scenes.body_force_field(x0, seed + 7919, length=length, amp_max=50.0, max_cycles=4.0)
+    xi = scenes.jitter(x0, jitter, seed + 104729, pinned)
+    return scenes.Body(x0=x0, tets=tets, model=model, young=young, poisson=poisson,
                        density=1000.0, x_init=xi, pinned=pinned, ext_acc=acc)
 
 
-def batch_scene(seeds, iterations: int = 30) -> scenes.Scene:
-    return scenes.Scene("beam450-batch", [beam_trajectory_body(s) for s in seeds], 1.0 / 60.0, 1,
-                        iterations, 60, ground=((0.0, 1.0, 0.0), 1.0))
+def beam_trajectory_body(seed: int):
+    """One 450-tet cantilever trajectory."""
+    x0, tets = scenes.bar_5tet(11, 4, 4, 0.1)
+    return _trajectory_body(seed, x0, tets, scenes.MODEL_STVK, 1e5, 0.45, 1.0, 1e-3)
 
 
-def generate(seeds, frames: int = 60, iterations: int = 30, exec_mode: int = 1):
+def beam98k_trajectory_body(seed: int):
+    """One 98,304-tet beam trajectory."""
+    x0, tets = scenes.bar_6tet(65, 17, 17, 0.05)
+    return _trajectory_body(seed, x0, tets, scenes.MODEL_SNH, 1e6, 0.49, 3.2, 1e-4)
+
+
+@dataclass(frozen=True)
+class Workload:
+    name: str
+    make_body: Callable
+    substeps: int
+    iterations: int
+    frame_dt: float = 1.0 / 60.0
+
+
+CANTILEVER = Workload("beam450", beam_trajectory_body, 1, 30)
+BEAM98K = Workload("beam98k", beam98k_trajectory_body, 4, 30)
+
+
+def batch_scene(seeds, iterations: int | None = None, workload: Workload = CANTILEVER) -> scenes.Scene:
+    it = workload.iterations if iterations is None else iterations
+    return scenes.Scene(f"{workload.name}-batch", [workload.make_body(s) for s in seeds], workload.frame_dt,
+                        workload.substeps, it, 60, ground=((0.0, 1.0, 0.0), 1.0))
+
+
+def generate(seeds, frames: int = 60, iterations: int | None = None, exec_mode: int = 1,
+             workload: Workload = CANTILEVER, keep: float = 1.0, seed: int = 0):
     """Runs the plain solver on the trajectories `seeds` and returns
     (features [N,16], targets [N,3]): per substep and vertex, the features at
-    the predicted state and the part of the displacement the 30-iteration
-    solve applied that the previous substep's displacement (features 3:6)
-    does not already give."""
-    sc = batch_scene(seeds, iterations)
+    the predicted state and the part of the displacement the plain solve
+    applied that the previous substep's displacement (features 3:6) does not
+    already give.  keep < 1 keeps that random fraction of the vertices of
+    each substep (bounds the data of large bodies)."""
+    sc = batch_scene(seeds, iterations, workload)
     g = capi.Solver(sc, exec_mode=exec_mode)
-    dt = sc.frame_dt
+    dt = sc.frame_dt / sc.substeps
+    rng = np.random.default_rng(seed)
     X, Y = [], []
     for f in range(frames):
         g.detect_contacts()
-        g.predict(dt)
-        feat = g.features()
-        xp = g.predicted_all()
-        g.solve(dt, iterations)
-        X.append(feat)
-        Y.append(g.predicted_all() - xp - feat[:, 3:6])
-        g.update_velocities(dt)
+        for _ in range(sc.substeps):
+            g.predict(dt)
+            feat = g.features()
+            xp = g.predicted_all()
+            g.solve(dt, sc.iterations)
+            y = g.predicted_all() - xp - feat[:, 3:6]
+            if keep < 1.0:
+                sel = rng.random(len(feat)) < keep
+                feat, y = feat[sel], y[sel]
+            X.append(feat.astype(np.float32))
+            Y.append(y.astype(np.float32))
+            g.update_velocities(dt)
     g.close()
-    return np.concatenate(X).astype(np.float32), np.concatenate(Y).astype(np.float32)
+    return np.concatenate(X), np.concatenate(Y)
 
 
 def fit(X, Y, steps: int = 20000, batch: int = 65536, lr: float = 1e-3, seed: int = 0, device: int = 0,
@@ -83,57 +124,62 @@ def residual_after(g, dt):
     return g.residual(dt)[0]
 
 
-def _plain_frame(g, dt, iterations):
-    """One frame of the plain solver that also records the prediction, so
-    the next substep knows its previous solve displacement."""
+def _plain_frame(g, sc):
+    """One frame of the plain solver that also records the predictions, so
+    every substep knows its previous solve displacement."""
+    dt = sc.frame_dt / sc.substeps
     g.detect_contacts()
-    g.predict(dt)
-    g.features()
-    g.solve(dt, iterations)
-    g.update_velocities(dt)
+    for _ in range(sc.substeps):
+        g.predict(dt)
+        g.features()
+        g.solve(dt, sc.iterations)
+        g.update_velocities(dt)
 
 
-def evaluate(mlp, seeds, frame: int = 20, iterations: int = 30, max_iters: int = 60, exec_mode: int = 1,
-             fit_sweeps: int = 1):
+def evaluate(mlp, seeds, frame: int = 20, iterations: int | None = None, max_iters: int = 60,
+             exec_mode: int = 1, fit_sweeps: int = 1, workload: Workload = CANTILEVER):
     """For each held-out trajectory, two handles advance `frame` plain frames
-    in lockstep (identical states); then one runs plain sweeps (residual
-    r_plain[k] after k sweeps) and the other the warm start (fit sweeps, then
-    sweeps continuing from the fitted multipliers).  The warm start is
+    in lockstep (identical states); then, on the first substep of the next
+    frame, one runs plain sweeps (residual r_plain[k] after k sweeps) and the
+    other the warm start (fit sweeps, then sweeps continuing from the fitted
+    multipliers; fit_sweeps = 0: the carry start).  The warm start is
     discarded, and the plain start used, when its residual after the fit
-    exceeds r_plain[1]; otherwise `iterations` is the number of sweeps (fit
-    sweeps included) it needs to reach r_plain[iterations].  Returns a list of
-    dicts."""
+    exceeds the plain start's after as many sweeps (r_plain[0]: at the
+    prediction, with zero multipliers); otherwise `iterations` is the number
+    of sweeps (fit sweeps included) it needs to reach r_plain[iterations].
+    Returns a list of dicts."""
     out = []
     for s in seeds:
-        sc = batch_scene([s], iterations)
+        sc = batch_scene([s], iterations, workload)
+        it = sc.iterations
         a = capi.Solver(sc, exec_mode=exec_mode)
         b = capi.Solver(sc, exec_mode=exec_mode)
-        dt = sc.frame_dt
+        dt = sc.frame_dt / sc.substeps
         for _ in range(frame):
-            _plain_frame(a, dt, iterations)
-            _plain_frame(b, dt, iterations)
+            _plain_frame(a, sc)
+            _plain_frame(b, sc)
         same = bool(np.array_equal(a.get_state(0)[0], b.get_state(0)[0]))
         a.detect_contacts()
         a.predict(dt)
         a.features()
-        r_plain = [None]
-        for k in range(1, iterations + 1):
+        r_plain = [residual_after(a, dt)]
+        for k in range(1, it + 1):
             a.solve_ex(dt, 1, k == 1)
             r_plain.append(residual_after(a, dt))
-        target = r_plain[iterations]
+        target = r_plain[it]
         b.detect_contacts()
         b.predict(dt)
         b.set_warm_start(mlp, fit_sweeps)
         b.warm_start_init(dt)
         r_fit = residual_after(b, dt)
-        used, fallback, r_end = iterations, True, target
-        if r_fit <= r_plain[1]:
+        used, fallback, r_end = it, True, target
+        if r_fit <= r_plain[min(fit_sweeps, it)]:
             k, r = fit_sweeps, r_fit
             while r > target and k < max_iters:
                 b.solve_ex(dt, 1, False)
                 k += 1
                 r = residual_after(b, dt)
-            if r <= target and k <= iterations:
+            if r <= target and k <= it:
                 used, fallback, r_end = k, False, r
         b.set_warm_start(None)
         out.append({"seed": int(s), "same_start": same, "r_plain": float(target), "r_plain_1": float(r_plain[1]),
@@ -142,3 +188,62 @@ def evaluate(mlp, seeds, frame: int = 20, iterations: int = 30, max_iters: int =
         a.close()
         b.close()
     return out
+
+
+def main(argv=None):
+    """Generate, train and evaluate one warm-start experiment; prints one
+    JSON line (python -m sbs_gb300.warmstart --workload beam98k ...)."""
+    import argparse
+    import json
+    import time
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="beam450", choices=["beam450", "beam98k"])
+    ap.add_argument("--train-seeds", type=int, default=256, help="training trajectories")
+    ap.add_argument("--bodies-per-handle", type=int, default=64, help="trajectories run as one handle's bodies")
+    ap.add_argument("--frames", type=int, default=60)
+    ap.add_argument("--keep", type=float, default=1.0, help="fraction of vertices kept per substep")
+    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--eval-seeds", type=int, default=40)
+    ap.add_argument("--eval-frame", type=int, default=20)
+    ap.add_argument("--fit-sweeps", default="0,2,3", help="0: carry the previous multipliers")
+    args = ap.parse_args(argv)
+    wl = {"beam450": CANTILEVER, "beam98k": BEAM98K}[args.workload]
+    t0 = time.perf_counter()
+    Xs, Ys = [], []
+    seeds = list(range(1000, 1000 + args.train_seeds))
+    for i in range(0, len(seeds), args.bodies_per_handle):
+        X, Y = generate(seeds[i:i + args.bodies_per_handle], frames=args.frames, workload=wl, keep=args.keep,
+                        seed=i)
+        Xs.append(X)
+        Ys.append(Y)
+    X, Y = np.concatenate(Xs), np.concatenate(Ys)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    m, losses = fit(X, Y, steps=args.steps, batch=args.batch, lr=1e-3, seed=1)
+    t_fit = time.perf_counter() - t0
+    line = {"workload": wl.name, "substeps": wl.substeps, "plain_iterations": wl.iterations,
+            "train_trajectories": args.train_seeds, "frames": args.frames, "samples": int(len(X)),
+            "generate_s": t_gen, "train_steps": args.steps, "train_s": t_fit,
+            "loss_first": float(losses[0]), "loss_last": float(losses[-1]), "eval": {}}
+    eval_seeds = list(range(50000, 50000 + args.eval_seeds))
+    for fs in [int(v) for v in args.fit_sweeps.split(",")]:
+        res = evaluate(m, eval_seeds, frame=args.eval_frame, fit_sweeps=fs, workload=wl)
+        its = np.array([r["iterations"] for r in res])
+        line["eval"][f"fit_{fs}"] = {"mean_iterations": float(its.mean()),
+                                     "fallbacks": int(sum(r["fallback"] for r in res)),
+                                     "same_start": all(r["same_start"] for r in res),
+                                     "sweep_fraction": float(its.mean() / wl.iterations)}
+    # the previous-displacement guess alone (network output zero)
+    m.set_params(np.zeros(m.n_params, np.float32))
+    for fs in (0, 2):
+        res = evaluate(m, eval_seeds, frame=args.eval_frame, fit_sweeps=fs, workload=wl)
+        line["eval"][f"prev_displacement_only_fit_{fs}"] = {
+            "mean_iterations": float(np.mean([r["iterations"] for r in res])),
+            "fallbacks": int(sum(r["fallback"] for r in res))}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

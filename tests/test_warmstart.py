@@ -1,7 +1,8 @@
 """Learned warm start: the previous-displacement feature, the fit sweeps'
 contract, and a gain in Gauss-Seidel sweeps at equal XPBD residual over the
 plain solver on held-out trajectories (450-tet cantilever under random body
-forces, 30 plain iterations)."""
+forces, 30 plain iterations), with the carry start (previous substep's
+multipliers) and with fit sweeps."""
 import numpy as np
 import pytest
 
@@ -40,9 +41,10 @@ def test_fit_sweeps_argument(capi_mod):
     g = capi_mod.Solver(sc, exec_mode=1)
     m = capi_mod.Mlp(device=0, seed=0)
     with pytest.raises(capi_mod.SbsError):
-        g.set_warm_start(m, 0)
-    with pytest.raises(capi_mod.SbsError):
         g.set_warm_start(m, 17)
+    g.set_warm_start(m, 0)             # carry start
+    g.step(2)
+    assert np.isfinite(g.positions()).all()
     m.set_params(np.zeros(m.n_params, np.float32))   # guess = previous displacement
     g.set_warm_start(m, 3)
     g.step(2)                          # frames run through the warm-start path
@@ -55,15 +57,26 @@ def test_warm_start_saves_sweeps(capi_mod):
     X, Y = warmstart.generate(list(range(1000, 1128)), frames=40, iterations=30)
     m, losses = warmstart.fit(X, Y, steps=3000, batch=32768, lr=1e-3, seed=1, chunk=1000)
     assert losses[-1] < losses[0]
-    res = warmstart.evaluate(m, list(range(50000, 50012)), frame=20, iterations=30, fit_sweeps=3)
+    seeds = list(range(50000, 50012))
+    # carry start (previous multipliers): the plain 30-sweep residual in at
+    # most 40% of the sweeps on average, fallbacks counted as 30
+    res = warmstart.evaluate(m, seeds, frame=20, iterations=30, fit_sweeps=0)
     assert all(r["same_start"] for r in res)
     its = np.array([r["iterations"] for r in res])
-    # never worse than plain (the fallback), and fewer sweeps on average
     assert (its <= 30).all()
-    assert its.mean() <= 28.0, its
+    assert its.mean() <= 12.0, its
     for r in res:
         if not r["fallback"]:
             assert r["r_end"] <= r["r_plain"]
+    # the trained network beats its own previous-displacement guess
+    m_zero = capi_mod.Mlp(device=0, seed=0)
+    m_zero.set_params(np.zeros(m_zero.n_params, np.float32))
+    m_zero.set_normalization(X.mean(0), np.maximum(X.std(0), 1e-8), Y.std(0) + 1e-12)
+    res0 = warmstart.evaluate(m_zero, seeds, frame=20, iterations=30, fit_sweeps=0)
+    assert its.mean() < np.mean([r["iterations"] for r in res0])
+    # fit sweeps: never worse than plain (the fallback)
+    resf = warmstart.evaluate(m, seeds[:4], frame=20, iterations=30, fit_sweeps=3)
+    assert all(r["iterations"] <= 30 for r in resf)
 
 
 def test_warm_start_with_springs_and_grid_environment(capi_mod):
