@@ -54,18 +54,32 @@ def beam98k_trajectory_body(seed: int):
 @dataclass(frozen=True)
 class Workload:
     name: str
-    make_body: Callable
+    make_body: Callable | None    # seed -> one trajectory body (None: make_scene)
     substeps: int
     iterations: int
     frame_dt: float = 1.0 / 60.0
+    make_scene: Callable | None = None   # seed -> a whole scene (one trajectory)
+
+
+def _box_scene(seed: int) -> scenes.Scene:
+    return scenes.box_drop(seed=seed)
 
 
 CANTILEVER = Workload("beam450", beam_trajectory_body, 1, 30)
 BEAM98K = Workload("beam98k", beam98k_trajectory_body, 4, 30)
+# the batch of 512 boxes (StVK, body-body contacts, 2 substeps x 20
+# iterations); a trajectory is a whole scene of 512 bodies
+BOXES512 = Workload("boxes512", None, 2, 20, make_scene=_box_scene)
 
 
 def batch_scene(seeds, iterations: int | None = None, workload: Workload = CANTILEVER) -> scenes.Scene:
     it = workload.iterations if iterations is None else iterations
+    if workload.make_scene is not None:
+        if len(seeds) != 1:
+            raise ValueError(f"{workload.name}: one scene per seed")
+        import dataclasses
+        sc = workload.make_scene(seeds[0])
+        return dataclasses.replace(sc, iterations=it, substeps=workload.substeps, frame_dt=workload.frame_dt)
     return scenes.Scene(f"{workload.name}-batch", [workload.make_body(s) for s in seeds], workload.frame_dt,
                         workload.substeps, it, 60, ground=((0.0, 1.0, 0.0), 1.0))
 
@@ -198,7 +212,7 @@ def main(argv=None):
     import time
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="beam450", choices=["beam450", "beam98k"])
+    ap.add_argument("--workload", default="beam450", choices=["beam450", "beam98k", "boxes512"])
     ap.add_argument("--train-seeds", type=int, default=256, help="training trajectories")
     ap.add_argument("--bodies-per-handle", type=int, default=64, help="trajectories run as one handle's bodies")
     ap.add_argument("--frames", type=int, default=60)
@@ -209,7 +223,9 @@ def main(argv=None):
     ap.add_argument("--eval-frame", type=int, default=20)
     ap.add_argument("--fit-sweeps", default="0,2,3", help="0: carry the previous multipliers")
     args = ap.parse_args(argv)
-    wl = {"beam450": CANTILEVER, "beam98k": BEAM98K}[args.workload]
+    wl = {"beam450": CANTILEVER, "beam98k": BEAM98K, "boxes512": BOXES512}[args.workload]
+    if wl.make_scene is not None:
+        args.bodies_per_handle = 1
     t0 = time.perf_counter()
     Xs, Ys = [], []
     seeds = list(range(1000, 1000 + args.train_seeds))
@@ -237,7 +253,7 @@ def main(argv=None):
                                      "sweep_fraction": float(its.mean() / wl.iterations)}
     # the previous-displacement guess alone (network output zero)
     m.set_params(np.zeros(m.n_params, np.float32))
-    for fs in (0, 2):
+    for fs in [int(v) for v in args.fit_sweeps.split(",")]:
         res = evaluate(m, eval_seeds, frame=args.eval_frame, fit_sweeps=fs, workload=wl)
         line["eval"][f"prev_displacement_only_fit_{fs}"] = {
             "mean_iterations": float(np.mean([r["iterations"] for r in res])),
