@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <numeric>
 #include <string>
@@ -39,10 +40,14 @@ struct BodyHost {
 struct GraphKey {
     double dt;
     uint32_t substeps, iterations;
+    // 0: plain frame; warm-started frame: 1 without, 2 with the previous
+    // substep's displacement known at its start
+    int warm;
     bool operator<(const GraphKey& o) const {
         if (dt != o.dt) return dt < o.dt;
         if (substeps != o.substeps) return substeps < o.substeps;
-        return iterations < o.iterations;
+        if (iterations != o.iterations) return iterations < o.iterations;
+        return warm < o.warm;
     }
 };
 
@@ -1554,6 +1559,47 @@ static sbs_status enqueue_frame_kernels(sbs_gpu* h, const StepParams& p) {
 static sbs_status enqueue_warm_init(sbs_gpu* h, const StepParams& p);
 static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t iterations, bool reset);
 
+// Learned warm start: per substep predict -> features -> MLP -> carry or fit
+// sweeps, then the sweeps continue from those multipliers.
+static sbs_status enqueue_warm_frame(sbs_gpu* h, const StepParams& p, uint32_t substeps, uint32_t iterations) {
+    CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+    CU(h, launch_detect_ground(h->d, p, h->st));
+    if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
+    for (uint32_t sub = 0; sub < substeps; ++sub) {
+        CU(h, launch_predict(h->d, p, (int)sub, h->st));
+        sbs_status s = enqueue_warm_init(h, p);
+        if (s) return s;
+        if ((s = enqueue_segments(h, p, iterations, false)) != SBS_OK) return s;
+        CU(h, launch_finalize(h->d, p, h->st));
+    }
+    CU(h, launch_end_frame(h->d, h->st));
+    return SBS_OK;
+}
+
+// Launches the CUDA graph of `key`, capturing it from `enqueue` first.
+static sbs_status run_graph(sbs_gpu* h, const GraphKey& key, const std::function<sbs_status()>& enqueue) {
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+        cudaGraph_t g;
+        const uint64_t k0 = launch_counter();
+        CU(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        sbs_status s = enqueue();
+        cudaError_t e = cudaStreamEndCapture(h->st, &g);
+        h->graph_kernels[key] = launch_counter() - k0;
+        launch_counter() = k0;   // captured, not run
+        if (s != SBS_OK) return s;
+        if (e != cudaSuccess) return fail(h, SBS_ECUDA, std::string("capture: ") + cudaGetErrorString(e));
+        cudaGraphExec_t ge;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(h, SBS_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+        it = h->graphs.emplace(key, ge).first;
+    }
+    CU(h, cudaGraphLaunch(it->second, h->st));
+    count_launch(h->graph_kernels[key]);
+    return SBS_OK;
+}
+
 static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations) {
     StepParams p;
     fill_params(h, p, dt, substeps, iterations);
@@ -1561,19 +1607,13 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
     for (uint32_t k = 0; k < substeps; ++k) t_end += dt;   // same double sequence as the CPU loop
     const uint64_t launches0 = launch_counter();
     if (h->mlp) {
-        // learned warm start: per substep predict -> features -> MLP -> fit
-        // sweep, then the sweeps continue from the fitted multipliers
-        CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
-        CU(h, launch_detect_ground(h->d, p, h->st));
-        if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
-        for (uint32_t sub = 0; sub < substeps; ++sub) {
-            CU(h, launch_predict(h->d, p, (int)sub, h->st));
-            sbs_status s = enqueue_warm_init(h, p);
-            if (s) return s;
-            if ((s = enqueue_segments(h, p, iterations, false)) != SBS_OK) return s;
-            CU(h, launch_finalize(h->d, p, h->st));
-        }
-        CU(h, launch_end_frame(h->d, h->st));
+        // the warm-started frame as one CUDA graph per shape (a substep is
+        // hundreds of small kernels); whether the previous substep's
+        // displacement is known at the frame's start is part of the shape
+        const GraphKey key{dt, substeps, iterations, h->xpred_valid ? 2 : 1};
+        sbs_status s = run_graph(h, key, [&]() { return enqueue_warm_frame(h, p, substeps, iterations); });
+        if (s) return s;
+        h->xpred_valid = true;
     } else if (h->exec_mode == SBS_EXEC_CLUSTER) {
         // the kernel publishes the frame's contacts into the last-frame slots
         CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
@@ -1597,26 +1637,9 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
         CU(h, cudaMemsetAsync(h->d.bar, 0, 2 * sizeof(unsigned), h->st));   // barrier arrival count
         CU(h, launch_persistent_frame(h->d, p, h->pers_block, h->pers_grid, h->st));
     } else {
-        GraphKey key{dt, substeps, iterations};
-        auto it = h->graphs.find(key);
-        if (it == h->graphs.end()) {
-            cudaGraph_t g;
-            const uint64_t k0 = launch_counter();
-            CU(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-            sbs_status s = enqueue_frame_kernels(h, p);
-            cudaError_t e = cudaStreamEndCapture(h->st, &g);
-            h->graph_kernels[key] = launch_counter() - k0;
-            launch_counter() = k0;   // captured, not run
-            if (s != SBS_OK) return s;
-            if (e != cudaSuccess) return fail(h, SBS_ECUDA, std::string("capture: ") + cudaGetErrorString(e));
-            cudaGraphExec_t ge;
-            e = cudaGraphInstantiate(&ge, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) return fail(h, SBS_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e));
-            it = h->graphs.emplace(key, ge).first;
-        }
-        CU(h, cudaGraphLaunch(it->second, h->st));
-        count_launch(h->graph_kernels[key]);
+        const GraphKey key{dt, substeps, iterations, 0};
+        sbs_status s = run_graph(h, key, [&]() { return enqueue_frame_kernels(h, p); });
+        if (s) return s;
     }
     h->kernel_launches += launch_counter() - launches0;
     h->frames++;
@@ -2066,6 +2089,7 @@ sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps) {
     if (m && m->d.device != h->prm.device) return fail(h, SBS_EINVAL, "MLP lives on another device");
     if (m && (s = warm_prepare(h)) != SBS_OK) return s;
     if (m) CU(h, mlp_reserve(m->d, (int)h->n_verts));
+    if (m) CU(h, mlp_tc_configure());
     h->mlp = m;
     if (m) h->fit_sweeps = fit_sweeps;
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);

@@ -53,6 +53,8 @@ cudaError_t mlp_reserve(MlpDev& d, int n);
 cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cudaStream_t st);
 // Inference only (no activations kept): the fused tcgen05 kernel of
 // mlp_tc.cu.  A wait that times out stores err_code into *err (if 0).
+// Sets the tcgen05 inference kernel's shared-memory limit on the current device.
+cudaError_t mlp_tc_configure();
 cudaError_t mlp_infer_tc(const MlpDev& d, const float* x, int n, float* y, int* err, int err_code, int n_sm,
                          cudaStream_t st);
 cudaError_t mlp_backward_dev(MlpDev& d, const float* x, const float* t, int n, cudaStream_t st);

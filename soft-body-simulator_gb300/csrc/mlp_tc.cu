@@ -279,12 +279,20 @@ __global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_infer_tc(TcArgs a) {
 
 }  // namespace
 
+cudaError_t mlp_tc_configure() {
+    return cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+}
+
 cudaError_t mlp_infer_tc(const MlpDev& d, const float* x, int n, float* y, int* err, int err_code, int n_sm,
                          cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    // per device and cheap: set on every call (the caller may switch devices)
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+    // per device and cheap: set on every call (the caller may switch
+    // devices), except while the stream is being captured into a graph (the
+    // warm-start path sets it when the network is attached)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
     if (e != cudaSuccess) return e;
+    if (cs == cudaStreamCaptureStatusNone && (e = mlp_tc_configure()) != cudaSuccess) return e;
     TcArgs a;
     a.x = x;
     a.n = n;

@@ -308,9 +308,10 @@ class Solver:
         for _ in range(frames):
             self._check(self.L.sbs_gpu_step(self.h, fdt, sub, its))
 
-    def step_timed(self) -> float:
+    def step_timed(self, iterations=None) -> float:
         s = self.scene
-        self._check(self.L.sbs_gpu_step_timed(self.h, s.frame_dt, s.substeps, s.iterations))
+        its = s.iterations if iterations is None else iterations
+        self._check(self.L.sbs_gpu_step_timed(self.h, s.frame_dt, s.substeps, its))
         return self.stats().last_frame_ms
 
     def solve(self, dt: float, iterations: int):

@@ -204,6 +204,49 @@ def evaluate(mlp, seeds, frame: int = 20, iterations: int | None = None, max_ite
     return out
 
 
+def frame_rate(mlp, seeds, k_list, frames: int = 30, lead_frames: int = 20, fit_sweeps: int = 0,
+               workload: Workload = CANTILEVER):
+    """Frames per second against residual: per held-out trajectory a plain
+    handle (default execution mode, the workload's iterations) and, for each
+    k in `k_list`, a warm-started one (k iterations per substep, its frames
+    captured as CUDA graphs) advance `lead_frames` plain frames; a warm
+    handle then runs one untimed warm-started frame (so every substep knows
+    its predecessor's displacement), and each handle steps `frames` timed
+    frames.  The trajectories part ways, so the comparison is statistical:
+    median device time per frame and median residual after a frame, over all
+    frames and trajectories."""
+    plain_ms, plain_r = [], []
+    warm_ms = {k: [] for k in k_list}
+    warm_r = {k: [] for k in k_list}
+    for s in seeds:
+        sc = batch_scene([s], None, workload)
+        dt = sc.frame_dt / sc.substeps
+        a = capi.Solver(sc)
+        a.step(lead_frames + 1)
+        for _ in range(frames):
+            plain_ms.append(a.step_timed())
+            plain_r.append(a.residual(dt)[0])
+        a.close()
+        for k in k_list:
+            b = capi.Solver(sc, exec_mode=1)
+            b.step(lead_frames)
+            b.set_warm_start(mlp, fit_sweeps)
+            b.step(1, iterations=k)
+            for _ in range(frames):
+                warm_ms[k].append(b.step_timed(iterations=k))
+                warm_r[k].append(b.residual(dt)[0])
+            b.set_warm_start(None)
+            b.close()
+    pm, pr = float(np.median(plain_ms)), float(np.median(plain_r))
+    out = {"plain_iterations": sc.iterations, "frames": len(plain_ms), "plain_ms_per_frame": pm,
+           "plain_residual_median": pr, "warm": {}}
+    for k in k_list:
+        wm, wr = float(np.median(warm_ms[k])), float(np.median(warm_r[k]))
+        out["warm"][str(k)] = {"ms_per_frame": wm, "residual_median": wr, "frames_per_s_ratio": pm / wm,
+                               "residual_ratio": wr / pr}
+    return out
+
+
 def main(argv=None):
     """Generate, train and evaluate one warm-start experiment; prints one
     JSON line (python -m sbs_gb300.warmstart --workload beam98k ...)."""
@@ -222,6 +265,10 @@ def main(argv=None):
     ap.add_argument("--eval-seeds", type=int, default=40)
     ap.add_argument("--eval-frame", type=int, default=20)
     ap.add_argument("--fit-sweeps", default="0,2,3", help="0: carry the previous multipliers")
+    ap.add_argument("--rate-k", default="",
+                    help="comma list: also time frames with these warm-started iterations per substep")
+    ap.add_argument("--rate-seeds", type=int, default=4)
+    ap.add_argument("--rate-frames", type=int, default=30)
     args = ap.parse_args(argv)
     wl = {"beam450": CANTILEVER, "beam98k": BEAM98K, "boxes512": BOXES512}[args.workload]
     if wl.make_scene is not None:
@@ -251,6 +298,10 @@ def main(argv=None):
                                      "fallbacks": int(sum(r["fallback"] for r in res)),
                                      "same_start": all(r["same_start"] for r in res),
                                      "sweep_fraction": float(its.mean() / wl.iterations)}
+    if args.rate_k:
+        line["frame_rate"] = frame_rate(m, list(range(60000, 60000 + args.rate_seeds)),
+                                        [int(v) for v in args.rate_k.split(",")], frames=args.rate_frames,
+                                        lead_frames=args.eval_frame, workload=wl)
     # the previous-displacement guess alone (network output zero)
     m.set_params(np.zeros(m.n_params, np.float32))
     for fs in [int(v) for v in args.fit_sweeps.split(",")]:
