@@ -1561,6 +1561,9 @@ static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t ite
 
 // Learned warm start: per substep predict -> features -> MLP -> carry or fit
 // sweeps, then the sweeps continue from those multipliers.
+// In the cluster mode the sweeps of each substep run as one launch of the
+// cluster-resident kernel on the warm-started positions and multipliers
+// (kClExternal | kClCarry); the other modes enqueue the per-phase kernels.
 static sbs_status enqueue_warm_frame(sbs_gpu* h, const StepParams& p, uint32_t substeps, uint32_t iterations) {
     CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
     CU(h, launch_detect_ground(h->d, p, h->st));
@@ -1569,7 +1572,14 @@ static sbs_status enqueue_warm_frame(sbs_gpu* h, const StepParams& p, uint32_t s
         CU(h, launch_predict(h->d, p, (int)sub, h->st));
         sbs_status s = enqueue_warm_init(h, p);
         if (s) return s;
-        if ((s = enqueue_segments(h, p, iterations, false)) != SBS_OK) return s;
+        if (h->exec_mode == SBS_EXEC_CLUSTER) {
+            StepParams q = p;
+            q.substeps = 1;
+            q.cl_flags = kClExternal | kClCarry;
+            CU(h, launch_cluster_frame(h->d, h->cd, q, h->sim_time, h->cl_grid, h->cl_block, h->cl_smem, h->st));
+        } else if ((s = enqueue_segments(h, p, iterations, false)) != SBS_OK) {
+            return s;
+        }
         CU(h, launch_finalize(h->d, p, h->st));
     }
     CU(h, launch_end_frame(h->d, h->st));

@@ -274,9 +274,62 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
         // the group's first colour phase: its records arrive while the slice loads
         if (c.stage && threadIdx.x == 0 && gd.n_col > 0 && p.substeps > 0 && p.iterations > 0)
             stage_issue(s, c, s_cb[0], s_ce[0], stg_base + (ph & 1u) * stg_bytes, mb_base + (ph & 1u) * 8u);
+        const bool ext = (p.cl_flags & kClExternal) != 0;
         // load own slice; ground contacts of own surface vertices from the
         // frame-start positions (bvh_model.cpp:72-94 with the plane SDF)
-        for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+        for (uint32_t i = threadIdx.x; i < nown && ext; i += blockDim.x) {
+            // one warm-started substep: positions as predicted and moved by
+            // the warm start; contacts from the frame's list (below)
+            const uint32_t gv = own0 + i;
+            xi[i] = s.xi[gv];
+            xn[i] = s.xn[gv];
+            vv[i] = s.v[gv];
+            for (int pl = 0; pl < p.n_planes; ++pl)
+                rec[(size_t)i * S + pl] = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+            if (c.body) {
+                const float4 bq = c.bc_q[gv];
+                float4 r = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+                if (bq.w != 0.0f) {
+                    const float4 nn = c.bc_n[gv];
+                    r = make_float4(bq.x, bq.y, bq.z, 0.0f);
+                    bn[i] = nn;
+                    gidx[(size_t)i * S + p.n_planes] = __float_as_uint(nn.w);
+                }
+                rec[(size_t)i * S + p.n_planes] = r;
+            }
+        }
+        if (ext) {
+            __syncthreads();
+            for (int pl = 0; pl < p.n_planes; ++pl) {
+                const uint32_t cnt = min(__ldcg(&s.counters[pl]), s.n_surf);
+                for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                    const Contact ct = s.contacts[(size_t)pl * s.n_surf + k];
+                    const uint32_t gv = __float_as_uint(ct.q.w);
+                    if (gv < own0 || gv >= own1) continue;
+                    const uint32_t i = gv - own0;
+                    rec[(size_t)i * S + pl] = make_float4(ct.q.x, ct.q.y, ct.q.z, 0.0f);
+                    gidx[(size_t)i * S + pl] = k;
+                }
+            }
+            __syncthreads();
+            for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+                bool any = false;
+                for (int sl = 0; sl < S; ++sl) any |= !isnan(rec[(size_t)i * S + sl].x);
+                if (any) clist[atomicAdd(&s_ncont, 1u)] = i;
+            }
+            if (p.cl_flags & kClCarry) {
+                // the multipliers the warm start left (carried or fitted)
+                for (uint32_t col = 0; col < gd.n_col; ++col) {
+                    const uint32_t b = s_cb[col], e = s_ce[col];
+                    float* lb = lam_s + s_lb[col] - b;
+                    for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x) {
+                        lb[tt] = s.lam0[tt];
+                        lb[tt + c.lcap] = s.lam1[tt];
+                    }
+                }
+            }
+        }
+        for (uint32_t i = threadIdx.x; i < nown && !ext; i += blockDim.x) {
             const uint32_t gv = own0 + i;
             const float4 x = s.xn[gv];
             xn[i] = x;
@@ -335,7 +388,7 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
         for (int sub = 0; sub < p.substeps; ++sub) {
             const double t_next = t + p.dt_d;
             // prediction of own vertices (timestep.cpp:35-43) + prescribed motion
-            for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+            for (uint32_t i = threadIdx.x; i < nown && !ext; i += blockDim.x) {
                 float4 v = vv[i];
                 const float4 x = xn[i];
                 if (v.w != 0.0f) {
@@ -366,7 +419,8 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
             }
             cluster_sync();
             for (int it = 0; it < p.iterations; ++it) {
-                const bool first = it == 0;
+                const bool first = it == 0;                                 // contacts start from 0
+                const bool first_lam = first && !(p.cl_flags & kClCarry);  // elastic multipliers
                 // contacts: own vertices only (collision_constraint.cpp:21-41)
                 for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
                     const uint32_t i = clist[k];
@@ -419,7 +473,7 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                                     project_tet_dsmem(c, p,
                                                       cl_make_tet(I[k], B[c.stage + k], B[2 * c.stage + k],
                                                                   B[3 * c.stage + k], xi_base),
-                                                      first, lb + b + k, c.lcap);
+                                                      first_lam, lb + b + k, c.lcap);
                             } else {
                                 stage_bad = true;
                                 atomicCAS(s.err, 0, kErrTimeoutCl);
@@ -428,13 +482,13 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                         ++ph;
                     } else {
                         for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
-                            project_tet_dsmem(c, p, cl_load_tet(s, c, tt, xi_base), first, lb + tt, c.lcap);
+                            project_tet_dsmem(c, p, cl_load_tet(s, c, tt, xi_base), first_lam, lb + tt, c.lcap);
                     }
                     cluster_sync();
                 }
             }
             // velocity update of own vertices (timestep.cpp:48-57)
-            for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+            for (uint32_t i = threadIdx.x; i < nown && !ext; i += blockDim.x) {
                 const float4 a = xi[i];
                 const float4 b = xn[i];
                 float4 v = vv[i];

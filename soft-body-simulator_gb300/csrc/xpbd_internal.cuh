@@ -106,7 +106,16 @@ struct StepParams {
     uint32_t colour_split[kMaxColours];  // first SNH tet of each colour
     int n_edge_colours;
     uint32_t edge_start[kMaxEdgeColours + 1];
+    int cl_flags;                // cluster mode, one warm-started substep: kClExternal | kClCarry
 };
+
+// k_cluster_frame flags.  kClExternal: the substep's positions come
+// predicted (and warm-started) in xi; the kernel runs that one substep's
+// sweeps on them, takes the frame's contacts from the global contact list,
+// and leaves prediction and velocity update to the global kernels.
+// kClCarry: the elastic multipliers start from lam0/lam1, not from zero.
+constexpr int kClExternal = 1;
+constexpr int kClCarry = 2;
 
 // Kernel launchers (xpbd_kernels.cu).  All enqueue on `st`.
 cudaError_t launch_detect_ground(const SceneDev& s, const StepParams& p, cudaStream_t st);

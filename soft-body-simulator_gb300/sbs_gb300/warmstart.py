@@ -208,8 +208,8 @@ def frame_rate(mlp, seeds, k_list, frames: int = 30, lead_frames: int = 20, fit_
                workload: Workload = CANTILEVER):
     """Frames per second against residual: per held-out trajectory a plain
     handle (default execution mode, the workload's iterations) and, for each
-    k in `k_list`, a warm-started one (k iterations per substep, its frames
-    captured as CUDA graphs) advance `lead_frames` plain frames; a warm
+    k in `k_list`, a warm-started one (default mode too, k iterations per
+    substep, its frames captured as CUDA graphs) advance `lead_frames` plain frames; a warm
     handle then runs one untimed warm-started frame (so every substep knows
     its predecessor's displacement), and each handle steps `frames` timed
     frames.  The trajectories part ways, so the comparison is statistical:
@@ -228,7 +228,7 @@ def frame_rate(mlp, seeds, k_list, frames: int = 30, lead_frames: int = 20, fit_
             plain_r.append(a.residual(dt)[0])
         a.close()
         for k in k_list:
-            b = capi.Solver(sc, exec_mode=1)
+            b = capi.Solver(sc)
             b.step(lead_frames)
             b.set_warm_start(mlp, fit_sweeps)
             b.step(1, iterations=k)

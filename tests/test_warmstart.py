@@ -103,3 +103,31 @@ def test_warm_start_with_springs_and_grid_environment(capi_mod):
     assert x[offs[1]:, 1].min() > -0.35               # pushed out of the grid floor
     g.set_warm_start(None)
     g.close()
+
+
+@pytest.mark.parametrize("fit_sweeps", [0, 2])
+def test_warm_start_cluster_matches_graph(capi_mod, oracle_mod, fit_sweeps):
+    """Warm-started frames in the cluster-resident mode (one launch per
+    substep on the warm-started positions and multipliers) against the same
+    frames in the graph mode: the same sweep, so within the FP32 noise floor."""
+    from sbs_gb300 import scenes
+    sc = scenes.beam_twist(16, 4, 4, 0.05)
+    m = capi_mod.Mlp(device=0, seed=3)       # untrained: a small, deterministic correction
+    m.set_normalization(np.zeros(16, np.float32), np.ones(16, np.float32), np.full(3, 1e-4, np.float32))
+    a = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_CLUSTER)
+    b = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_GRAPH)
+    a.step(1)
+    b.step(1)
+    a.set_warm_start(m, fit_sweeps)
+    b.set_warm_start(m, fit_sweeps)
+    a.step(2, iterations=12)
+    b.step(2, iterations=12)
+    xa, xb = a.positions(), b.positions()
+    assert np.isfinite(xa).all()
+    order, off = capi_mod.plan_sweep(sc)
+    floor = oracle_mod.noise_floor(sc, 3, order, off)
+    assert np.abs(xa - xb).max() < 20 * floor + 1e-6 * sc.bbox_diag()
+    # the cluster frames ran (one launch per substep plus the global kernels)
+    assert a.stats().exec_mode == capi_mod.EXEC_CLUSTER
+    a.set_warm_start(None)
+    b.set_warm_start(None)
