@@ -39,6 +39,13 @@ __device__ __forceinline__ m3 deformation(f3 d1, f3 d2, f3 d3, f3 r0, f3 r1, f3 
 
 __device__ __forceinline__ float det3(const m3& F) { return dot(F.c0, cross(F.c1, F.c2)); }
 
+// The Jacobi rotation in plane (p, q) is skipped when its off-diagonal is
+// negligible.
+template <int P, int Q>
+__device__ __forceinline__ bool jacobi_skips(const float (&S)[3][3]) {
+    return fabsf(S[P][Q]) <= 1e-30f + 1e-9f * (fabsf(S[P][P]) + fabsf(S[Q][Q]));
+}
+
 // One cyclic-Jacobi rotation on the symmetric matrix S (upper triangle
 // s00 s01 s02 s11 s12 s22) in plane (p, q), accumulating into V's columns.
 // Rotation from the symmetric 2x2 Schur decomposition (Golub & Van Loan,
@@ -50,7 +57,7 @@ template <int P, int Q>
 __device__ __forceinline__ void jacobi_rot(float (&S)[3][3], f3 (&V)[3]) {
     const float spq = S[P][Q];
     const float spp = S[P][P], sqq = S[Q][Q];
-    if (fabsf(spq) <= 1e-30f + 1e-9f * (fabsf(spp) + fabsf(sqq))) return;
+    if (jacobi_skips<P, Q>(S)) return;
     const float tau = __fdividef(sqq - spp, 2.0f * spq);
     const float q = 1.0f + tau * tau;
     const float t = __fdividef(copysignf(1.0f, tau), fabsf(tau) + q * rsqrtf(q));
@@ -69,8 +76,12 @@ __device__ __forceinline__ void jacobi_rot(float (&S)[3][3], f3 (&V)[3]) {
 
 // SVD of F in the convention of Eigen's JacobiSVD: F = U diag(s) V^T with
 // s >= 0 in decreasing order (U, V orthogonal, either handedness).
-// Method: cyclic Jacobi eigen-decomposition of F^T F for V (5 sweeps),
-// ordering by eigenvalue, then U from Gram-Schmidt on the columns of F V.
+// Method: cyclic Jacobi eigen-decomposition of F^T F for V (at most 5
+// sweeps), ordering by eigenvalue, then U from Gram-Schmidt on the columns of
+// F V.  A tet's sweeps stop early once the next sweep would skip all three
+// rotations (jacobi_rot's own test), when nothing would change any more: the
+// result is bit-identical to five sweeps.  The test is the tet's own (not a
+// warp vote), so it does not depend on which tets share a warp.
 __device__ __forceinline__ void svd3(const m3& F, f3 (&U)[3], float (&s)[3], f3 (&V)[3]) {
     float S[3][3];
     S[0][0] = dot(F.c0, F.c0);
@@ -87,6 +98,7 @@ __device__ __forceinline__ void svd3(const m3& F, f3 (&U)[3], float (&s)[3], f3 
         jacobi_rot<0, 1>(S, V);
         jacobi_rot<0, 2>(S, V);
         jacobi_rot<1, 2>(S, V);
+        if (sweep < 4 && jacobi_skips<0, 1>(S) && jacobi_skips<0, 2>(S) && jacobi_skips<1, 2>(S)) break;
     }
     float e0 = S[0][0], e1 = S[1][1], e2 = S[2][2];
     // sort eigenvalues (and V columns) descending
