@@ -64,3 +64,24 @@ def test_jitter_is_seeded_and_frozen():
     b = scenes.jitter(x, 1e-3, 7, frozen=np.array([0, 3]))
     assert np.array_equal(a, b)
     assert np.all(a[[0, 3]] == 0) and np.abs(a).max() <= 1e-3
+
+
+def test_warm_start_workloads():
+    """The warm-start workloads build the scenes their configurations name."""
+    from sbs_gb300 import warmstart
+    sc = warmstart.batch_scene([1, 2], workload=warmstart.CANTILEVER)
+    assert len(sc.bodies) == 2 and sc.substeps == 1 and sc.iterations == 30
+    assert sc.bodies[0].tets.shape == (450, 4) and sc.bodies[0].ext_acc is not None
+    sc = warmstart.batch_scene([7], workload=warmstart.BEAM98K)
+    b = sc.bodies[0]
+    assert b.tets.shape == (98304, 4) and b.model == scenes.MODEL_SNH
+    assert sc.substeps == 4 and sc.iterations == 30
+    assert len(b.pinned) in (17 * 17, 65 * 17)          # one face of the 64x16x16 grid
+    # the box batch: one whole scene per seed
+    with pytest.raises(ValueError):
+        warmstart.batch_scene([1, 2], workload=warmstart.BOXES512)
+    # seeds differ in force field and pinned face, deterministically
+    a1 = warmstart.beam_trajectory_body(5)
+    a2 = warmstart.beam_trajectory_body(5)
+    a3 = warmstart.beam_trajectory_body(6)
+    assert np.array_equal(a1.ext_acc, a2.ext_acc) and not np.array_equal(a1.ext_acc, a3.ext_acc)
