@@ -335,11 +335,20 @@ class Solver:
     def _nv(self, body: int) -> int:
         return self.scene.n_verts if body == -1 else self.body_sizes[body]
 
-    def get_state(self, body: int = 0):
-        """(x, v) of one body, or of the whole scene with body = -1."""
+    def get_state(self, body: int = 0, out_x=None, out_v=None):
+        """(x, v) of one body, or of the whole scene with body = -1.  out_x /
+        out_v: contiguous float32 arrays of 3 * n values to write into (for
+        example pinned host memory, which the copies reach directly)."""
         n = self._nv(body)
-        x = np.zeros(3 * n, np.float32)
-        v = np.zeros(3 * n, np.float32)
+
+        def buf(out):
+            if out is None:
+                return np.zeros(3 * n, np.float32)
+            if out.dtype != np.float32 or out.size != 3 * n or not out.flags.c_contiguous:
+                raise ValueError("output buffers must be contiguous float32 of 3 * n_verts values")
+            return out
+        x = buf(out_x)
+        v = buf(out_v)
         self._check(self.L.sbs_gpu_get_state(self.h, body, x.ctypes.data, v.ctypes.data))
         return x.reshape(-1, 3), v.reshape(-1, 3)
 

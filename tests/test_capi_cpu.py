@@ -120,3 +120,20 @@ def test_golden_fixtures_reproduce(oracle_mod):
         assert np.array_equal(o.get(), d[f"{name}_x1"])
         o.step(9)
         assert np.array_equal(o.get(), d[f"{name}_x10"])
+
+
+def test_get_state_rejects_bad_output_buffers():
+    """Output buffers are checked on the host before any library call."""
+    class Fake(capi.Solver):
+        def __init__(self):
+            pass
+
+        def _nv(self, body):
+            return 4
+    f = Fake()
+    with pytest.raises(ValueError):
+        f.get_state(-1, np.zeros(12, np.float64), None)
+    with pytest.raises(ValueError):
+        f.get_state(-1, np.zeros(11, np.float32), None)
+    with pytest.raises(ValueError):
+        f.get_state(-1, np.zeros((12, 2), np.float32)[:, 0], None)
