@@ -359,6 +359,7 @@ def main():
                    "bodies": len(scene.bodies),
                    "exec_mode": ["auto", "graph", "persistent", "cluster", "wavefront"][st.exec_mode],
                    "grid_ctas": st.grid_ctas, "block": st.block_size, "colours": st.n_colours,
+                   "tail_colours": st.n_tail_colours,
                    **({"max_tets_per_cta_colour": st.cluster_phase_max_tets,
                        "stage_records": args.stage_records} if st.exec_mode == capi.EXEC_CLUSTER else {}),
                    "l2": (f"flushed (256 MB write) before every timed frame; the "

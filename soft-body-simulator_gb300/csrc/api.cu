@@ -1660,6 +1660,13 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
     return SBS_OK;
 }
 
+// Drops the captured frame graphs (they hold the step parameters).
+static void clear_graphs(sbs_gpu* h) {
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    h->graph_kernels.clear();
+}
+
 // Autotuner: times each candidate configuration on a copy of the state and
 // restores the state afterwards.
 static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations) {
@@ -1727,6 +1734,38 @@ static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t it
     }
     h->exec_mode = bestc.mode;
     if (bestc.mode == SBS_EXEC_PERSISTENT) { h->pers_block = bestc.block; h->pers_grid = bestc.grid; }
+    // second stage, for a winning global mode: the small-colour merge
+    // threshold (colours of at most that many tets run one after another in
+    // one CTA, saving a grid barrier or a launch each), unless the caller set it
+    if ((bestc.mode == SBS_EXEC_PERSISTENT || bestc.mode == SBS_EXEC_GRAPH) && h->prm.tail_threshold < 0 &&
+        best < 1e30f) {
+        const uint32_t ft0 = h->first_tail;
+        uint32_t best_ft = ft0;
+        std::vector<uint32_t> tried{ft0};
+        for (uint32_t thr : {0u, 256u, 1024u, 4096u}) {
+            uint32_t ft = h->n_colours;
+            while (ft > 0 && h->colour_offsets[ft] - h->colour_offsets[ft - 1] <= thr) --ft;
+            if (std::find(tried.begin(), tried.end(), ft) != tried.end()) continue;
+            tried.push_back(ft);
+            h->first_tail = ft;
+            h->base.first_tail = (int)ft;
+            clear_graphs(h);
+            sbs_status s = run_frame(h, dt, substeps, iterations);
+            if (s != SBS_OK) continue;
+            CU(h, cudaEventRecord(h->ev0, h->st));
+            for (int r = 0; r < 3 && s == SBS_OK; ++r) s = run_frame(h, dt, substeps, iterations);
+            CU(h, cudaEventRecord(h->ev1, h->st));
+            CU(h, cudaEventSynchronize(h->ev1));
+            if (s != SBS_OK) continue;
+            if (check_err(h) != SBS_OK) break;
+            float ms = 0;
+            CU(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+            if (ms < best) { best = ms; best_ft = ft; }
+        }
+        h->first_tail = best_ft;
+        h->base.first_tail = (int)best_ft;
+        clear_graphs(h);
+    }
     if (bestc.mode == SBS_EXEC_CLUSTER) {
         int active = 0;
         h->cl_block = bestc.block;
@@ -2102,9 +2141,7 @@ sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps) {
     if (m) CU(h, mlp_tc_configure());
     h->mlp = m;
     if (m) h->fit_sweeps = fit_sweeps;
-    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-    h->graphs.clear();
-    h->graph_kernels.clear();
+    clear_graphs(h);
     return SBS_OK;
 }
 
