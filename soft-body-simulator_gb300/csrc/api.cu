@@ -1947,22 +1947,24 @@ static sbs_status write_fields(sbs_gpu* h, int32_t body, const float* x, bool bo
     sbs_status s = state_range(h, body, &b);
     if (s) return s;
     const size_t bytes = 3ull * b->nv * sizeof(float);
-    CU(h, cudaStreamSynchronize(h->st));   // staging reuse
+    // One synchronisation at the end: the staging buffers are ordered by the
+    // stream, and the scatters skip on the device when the position check
+    // failed, so a rejected call leaves the state as it was.
+    int bad = 0;
+    CU(h, cudaMemsetAsync(h->d_bad, 0, sizeof(int), h->st));
     if (x) {
-        int bad = 0;
         CU(h, cudaMemcpyAsync(h->d_stage_x, x, bytes, cudaMemcpyHostToDevice, h->st));
-        CU(h, cudaMemsetAsync(h->d_bad, 0, sizeof(int), h->st));
         CU(h, launch_check_finite(h->d_stage_x, 3ull * b->nv, h->d_bad, h->st));
-        CU(h, cudaMemcpyAsync(&bad, h->d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-        CU(h, cudaStreamSynchronize(h->st));
-        if (bad) return fail(h, SBS_EINVAL, "non-finite input position");
-        CU(h, launch_scatter_xyz(h->d.xi, both ? h->d.xn : nullptr, h->d_o2n, b->v0, b->nv, h->d_stage_x, h->st));
+        CU(h, launch_scatter_xyz(h->d.xi, both ? h->d.xn : nullptr, h->d_o2n, b->v0, b->nv, h->d_stage_x, h->st,
+                                 h->d_bad));
     }
     if (v) {
         CU(h, cudaMemcpyAsync(h->d_stage_v, v, bytes, cudaMemcpyHostToDevice, h->st));
-        CU(h, launch_scatter_xyz(h->d.v, nullptr, h->d_o2n, b->v0, b->nv, h->d_stage_v, h->st));
+        CU(h, launch_scatter_xyz(h->d.v, nullptr, h->d_o2n, b->v0, b->nv, h->d_stage_v, h->st, h->d_bad));
     }
+    CU(h, cudaMemcpyAsync(&bad, h->d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CU(h, cudaStreamSynchronize(h->st));
+    if (bad) return fail(h, SBS_EINVAL, "non-finite input position");
     return SBS_OK;
 }
 

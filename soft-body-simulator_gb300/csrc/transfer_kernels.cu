@@ -27,9 +27,12 @@ __global__ void k_check_finite(const float* __restrict__ in, uint64_t n, int* ba
         if (!isfinite(in[i])) atomicExch(bad, 1);
 }
 
-// dst[o2n[v0 + o]].xyz = in[3o..3o+2] (.w kept); also into dst2 when given
+// dst[o2n[v0 + o]].xyz = in[3o..3o+2] (.w kept); also into dst2 when given.
+// Nothing is written when skip is given and set (a failed input check ahead
+// on the stream), so a rejected input leaves the state as it was.
 __global__ void k_scatter_xyz(float4* __restrict__ dst, float4* __restrict__ dst2, const uint32_t* __restrict__ o2n,
-                              uint32_t v0, uint32_t nv, const float* __restrict__ in) {
+                              uint32_t v0, uint32_t nv, const float* __restrict__ in, const int* skip) {
+    if (skip && *skip) return;
     for (uint32_t o = blockIdx.x * blockDim.x + threadIdx.x; o < nv; o += gridDim.x * blockDim.x) {
         const uint32_t n = o2n[v0 + o];
         float4 q = dst[n];
@@ -66,9 +69,9 @@ cudaError_t launch_check_finite(const float* in, uint64_t n, int* bad, cudaStrea
 }
 
 cudaError_t launch_scatter_xyz(float4* dst, float4* dst2, const uint32_t* o2n, uint32_t v0, uint32_t nv,
-                               const float* in, cudaStream_t st) {
+                               const float* in, cudaStream_t st, const int* skip) {
     if (nv == 0) return cudaSuccess;
-    k_scatter_xyz<<<blocks(nv), 256, 0, st>>>(dst, dst2, o2n, v0, nv, in);
+    k_scatter_xyz<<<blocks(nv), 256, 0, st>>>(dst, dst2, o2n, v0, nv, in, skip);
     count_launch();
     return cudaGetLastError();
 }

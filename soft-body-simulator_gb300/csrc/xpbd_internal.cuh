@@ -139,7 +139,7 @@ cudaError_t launch_gather_xyz(const float4* src, const uint32_t* o2n, uint32_t v
                               int check, int* bad, cudaStream_t st);
 cudaError_t launch_check_finite(const float* in, uint64_t n, int* bad, cudaStream_t st);
 cudaError_t launch_scatter_xyz(float4* dst, float4* dst2, const uint32_t* o2n, uint32_t v0, uint32_t nv,
-                               const float* in, cudaStream_t st);
+                               const float* in, cudaStream_t st, const int* skip = nullptr);
 // Wavefront variant of the frame kernel: every CTA owns the tets of one
 // region of the mesh (s.wave_start / s.wave_idx) in every colour and, instead
 // of a grid barrier per colour, waits until the CTAs it shares vertices with

@@ -293,8 +293,15 @@ def test_invalid_arguments(capi_mod):
     assert L.sbs_gpu_pin_vertices(h, 5, tets, 1) == capi_mod.SBS_EINVAL
     assert L.sbs_gpu_finalize(h) == capi_mod.SBS_OK
     assert L.sbs_gpu_step(h, -1.0, 1, 1) == capi_mod.SBS_EINVAL
+    xs, vs = np.zeros(12, np.float32), np.zeros(12, np.float32)
+    assert L.sbs_gpu_get_state(h, 0, xs.ctypes.data, vs.ctypes.data) == capi_mod.SBS_OK
     xbad = np.full(12, np.nan, np.float32)
-    assert L.sbs_gpu_set_state(h, 0, xbad.ctypes.data, None) == capi_mod.SBS_EINVAL
+    vnew = np.ones(12, np.float32)
+    assert L.sbs_gpu_set_state(h, 0, xbad.ctypes.data, vnew.ctypes.data) == capi_mod.SBS_EINVAL
+    # a rejected call leaves positions and velocities as they were
+    x2, v2 = np.zeros(12, np.float32), np.zeros(12, np.float32)
+    assert L.sbs_gpu_get_state(h, 0, x2.ctypes.data, v2.ctypes.data) == capi_mod.SBS_OK
+    assert np.array_equal(xs, x2) and np.array_equal(vs, v2)
     assert L.sbs_gpu_destroy(h) == capi_mod.SBS_OK
 
 
