@@ -377,3 +377,28 @@ def test_cluster_staging_is_exact(capi_mod, make):
     b.step(3)
     assert np.array_equal(a.positions(), b.positions())
     assert np.array_equal(a.velocities(), b.velocities())
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_small_colour_merge_is_exact(capi_mod, mode):
+    """A colour run across the grid or, among the merged small colours, by one
+    CTA after the others: the merge threshold the autotuner picks does not
+    change results.  The graph mode's two kernels agree to the bit; in the
+    persistent kernel the tail phase inlines the projection at another site,
+    where the compiler contracts multiply-adds differently, so one iteration
+    agrees to a few ulps (which the sequential loop then amplifies, as any
+    rounding difference)."""
+    sc = scenes.beam_c1()
+    a = capi_mod.Solver(sc, exec_mode=mode, tail_threshold=0)        # every colour across the grid
+    b = capi_mod.Solver(sc, exec_mode=mode, tail_threshold=1 << 20)  # every colour in the one-CTA tail
+    assert a.stats().n_tail_colours == 0
+    assert b.stats().n_tail_colours == b.stats().n_colours
+    if mode == 1:
+        a.step(3)
+        b.step(3)
+        assert np.array_equal(a.positions(), b.positions())
+        assert np.array_equal(a.velocities(), b.velocities())
+    else:
+        a.step(1, iterations=1)
+        b.step(1, iterations=1)
+        assert np.abs(a.positions() - b.positions()).max() < 1e-6 * sc.bbox_diag()
