@@ -44,7 +44,9 @@ struct GemmArgs {
     __nv_bfloat16* Cb;    // optional BF16 copy of C (pre-activation), ld = ldc
     __nv_bfloat16* Act;   // optional BF16 SiLU(C), ld = ldc
     int M, N, K;
-    int splitk;           // > 1: blockIdx.z takes a K slice and atomically adds into C (pre-zeroed)
+    int splitk;           // > 1: blockIdx.z takes a K slice and writes its partial product
+                          // to ws[z][M x N]; k_splitk_sum then adds the slices in order
+    float* ws;
 };
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
                 float v = acc[i][j][r];
                 float* cp = g.C + m * g.ldc + n;
                 if (g.splitk > 1) {
-                    atomicAdd(cp, v);
+                    g.ws[(size_t)blockIdx.z * g.M * g.N + (size_t)m * g.N + n] = v;
                     continue;
                 }
                 if (g.beta != 0.0f) v += g.beta * *cp;
@@ -134,10 +136,27 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
             }
 }
 
+// C[i] = sum over the K slices z = 0, 1, ... of ws[z][i], always in that
+// order: split-K products come out the same bit for bit on every run (an
+// atomic accumulation would add the slices in whatever order they finish).
+__global__ void k_splitk_sum(const float* __restrict__ ws, float* __restrict__ C, int mn, int splitk) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < mn; i += gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int z = 0; z < splitk; ++z) s += ws[(size_t)z * mn + i];
+        C[i] = s;
+    }
+}
+
 static cudaError_t gemm(const GemmArgs& g, cudaStream_t st) {
     dim3 grid((g.N + GN - 1) / GN, (g.M + GM - 1) / GM, g.splitk > 1 ? g.splitk : 1);
     k_gemm<<<grid, 128, 0, st>>>(g);
     count_launch();
+    if (g.splitk > 1) {
+        // the slices' sum into C (ldc == N for the split-K products)
+        const int mn = g.M * g.N;
+        k_splitk_sum<<<(mn + 255) / 256, 256, 0, st>>>(g.ws, g.C, mn, g.splitk);
+        count_launch();
+    }
     return cudaGetLastError();
 }
 
@@ -292,10 +311,8 @@ cudaError_t mlp_backward_dev(MlpDev& d, const float* x, const float* t, int n, c
         g.B = act; g.sbk = fin[l]; g.sbn = 1;           // B(k=r, n=i) = act[r][i]
         g.C = d.grad + d.woff[l]; g.ldc = fin[l]; g.beta = 0.0f;
         g.M = fout[l]; g.N = fin[l]; g.K = n;
-        g.splitk = std::max(1, std::min(256, n / 1024));
-        if (g.splitk > 1 &&
-            (e = cudaMemsetAsync(g.C, 0, sizeof(float) * (size_t)fout[l] * fin[l], st)) != cudaSuccess)
-            return e;
+        g.splitk = std::max(1, std::min(kMaxSplitK, n / 1024));
+        g.ws = d.splitk_ws;
         if ((e = gemm(g, st)) != cudaSuccess) return e;
         k_colsum<<<fout[l], 256, 0, st>>>(d.dz[l], d.grad + d.boff[l], n, fout[l]);
         count_launch();

@@ -113,6 +113,7 @@ sbs_status sbs_mlp_create(int32_t device, uint64_t seed, sbs_mlp** out) {
     };
     A((void**)&d.w, kParams * sizeof(float));
     A((void**)&d.grad, kParams * sizeof(float));
+    A((void**)&d.splitk_ws, (size_t)kMaxSplitK * kHid * kHid * sizeof(float));
     A((void**)&d.m1, kParams * sizeof(float));
     A((void**)&d.m2, kParams * sizeof(float));
     A((void**)&d.wball, kParams * sizeof(__nv_bfloat16));

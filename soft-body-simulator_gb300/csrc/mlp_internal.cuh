@@ -47,7 +47,11 @@ struct MlpDev {
     uint32_t n_data = 0;
     int* tc_err = nullptr;     // error flag of the fused inference kernel
     int n_sm = 0;
+    float* splitk_ws = nullptr;   // [kMaxSplitK][kHid x kHid] partial weight gradients
 };
+
+// K slices of a split-K weight-gradient product at most
+constexpr int kMaxSplitK = 256;
 
 cudaError_t mlp_reserve(MlpDev& d, int n);
 cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cudaStream_t st);

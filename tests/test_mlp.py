@@ -92,3 +92,20 @@ def test_gpu_adam_training_reduces_loss(capi_mod):
     m.train(400, 8192, 1e-3, seed=1)
     l1, _ = m.loss_grad(x[:8192], t[:8192])
     assert l1 < 0.2 * l0
+
+
+@pytest.mark.gpu
+def test_gpu_training_is_reproducible(capi_mod):
+    """Two trainings from the same seeds end with identical parameters: the
+    split-K weight gradients add their K slices in a fixed order."""
+    x, t = data(40000, seed=6)
+    mean, std, scale = norm_of(x, t)
+    out = []
+    for _ in range(2):
+        m = capi_mod.Mlp(seed=7)
+        m.set_normalization(mean, std, scale)
+        m.set_dataset(x, t)
+        m.train(50, 32768, 1e-3, seed=3)    # batches large enough to split K
+        out.append(m.params())
+        m.close()
+    assert np.array_equal(out[0], out[1])
