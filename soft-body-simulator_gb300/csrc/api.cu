@@ -2126,6 +2126,7 @@ static sbs_status warm_prepare(sbs_gpu* h) {
     if ((s = dalloc(h, &h->wd.xpred, V)) != SBS_OK) return s;
     if ((s = dalloc(h, &h->wd.inc_start, V + 1)) != SBS_OK) return s;
     if ((s = dalloc(h, &h->wd.inc, 4ull * T)) != SBS_OK) return s;
+    if ((s = dalloc(h, &h->wd.tet_f, 3ull * T)) != SBS_OK) return s;
     if ((s = upload(h, h->wd.inc_start, cnt.data(), (V + 1) * 4)) != SBS_OK) return s;
     if ((s = upload(h, h->wd.inc, inc.data(), 4ull * T * 4)) != SBS_OK) return s;
     CU(h, cudaStreamSynchronize(h->st));

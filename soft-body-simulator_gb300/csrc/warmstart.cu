@@ -31,6 +31,20 @@ namespace sbs {
 // dprev_valid: w.xpred holds the prediction of the substep that produced the
 // current x (features ran on it and the state was not replaced since), so
 // x - w.xpred is that substep's solve displacement.
+// Deformation gradient of every tet at the predicted positions, row-major in
+// three float4 (each tet once, instead of once per incident vertex).
+__global__ void k_tet_f(SceneDev s, WarmDev w) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < s.n_tets; t += gridDim.x * blockDim.x) {
+        const uint4 id = s.tet[t];
+        const f3 x3 = mk(s.xi[id.w]);
+        const f3 d1 = mk(s.xi[id.x]) - x3, d2 = mk(s.xi[id.y]) - x3, d3 = mk(s.xi[id.z]) - x3;
+        const m3 Fm = deformation(d1, d2, d3, mk(s.dm0[t]), mk(s.dm1[t]), mk(s.dm2[t]));
+        w.tet_f[3ull * t] = make_float4(Fm.c0.x, Fm.c1.x, Fm.c2.x, 0.0f);
+        w.tet_f[3ull * t + 1] = make_float4(Fm.c0.y, Fm.c1.y, Fm.c2.y, 0.0f);
+        w.tet_f[3ull * t + 2] = make_float4(Fm.c0.z, Fm.c1.z, Fm.c2.z, 0.0f);
+    }
+}
+
 __global__ void k_features(SceneDev s, WarmDev w, StepParams p, int dprev_valid) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < s.n_verts; v += gridDim.x * blockDim.x) {
         const float4 xp = s.xi[v], x = s.xn[v];
@@ -46,17 +60,15 @@ __global__ void k_features(SceneDev s, WarmDev w, StepParams p, int dprev_valid)
         } else {
             f[3] = f[4] = f[5] = 0.0f;
         }
+        // mean of the incident tets' gradients (k_tet_f), in incidence order
         float F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         const uint32_t b = w.inc_start[v], e = w.inc_start[v + 1];
         for (uint32_t k = b; k < e; ++k) {
             const uint32_t t = w.inc[k];
-            const uint4 id = s.tet[t];
-            const f3 x3 = mk(s.xi[id.w]);
-            const f3 d1 = mk(s.xi[id.x]) - x3, d2 = mk(s.xi[id.y]) - x3, d3 = mk(s.xi[id.z]) - x3;
-            const m3 Fm = deformation(d1, d2, d3, mk(s.dm0[t]), mk(s.dm1[t]), mk(s.dm2[t]));
-            F[0] += Fm.c0.x; F[1] += Fm.c1.x; F[2] += Fm.c2.x;
-            F[3] += Fm.c0.y; F[4] += Fm.c1.y; F[5] += Fm.c2.y;
-            F[6] += Fm.c0.z; F[7] += Fm.c1.z; F[8] += Fm.c2.z;
+            const float4 r0 = w.tet_f[3ull * t], r1 = w.tet_f[3ull * t + 1], r2 = w.tet_f[3ull * t + 2];
+            F[0] += r0.x; F[1] += r0.y; F[2] += r0.z;
+            F[3] += r1.x; F[4] += r1.y; F[5] += r1.z;
+            F[6] += r2.x; F[7] += r2.y; F[8] += r2.z;
         }
         const float inv = e > b ? 1.0f / (float)(e - b) : 0.0f;
         for (int i = 0; i < 9; ++i) F[i] *= inv;
@@ -208,6 +220,9 @@ cudaError_t launch_carry(const SceneDev& s, const WarmDev& w, cudaStream_t st) {
 
 cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParams& p, int dprev_valid,
                             cudaStream_t st) {
+    const int tgrid = (int)std::min<uint32_t>(4096, (s.n_tets + 255) / 256);
+    k_tet_f<<<tgrid > 0 ? tgrid : 1, 256, 0, st>>>(s, w);
+    count_launch();
     const int grid = (int)std::min<uint32_t>(4096, (s.n_verts + 255) / 256);
     k_features<<<grid > 0 ? grid : 1, 256, 0, st>>>(s, w, p, dprev_valid);
     count_launch();

@@ -16,6 +16,7 @@ struct WarmDev {
     float4* xpred;        // [V] predicted positions of the last substep that computed features
     uint32_t* inc_start;  // [V + 1] CSR of incident tet slots
     uint32_t* inc;        // [4T]
+    float4* tet_f;        // [3T] deformation gradient of each tet at x_pred (rows, .w unused)
 };
 
 cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParams& p, int dprev_valid,
