@@ -71,7 +71,9 @@ typedef struct sbs_gpu_params {
     int32_t exec_mode;            /* sbs_exec_mode */
     int32_t block_size;           /* threads per CTA of the projection kernels (0: auto) */
     int32_t ctas_per_sm;          /* persistent mode CTAs per SM (0: auto) */
-    int32_t tail_threshold;       /* colours with <= this many tets run in one CTA (-1: auto) */
+    int32_t tail_threshold;       /* colours with <= this many tets run in one CTA (-1: the block
+                                     size, then timed against 0 / 256 / 1024 / 4096 by the
+                                     SBS_EXEC_AUTO autotuner) */
     int32_t body_contacts;        /* 0 off; 1 vertex-in-tet contacts between bodies (spatial
                                      hash); 2 also within a body (self contacts) */
     float hash_cell;              /* spatial hash cell size in metres (0: 2 x mean edge length) */
