@@ -13,10 +13,12 @@ per 1/60 s frame), i.e. 11,796,480 tet projections.
            (sbs_gpu_set_state), steps, and reads them back (sbs_gpu_get_state).
   roofline the frame kernel's algorithmic bytes per launch / its event time.
   cpu_baseline  the FP64 CPU oracle (a restatement of the reference's
-           sequential loop, same sweep) on a bounded sample, single thread.
+           sequential loop) on a bounded sample, single thread, tet list order.
 
---impl reference times that CPU restatement with every host thread (colour-
-parallel sweep, bit-identical to the sequential one) on the same workload.
+--impl reference times that CPU restatement with every host thread on the
+same workload: the oracle plans its own colours (first-fit in list order) and
+projects each colour's vertex-disjoint tets in parallel; the CUDA library is
+not loaded in that arm.
 Several GPUs (torchrun) run independent replicas: the beam does not shard.
 """
 from __future__ import annotations
@@ -57,8 +59,8 @@ MATERIALS = {
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch (one launch = one
-# frame for these kernels), from profiles/k_cluster_frame_beam98k.md and
-# profiles/k_frame_block2m.md
+# frame for these kernels), from one ncu capture of the same workload and
+# execution mode
 TRAFFIC = {
     ("beam-98304-snh-twist", "k_cluster_frame"): 7.01e6,
     ("block-2621440-snh", "k_frame_t<false>"): 22.876e9 + 2.582e9,
@@ -183,35 +185,42 @@ def dist_env():
     return world, rank, local
 
 
-def cpu_baseline_sample(scene, budget: int, threads: int):
+def cpu_baseline_sample(scene, budget: int, threads: int, sequential: bool = False):
     """Times the FP64 oracle on a bounded sample of the workload; returns
-    (projections/s, seconds, projections, description)."""
+    (projections/s, seconds, projections, description).  sequential: the
+    reference's own order (tet list order, one constraint after another);
+    otherwise the oracle's own colour-major plan, run colour-parallel on
+    `threads` threads."""
     from oracle import oracle
-    from sbs_gb300 import capi
     sub, frames, desc = bounded_sample(scene, budget)
-    order, offsets = capi.plan_sweep(sub)
     o = oracle.Oracle(sub, threads=threads)
-    o.set_order(order, offsets)
+    if not sequential:
+        o.set_order(*o.plan_colours())
     secs = o.time_frames(frames)
     proj = frames * sub.substeps * sub.iterations * sub.n_tets
     return proj / secs, secs, proj, desc
 
 
 def run_reference(args):
+    """The reference's CPU path (the FP64 oracle, which restates it; the CUDA
+    library is never loaded here) on every host thread: the oracle plans its
+    own colours (first-fit in list order) and projects each colour's
+    vertex-disjoint tets in parallel, which gives the same result as the
+    sequential sweep over that order.  The line also carries the single-thread
+    sequential figure in list order, the reference's own structure."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
     scene = workload(args.workload)
     threads = os.cpu_count() or 1
     from oracle import oracle
-    from sbs_gb300 import capi
     # each step: one frame, or a bounded part of one for the large workloads
     sub, _, desc = bounded_sample(scene, 40_000_000)
     if sub is scene:
         desc = f"one frame of {scene.name}"
     per_step = sub.substeps * sub.iterations * sub.n_tets
-    order, offsets = capi.plan_sweep(sub)
     o = oracle.Oracle(sub, threads=threads)
+    order, offsets = o.plan_colours()
     o.set_order(order, offsets)
     for _ in range(args.warmup):
         o.step(1, fast=True)
@@ -220,6 +229,14 @@ def run_reference(args):
         o.step(1, fast=True)
     secs = time.perf_counter() - t0
     value = per_step * args.steps / secs
+    seq_val, seq_s, seq_proj, seq_desc = cpu_baseline_sample(scene, args.cpu_budget, 1, sequential=True)
+    loaded = []
+    try:
+        with open("/proc/self/maps") as f:
+            loaded = sorted({ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")
+                             and str(ROOT) in ln})
+    except OSError:
+        pass
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -228,8 +245,13 @@ def run_reference(args):
         "config": {"workload": scene.name, "tets": scene.n_tets, "vertices": scene.n_verts,
                    "substeps": scene.substeps, "iterations": scene.iterations},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} steps, each {desc}, "
-                                   f"colour-parallel sweep (bit-identical to the sequential reference order)"},
+                         "sample": f"{args.steps} steps, each {desc}; the oracle's own first-fit "
+                                   f"colouring ({len(offsets) - 1} colours), colour-parallel on "
+                                   f"{threads} threads"},
+        "single_thread": {"value": seq_val, "unit": UNIT, "cores": 1, "kind": "port",
+                          "sample": f"{seq_desc} ({seq_proj} tet projections), sequential sweep in "
+                                    f"tet list order, {seq_s:.1f} s"},
+        "libraries_loaded": loaded,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -336,10 +358,10 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline:
-        cpu_val, cpu_s, cpu_proj, cpu_desc = cpu_baseline_sample(scene, args.cpu_budget, 1)
+        cpu_val, cpu_s, cpu_proj, cpu_desc = cpu_baseline_sample(scene, args.cpu_budget, 1, sequential=True)
         cpu = {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"{cpu_desc} ({cpu_proj} tet projections) on the FP64 oracle, single thread, "
-                         f"{cpu_s:.1f} s"}
+                         f"sequential sweep in tet list order, {cpu_s:.1f} s"}
 
     st = solver.stats()
     footprint = scene_bytes(scene)
@@ -347,7 +369,7 @@ def main():
     kernel = {capi.EXEC_PERSISTENT: "k_frame_t<false>", capi.EXEC_CLUSTER: "k_cluster_frame",
               capi.EXEC_WAVEFRONT: "k_frame_t<true>"}.get(st.exec_mode, "k_colour")
     # DRAM bytes (read + write) per launch of the dominant kernel from one ncu
-    # capture of the same workload and mode (summaries under profiles/)
+    # capture of the same workload and mode
     traffic = TRAFFIC.get((scene.name, kernel))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

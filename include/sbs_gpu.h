@@ -332,12 +332,17 @@ sbs_status sbs_gpu_plan_sweep(const double* x0, uint32_t n_verts, const uint32_t
  * All pointers are DEVICE pointers: x [3*n_verts] float positions,
  * surface [n_surface] vertex ids, contact_verts [n_surface] and
  * contact_points [3*n_surface] outputs (contacts in the order of `surface`),
- * count [1] output.  n_surface <= 1,048,576 (SBS_EINVAL beyond).  Enqueued on
- * `stream` (a cudaStream_t; NULL for the default stream), asynchronous.
- * Working memory is a 32 KB static device array shared by every call on a
- * device: calls that overlap on the GPU race; the first call on a device
- * looks the array up (cudaGetSymbolAddress), so make that first call outside
- * any stream capture.  Allocates nothing. */
+ * count [1] output.  n_surface <= 1,048,576 (SBS_EINVAL beyond).  Surface
+ * ids >= n_verts are skipped (never read, never reported), so with such ids
+ * the count can be lower than the solver's.  Enqueued on `stream` (a
+ * cudaStream_t; NULL for the default stream), asynchronous.  A CUDA error
+ * already pending on the calling thread is returned as SBS_ECUDA before
+ * anything is enqueued.  Working memory is a 32 KB static device array
+ * shared by every call on a device: calls that overlap on the GPU race; the
+ * first call on a device looks the array up (cudaGetSymbolAddress) and keeps
+ * the address, so make that first call outside any stream capture, and do
+ * not use this call after a cudaDeviceReset in the same process.  Allocates
+ * nothing. */
 sbs_status sbs_gpu_plane_contacts_noalloc(const float* x, uint32_t n_verts, const uint32_t* surface,
                                           uint32_t n_surface, const double normal[3], double d,
                                           uint32_t* contact_verts, float* contact_points, uint32_t* count,

@@ -52,6 +52,8 @@ def lib():
         L.orc_add_ground_plane.argtypes = [P, dp, D]
         L.orc_add_sdf_grid.argtypes = [P, C.c_void_p, up, dp, dp]
         L.orc_set_tet_order.restype = I
+        L.orc_plan_colours.restype = U32
+        L.orc_plan_colours.argtypes = [P, up, up, U32]
         L.orc_set_tet_order.argtypes = [P, up, U32, C.c_void_p, U32]
         L.orc_step.argtypes = [P, D, U32, U32]
         L.orc_step_fast.argtypes = [P, D, U32, U32]
@@ -182,6 +184,17 @@ class Oracle:
                                           off.ctypes.data, len(off) - 1)
         if rc:
             raise ValueError("bad tet order")
+
+    def plan_colours(self):
+        """The oracle's own colour-parallel plan (first-fit colouring in list
+        order, colour-major): (order, offsets), without the CUDA library."""
+        order = np.zeros(self.n_tets, np.uint32)
+        cap = 4096
+        offsets = np.zeros(cap, np.uint32)
+        n = self.L.orc_plan_colours(self.h, order, offsets, cap)
+        if n == 0 and self.n_tets:
+            raise ValueError("more than 4095 colours")
+        return order, offsets[: n + 1].copy()
 
     def set_edge_order(self, order: np.ndarray, offsets: np.ndarray | None = None):
         """Projection order (input indices, colour-major) of the distance

@@ -1003,6 +1003,47 @@ int orc_set_tet_order(void* h, const uint32_t* order, uint32_t n, const uint32_t
     return 0;
 }
 
+// The oracle's own colour-parallel plan, independent of the CUDA library:
+// first-fit colouring of the tets in list order (each tet takes the lowest
+// colour none of its four vertices has yet), then the list colour-major with
+// list order kept inside a colour.  Tets of one colour share no vertex, so a
+// colour's projections commute and the colour-parallel sweep over this order
+// equals the sequential sweep over it.  Writes order [n_tets] and offsets
+// [n_colours + 1] (cap_offsets entries available); returns n_colours, or 0
+// when cap_offsets is too small.
+uint32_t orc_plan_colours(void* h, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets) {
+    sim_t& s = *(sim_t*)h;
+    const size_t nt = s.topo.size();
+    std::vector<std::vector<uint64_t>> used(s.particles.size());   // per vertex: colour bit words
+    std::vector<uint32_t> colour(nt);
+    uint32_t n_colours = 0;
+    for (size_t t = 0; t < nt; ++t) {
+        const uint32_t* v = s.topo[t].v;
+        uint32_t c = 0;
+        for (;; ++c) {
+            const size_t w = c >> 6;
+            const uint64_t bit = 1ull << (c & 63);
+            bool taken = false;
+            for (int k = 0; k < 4 && !taken; ++k) taken = w < used[v[k]].size() && (used[v[k]][w] & bit);
+            if (!taken) break;
+        }
+        colour[t] = c;
+        for (int k = 0; k < 4; ++k) {
+            auto& u = used[v[k]];
+            if (u.size() <= (c >> 6)) u.resize((c >> 6) + 1, 0);
+            u[c >> 6] |= 1ull << (c & 63);
+        }
+        n_colours = std::max(n_colours, c + 1);
+    }
+    if (cap_offsets < n_colours + 1) return 0;
+    std::vector<uint32_t> count(n_colours + 1, 0);
+    for (size_t t = 0; t < nt; ++t) ++count[colour[t] + 1];
+    for (uint32_t c = 0; c < n_colours; ++c) count[c + 1] += count[c];
+    for (uint32_t c = 0; c <= n_colours; ++c) offsets[c] = count[c];
+    for (size_t t = 0; t < nt; ++t) order[count[colour[t]]++] = (uint32_t)t;
+    return n_colours;
+}
+
 // distance_constraint_t objects (distance_constraint.cpp:8-22) for n 4-tuples
 // (b1, b2, v1, v2), as the reference's constructor takes them.
 int orc_add_distance(void* h, const uint32_t* ids, uint32_t n, double alpha, double beta) {

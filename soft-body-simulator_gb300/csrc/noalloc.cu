@@ -119,7 +119,10 @@ std::mutex g_na_mutex;
 uint32_t* g_na_ptr[256] = {};
 
 // Device address of the scratch array on the current device, looked up once
-// per device (the name is only a host-side stand-in for it).
+// per device (the name is only a host-side stand-in for it).  The cached
+// address belongs to the device's context of that moment: after a
+// cudaDeviceReset in the same process it is stale, so the entry point must
+// not be used after one.
 sbs_status na_scratch(uint32_t** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return SBS_ECUDA;
@@ -143,6 +146,9 @@ extern "C" sbs_status sbs_gpu_plane_contacts_noalloc(const float* x, uint32_t n_
     if (n_surface > kNaMaxSurface) return SBS_EINVAL;  // more than 1,048,576 surface vertices
     const double l = sqrt(normal[0] * normal[0] + normal[1] * normal[1] + normal[2] * normal[2]);
     if (!(l > 0.0) || !(d == d)) return SBS_EINVAL;
+    // An error left by earlier work on this thread is not this call's: report
+    // it without clearing it and enqueue nothing.
+    if (cudaPeekAtLastError() != cudaSuccess) return SBS_ECUDA;
     uint32_t* scratch = nullptr;
     sbs_status st = na_scratch(&scratch);
     if (st != SBS_OK) return st;
@@ -150,7 +156,9 @@ extern "C" sbs_status sbs_gpu_plane_contacts_noalloc(const float* x, uint32_t n_
     const PlaneF p{(float)(normal[0] / l), (float)(normal[1] / l), (float)(normal[2] / l), (float)(d / l)};
     const uint32_t nb = n_surface == 0 ? 1 : (n_surface + kNaBlock - 1) / kNaBlock;
     k_na_count<<<nb, kNaBlock, 0, s>>>(x, surface, n_surface, n_verts, p, scratch);
+    if (cudaGetLastError() != cudaSuccess) return SBS_ECUDA;
     k_na_scan<<<1, 1024, 0, s>>>(scratch, nb, count);
+    if (cudaGetLastError() != cudaSuccess) return SBS_ECUDA;
     k_na_write<<<nb, kNaBlock, 0, s>>>(x, surface, n_surface, n_verts, p, scratch, contact_verts, contact_points);
     return cudaGetLastError() == cudaSuccess ? SBS_OK : SBS_ECUDA;
 }
