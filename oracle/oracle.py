@@ -306,6 +306,21 @@ def hash_candidates(o: "Oracle", xf: np.ndarray, cell: float, self_contacts: boo
     return out
 
 
+def nudged_oracle(scene, order=None, offsets=None, seed: int = 0, threads: int = 1) -> "Oracle":
+    """An oracle whose initial positions are rounded to FP32 and then moved
+    one ulp up or down per coordinate (seeded): the smallest perturbation an
+    FP32 implementation makes to the initial state."""
+    b = Oracle(scene, threads=threads)
+    if order is not None:
+        b.set_order(order, offsets)
+    x = b.get()
+    rng = np.random.default_rng(seed)
+    x32 = x.astype(np.float32)
+    toward = np.where(rng.random(x.shape) < 0.5, -np.inf, np.inf).astype(np.float32)
+    b.set(FIELD_X, np.nextafter(x32, toward).astype(np.float64))
+    return b
+
+
 def noise_floor(scene, frames: int, order=None, offsets=None, seed: int = 0, threads: int = 1) -> float:
     """Max position deviation after `frames` between the oracle and the
     oracle restarted from FP32-rounded initial positions nudged by one ulp.
@@ -313,15 +328,9 @@ def noise_floor(scene, frames: int, order=None, offsets=None, seed: int = 0, thr
     loop, the yardstick for multi-frame FP32-vs-FP64 comparisons.  `threads`
     > 1 runs the colour-parallel sweep, bit-identical to the sequential one."""
     a = Oracle(scene, threads=threads)
-    b = Oracle(scene, threads=threads)
     if order is not None:
         a.set_order(order, offsets)
-        b.set_order(order, offsets)
-    x = b.get()
-    rng = np.random.default_rng(seed)
-    x32 = x.astype(np.float32)
-    toward = np.where(rng.random(x.shape) < 0.5, -np.inf, np.inf).astype(np.float32)
-    b.set(FIELD_X, np.nextafter(x32, toward).astype(np.float64))
+    b = nudged_oracle(scene, order, offsets, seed, threads)
     a.step(frames)
     b.step(frames)
     return float(np.abs(a.get() - b.get()).max())

@@ -402,3 +402,32 @@ def test_small_colour_merge_is_exact(capi_mod, mode):
         a.step(1, iterations=1)
         b.step(1, iterations=1)
         assert np.abs(a.positions() - b.positions()).max() < 1e-6 * sc.bbox_diag()
+
+
+@pytest.mark.parametrize("kind", ["uniaxial", "compressed", "shear", "general"])
+def test_snh_kernel_against_closed_form_stress(capi_mod, kind):
+    """The GPU's stable Neo-Hookean projection against the closed-form
+    Neo-Hookean stress (Macklin & Mueller 2021), independent of the oracle:
+    one projection from zero multipliers moves vertex i by w dt^2 f_i (1 - c w
+    + O(w^2)); two vertex masses m and 2m (Richardson) remove the O(w) term.
+    FP32 positions limit the comparison to ~1e-3 of the largest force."""
+    from test_oracle import REST, SNH_KAT_F, snh_closed_form_forces
+    E, nu, dt = 1e5, 0.3, 1 / 60
+    xrest = REST.copy()
+    x = (xrest - xrest[3]) @ SNH_KAT_F[kind].T + xrest[3]
+    f = snh_closed_form_forces(xrest, x, E, nu)
+    scaled = []
+    for m in (60.0, 120.0):
+        b = scenes.Body(x0=xrest, tets=np.array([[0, 1, 2, 3]], np.uint32), model=scenes.MODEL_SNH, young=E,
+                        poisson=nu, density=1000.0, x_init=x, mass=np.full(4, m))
+        sc = scenes.Scene("one", [b], dt, 1, 1, 1, gravity=(0.0, 0.0, 0.0), ground=None)
+        g = capi_mod.Solver(sc)
+        xf = x.astype(np.float32)
+        g.set_predicted(0, xf)
+        g.solve(dt, 1)
+        dx = g.get_predicted(0).astype(np.float64) - xf.astype(np.float64)
+        g.close()
+        scaled.append(dx * m / dt ** 2)
+    extrapolated = 2 * scaled[1] - scaled[0]
+    assert np.abs(scaled[1] - f).max() < 0.05 * np.abs(f).max()      # first order already close
+    assert np.abs(extrapolated - f).max() < 3e-3 * np.abs(f).max()

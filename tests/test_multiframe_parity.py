@@ -1,0 +1,78 @@
+"""Whole-run parity: the GPU's FP32 trajectory against the FP64 oracle
+replaying the GPU's sweep order, frame by frame, for the 450-tet cantilever
+(all 120 frames of the configuration) and the 98,304-tet twisting beam (the
+first 30 of its 300 frames).
+
+The sequential Gauss-Seidel loop amplifies rounding differences by x3-30 per
+sweep (test_oracle.py measures it), so no FP32 run can stay within a fixed
+bound of the FP64 trajectory over a whole run.  The yardstick at every frame
+is the loop's own FP32 noise floor: the largest deviation, from the oracle,
+of two oracles restarted from FP32-rounded initial positions nudged by one
+ulp (two seeds).  The GPU must stay within 2x of that floor at every frame:
+its arithmetic is FP32 throughout, yet its trajectory must be no further
+from the FP64 one than FP32 rounding of the initial state alone carries the
+loop.  Run with -s for the per-frame table (error / bounding-box diagonal).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import make_pair
+from sbs_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+RATIO = 2.0
+
+
+def per_frame_errors(scene, frames, capi, oracle, threads, seeds=(0, 1)):
+    g, o = make_pair(scene, capi, oracle)
+    order, off = g.tet_order()
+    o.L.orc_set_threads(o.h, threads)
+    nudged = [oracle.nudged_oracle(scene, order, off, s, threads) for s in seeds]
+    diag = scene.bbox_diag()
+    rows = []
+    for f in range(1, frames + 1):
+        g.step(1)
+        o.step(1)
+        for b in nudged:
+            b.step(1)
+        xo = o.get()
+        x = g.positions()
+        assert np.all(np.isfinite(x)), f"frame {f}: non-finite GPU state"
+        err = float(np.abs(x - xo).max()) / diag
+        floor = max(float(np.abs(b.get() - xo).max()) for b in nudged) / diag
+        rows.append((f, err, floor))
+    g.close()
+    return rows
+
+
+def report(name, rows, every):
+    print(f"\n{name}: frame, GPU vs FP64 oracle (x diag), FP32 noise floor (x diag), ratio")
+    for f, e, fl in rows:
+        if f % every == 0 or f == 1:
+            print(f"  {f:4d}  {e:.3e}  {fl:.3e}  {e / max(fl, 1e-30):.2f}")
+    worst = max(rows, key=lambda r: r[1] / max(r[2], 1e-30))
+    print(f"  worst ratio {worst[1] / max(worst[2], 1e-30):.2f} at frame {worst[0]}; "
+          f"max error {max(r[1] for r in rows):.3e}")
+
+
+def check(rows, abs_floor):
+    for f, e, fl in rows:
+        assert e <= RATIO * fl + abs_floor, f"frame {f}: GPU error {e:.3e} x diag, noise floor {fl:.3e}"
+
+
+def test_cantilever_all_frames(capi_mod, oracle_mod):
+    sc = scenes.beam_c1()                      # 120 frames, 10 iterations, StVK
+    rows = per_frame_errors(sc, sc.frames, capi_mod, oracle_mod, threads=1)
+    report(sc.name, rows, 10)
+    check(rows, 1e-7)
+
+
+def test_twisting_beam_first_30_frames(capi_mod, oracle_mod):
+    sc = scenes.beam_twist()
+    threads = max(1, min(16, os.cpu_count() or 1))
+    rows = per_frame_errors(sc, 30, capi_mod, oracle_mod, threads=threads)
+    report(sc.name, rows, 5)
+    check(rows, 1e-7)

@@ -99,6 +99,57 @@ def test_snh_single_tet_stays_at_rest(oracle_mod):
     assert np.abs(o.get() - REST).max() < 1e-15
 
 
+def snh_closed_form_forces(xrest, x, E, nu):
+    """Nodal elastic forces of one tet under the stable Neo-Hookean energy of
+    Macklin & Mueller 2021, psi = mu/2 (tr(F^T F) - 3) + lam/2 (det F - a)^2
+    with a = 1 + mu/lam, from its closed-form first Piola stress
+    P = mu F + lam (det F - a) cof(F):  f_i = -|V0| (P Dm^-T) e_i for the
+    first three vertices, f_4 = -(f_1 + f_2 + f_3).  Nothing here uses the
+    solver's constraint split (C_D = |F|, C_H = det F - a) or its 2x2 solve."""
+    mu = E / (2 * (1 + nu))
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    Dm = np.stack([xrest[i] - xrest[3] for i in range(3)], axis=1)
+    Ds = np.stack([x[i] - x[3] for i in range(3)], axis=1)
+    F = Ds @ np.linalg.inv(Dm)
+    cof = np.stack([np.cross(F[:, 1], F[:, 2]), np.cross(F[:, 2], F[:, 0]), np.cross(F[:, 0], F[:, 1])], axis=1)
+    P = mu * F + lam * (np.linalg.det(F) - (1 + mu / lam)) * cof
+    H = -abs(np.linalg.det(Dm) / 6) * P @ np.linalg.inv(Dm).T
+    return np.vstack([H.T, -H.sum(axis=1)])
+
+
+SNH_KAT_F = {
+    "uniaxial": np.diag([1.2, 0.95, 0.95]),
+    "compressed": np.diag([0.85, 1.03, 1.04]),
+    "shear": np.array([[1.0, 0.25, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]]),
+    "general": np.array([[1.1, 0.1, -0.05], [0.03, 0.92, 0.12], [-0.08, 0.02, 1.05]]),
+}
+
+
+@pytest.mark.parametrize("kind", list(SNH_KAT_F))
+def test_snh_projection_against_closed_form_stress(oracle_mod, kind):
+    """Known answer for the stable Neo-Hookean constraint pair: with heavy
+    vertices (w -> 0) one projection from zero multipliers moves vertex i by
+    w dt^2 f_i, f_i the elastic force of the closed-form Neo-Hookean stress
+    (XPBD: dlambda_j -> -C_j / alpha~_j, dx_i = w sum_j grad_i C_j dlambda_j
+    = -w dt^2 grad_i U).  This pins the constraint formulation (shared by the
+    oracle and the GPU kernels) to the published energy."""
+    E, nu = 1e5, 0.3
+    xrest = REST + np.array([0.3, -0.2, 0.1])
+    x = (xrest - xrest[3]) @ SNH_KAT_F[kind].T + xrest[3]
+    m = 1e7                                    # w = 1e-7: the O(w) correction is ~1e-7 relative
+    b = scenes.Body(x0=xrest, tets=np.array([[0, 1, 2, 3]], np.uint32), model=scenes.MODEL_SNH, young=E,
+                    poisson=nu, density=1000.0, x_init=x, mass=np.full(4, m))
+    dt = 1 / 60
+    sc = scenes.Scene("one", [b], dt, 1, 1, 1, gravity=(0.0, 0.0, 0.0), ground=None)
+    o = oracle_mod.Oracle(sc)
+    o.set(oracle_mod.FIELD_XI, x)
+    o.L.orc_solve(o.h, dt, 1)
+    dx = o.get(oracle_mod.FIELD_XI) - x
+    f = snh_closed_form_forces(xrest, x, E, nu)
+    assert np.abs(f).max() > 1.0
+    assert np.abs(dx * m / dt ** 2 - f).max() < 1e-6 * np.abs(f).max()
+
+
 def test_oracle_matches_numpy_restatement_first_frame(oracle_mod):
     sc = scenes.beam_c1(frames=1)
     o = oracle_mod.Oracle(sc)
