@@ -397,6 +397,43 @@ sbs_status sbs_mlp_train(sbs_mlp* m, uint32_t steps, uint32_t batch, float lr, u
  * (set_state / set_predicted / a frame without the network reset it to 0).
  * Do not train the same network while it is attached. */
 sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps);
+/* The plain solver as the judge of warm-started substeps (the reference
+ * always runs the plain sweep count from the predicted positions with zero
+ * multipliers, gauss_seidel_solver.cpp:8-37; its residual is the yardstick).
+ * With check_every > 0 and a network attached, every substep of
+ * sbs_gpu_step runs on the device:
+ *   1. the residual of the plain start (predicted positions, zero
+ *      multipliers) and of the warm start; a warm start whose residual is
+ *      not below the plain start's is discarded and the substep continues
+ *      from the plain start (a fallback);
+ *   2. sweeps in chunks of check_every, each followed by the residual, until
+ *      the residual is at or below the target or the next chunk would pass
+ *      max_sweeps (0: the step's `iterations`).
+ * The target of substep k of a frame is the residual that a plain substep k
+ * (the step's `iterations` sweeps) reached in the last calibration frame: the
+ * first judged frame and then every calibrate_every-th frame (0: the first
+ * only) run plain and record their residuals.  fixed_target > 0 sets the
+ * target of every substep instead, and then no frame calibrates.  Residual
+ * as sbs_gpu_residual (compensated FP32 sums of (C + alpha~ lambda)^2 over
+ * the elastic, distance and contact constraints).  The loop is a conditional
+ * node of the frame's CUDA graph whose condition the device sets, so a frame
+ * still needs no host round trip.  check_every = 0 turns the judge off.
+ * Calling this resets the totals of sbs_gpu_get_warm_stats. */
+sbs_status sbs_gpu_set_warm_judge(sbs_gpu* h, uint32_t check_every, uint32_t max_sweeps, uint32_t calibrate_every,
+                                  double fixed_target);
+typedef struct sbs_gpu_warm_stats {
+    uint64_t warm_substeps;         /* judged warm-started substeps run */
+    uint64_t calibration_substeps;  /* plain substeps run to record targets */
+    uint64_t sweeps;                /* sweeps of the judged substeps, in total */
+    uint64_t fallbacks;             /* warm starts discarded for the plain start */
+    uint64_t capped;                /* substeps that stopped at max_sweeps above their target */
+    double mean_residual_ratio;     /* final residual / target, mean over judged substeps */
+    double max_residual_ratio;      /* and its maximum */
+    double last_target;             /* target of substep 0 */
+    double last_residual;           /* final residual of the last judged substep */
+} sbs_gpu_warm_stats;
+/* Totals of the judge since sbs_gpu_set_warm_judge (synchronises). */
+sbs_status sbs_gpu_get_warm_stats(sbs_gpu* h, sbs_gpu_warm_stats* out);
 /* The warm-start half of a substep on its own, after sbs_gpu_predict. */
 sbs_status sbs_gpu_warm_start_init(sbs_gpu* h, double dt);
 /* As sbs_gpu_solve; with reset_lambda = 0 the sweeps continue from the

@@ -41,7 +41,8 @@ struct GraphKey {
     double dt;
     uint32_t substeps, iterations;
     // 0: plain frame; warm-started frame: 1 without, 2 with the previous
-    // substep's displacement known at its start
+    // substep's displacement known at its start; 3: a judge's calibration
+    // frame (plain substeps that record their residuals as targets)
     int warm;
     bool operator<(const GraphKey& o) const {
         if (dt != o.dt) return dt < o.dt;
@@ -138,6 +139,13 @@ struct sbs_gpu {
     std::vector<uint32_t> vis_map;             // surface vertex -> body-local vertex id
     SurfaceDev sd{};
     uint32_t fit_sweeps = 1;
+    // plain-solver judge of warm-started substeps (judge_chunk 0: off)
+    uint32_t judge_chunk = 0, judge_cap = 0, judge_calib_every = 0;
+    double judge_fixed_target = 0.0;
+    JudgeDev* d_judge = nullptr;
+    cudaStream_t side = nullptr;      // captures the bodies of the sweep loops
+    uint64_t judged_frames = 0;       // judged frames run (calibration ones included)
+    bool judge_target_valid = false;
     double sim_time = 0.0;   // host mirror of the simulation time
     std::vector<uint32_t> seg_split;  // first SNH slot of each colour segment
 
@@ -1557,7 +1565,8 @@ static sbs_status enqueue_frame_kernels(sbs_gpu* h, const StepParams& p) {
 }
 
 static sbs_status enqueue_warm_init(sbs_gpu* h, const StepParams& p);
-static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t iterations, bool reset);
+static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t iterations, bool reset,
+                                   cudaStream_t st);
 
 // Learned warm start: per substep predict -> features -> MLP -> carry or fit
 // sweeps, then the sweeps continue from those multipliers.
@@ -1577,8 +1586,130 @@ static sbs_status enqueue_warm_frame(sbs_gpu* h, const StepParams& p, uint32_t s
             q.substeps = 1;
             q.cl_flags = kClExternal | kClCarry;
             CU(h, launch_cluster_frame(h->d, h->cd, q, h->sim_time, h->cl_grid, h->cl_block, h->cl_smem, h->st));
-        } else if ((s = enqueue_segments(h, p, iterations, false)) != SBS_OK) {
+        } else if ((s = enqueue_segments(h, p, iterations, false, h->st)) != SBS_OK) {
             return s;
+        }
+        CU(h, launch_finalize(h->d, p, h->st));
+    }
+    CU(h, launch_end_frame(h->d, h->st));
+    return SBS_OK;
+}
+
+// Plain-solver judge (sbs_gpu_set_warm_judge).  A judged warm-started
+// substep runs, all on the device:
+//   predict; the plain start's residual (predicted positions, zero
+//   multipliers); the warm start (features, network, carry or fit); its
+//   residual, which keeps the warm start only if it is below the plain
+//   start's and otherwise restores the plain start (k_judge_fallback); then
+//   a WHILE conditional graph node whose body runs `chunk` sweeps and the
+//   residual, until the residual is at or below the target (the residual of
+//   a plain substep with the full sweep count, recorded by calibration
+//   frames) or the next chunk would pass the cap; velocity update.
+// The loop's condition is set by k_residual_final (JudgeOp), on the device,
+// so a frame is one graph launch with no host round trip.
+
+// One sweep chunk of the running substep on stream `st`.
+static sbs_status enqueue_judge_chunk(sbs_gpu* h, const StepParams& p, cudaStream_t st) {
+    if (h->exec_mode == SBS_EXEC_CLUSTER) {
+        StepParams q = p;
+        q.substeps = 1;
+        q.iterations = (int)h->judge_chunk;
+        q.cl_flags = kClExternal | kClCarry | kClContinue;
+        CU(h, launch_cluster_frame(h->d, h->cd, q, h->sim_time, h->cl_grid, h->cl_block, h->cl_smem, st));
+        return SBS_OK;
+    }
+    return enqueue_segments(h, p, h->judge_chunk, false, st);
+}
+
+static sbs_status enqueue_judge_residual(sbs_gpu* h, const StepParams& p, int zero_lam, const JudgeOp& op,
+                                         cudaStream_t st) {
+    const int grid = std::max(1, std::min(4096, (int)((h->n_tets + 255) / 256)));
+    CU(h, launch_residual_ex(h->d, p, 256, grid, 0, st, zero_lam, &op));
+    return SBS_OK;
+}
+
+// The sweep loop of substep `sub` inside the frame graph being captured on
+// h->st: a conditional handle (set by the start residual's judge step), the
+// WHILE node, and its body captured on the side stream.
+static sbs_status enqueue_judge_loop(sbs_gpu* h, const StepParams& p, int sub) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    CU(h, cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    if (cs != cudaStreamCaptureStatusActive || !g) return fail(h, SBS_ESTATE, "judged frames run as graphs");
+    cudaGraphConditionalHandle hc;
+    CU(h, cudaGraphConditionalHandleCreate(&hc, g, 0, 0));
+    JudgeOp op{};
+    op.kind = kJudgeStart;
+    op.substep = sub;
+    op.chunk = h->judge_chunk;
+    op.cap = h->judge_cap ? h->judge_cap : (uint32_t)p.iterations;
+    op.j = h->d_judge;
+    op.cond = (unsigned long long)hc;
+    sbs_status s = enqueue_judge_residual(h, p, 0, op, h->st);
+    if (s) return s;
+    CU(h, launch_judge_fallback(h->d, h->wd, h->d_judge, h->st));
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t nd = 0;
+    CU(h, cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, &deps, &edges, &nd));
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hc;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    CU(h, cudaGraphAddNode(&node, g, deps, edges, nd, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    CU(h, cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    op.kind = kJudgeChunk;
+    s = enqueue_judge_chunk(h, p, h->side);
+    if (s == SBS_OK) s = enqueue_judge_residual(h, p, 0, op, h->side);
+    cudaGraph_t body_out = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->side, &body_out);
+    if (s) return s;
+    if (e != cudaSuccess) return fail(h, SBS_ECUDA, std::string("loop body capture: ") + cudaGetErrorString(e));
+    CU(h, cudaStreamUpdateCaptureDependencies(h->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    CU(h, launch_judge_end(h->d_judge, sub, h->st));
+    return SBS_OK;
+}
+
+static sbs_status enqueue_judged_frame(sbs_gpu* h, const StepParams& p, uint32_t substeps, uint32_t iterations,
+                                       bool calibrate) {
+    CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+    CU(h, launch_detect_ground(h->d, p, h->st));
+    if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
+    for (uint32_t sub = 0; sub < substeps; ++sub) {
+        CU(h, launch_predict(h->d, p, (int)sub, h->st));
+        sbs_status s;
+        if (calibrate) {
+            // a plain substep (the features only record the prediction for
+            // the next warm substep's previous-displacement feature)
+            CU(h, launch_features(h->d, h->wd, p, h->xpred_valid ? 1 : 0, h->st));
+            h->xpred_valid = true;
+            CU(h, cudaMemsetAsync(h->d.contact_lam, 0, (size_t)(kMaxPlanes + 1) * h->d.n_surf * sizeof(float),
+                                  h->st));
+            if (h->exec_mode == SBS_EXEC_CLUSTER) {
+                StepParams q = p;
+                q.substeps = 1;
+                q.cl_flags = kClExternal;
+                CU(h, launch_cluster_frame(h->d, h->cd, q, h->sim_time, h->cl_grid, h->cl_block, h->cl_smem,
+                                           h->st));
+            } else if ((s = enqueue_segments(h, p, iterations, true, h->st)) != SBS_OK) {
+                return s;
+            }
+            JudgeOp op{};
+            op.kind = kJudgeCalib;
+            op.substep = (int)sub;
+            op.j = h->d_judge;
+            if ((s = enqueue_judge_residual(h, p, 0, op, h->st)) != SBS_OK) return s;
+        } else {
+            JudgeOp op{};
+            op.kind = kJudgePlain0;
+            op.substep = (int)sub;
+            op.j = h->d_judge;
+            if ((s = enqueue_judge_residual(h, p, 1, op, h->st)) != SBS_OK) return s;
+            if ((s = enqueue_warm_init(h, p)) != SBS_OK) return s;
+            if ((s = enqueue_judge_loop(h, p, (int)sub)) != SBS_OK) return s;
         }
         CU(h, launch_finalize(h->d, p, h->st));
     }
@@ -1616,7 +1747,20 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
     double t_end = h->sim_time;
     for (uint32_t k = 0; k < substeps; ++k) t_end += dt;   // same double sequence as the CPU loop
     const uint64_t launches0 = launch_counter();
-    if (h->mlp) {
+    if (h->mlp && h->judge_chunk) {
+        // judged warm-started frame, or a calibration frame of plain
+        // substeps when no target is known yet or one is due
+        if (substeps > (uint32_t)kMaxJudgeSubsteps)
+            return fail(h, SBS_EINVAL, "judged frames take at most 64 substeps");
+        const bool calibrate = !h->judge_target_valid ||
+                               (h->judge_calib_every > 0 && h->judged_frames % h->judge_calib_every == 0);
+        const GraphKey key{dt, substeps, iterations, calibrate ? 3 : (h->xpred_valid ? 2 : 1)};
+        sbs_status s = run_graph(h, key, [&]() { return enqueue_judged_frame(h, p, substeps, iterations, calibrate); });
+        if (s) return s;
+        h->xpred_valid = true;
+        h->judged_frames++;
+        if (calibrate) h->judge_target_valid = true;
+    } else if (h->mlp) {
         // the warm-started frame as one CUDA graph per shape (a substep is
         // hundreds of small kernels); whether the previous substep's
         // displacement is known at the frame's start is part of the shape
@@ -1669,7 +1813,22 @@ static void clear_graphs(sbs_gpu* h) {
 
 // Autotuner: times each candidate configuration on a copy of the state and
 // restores the state afterwards.
+static sbs_status autotune_modes(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations);
+
+// The execution mode is chosen by timing plain frames, also when a warm
+// start is attached (its graphs are rebuilt for the chosen mode).
 static sbs_status autotune(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations) {
+    sbs_mlp* m = h->mlp;
+    const bool xv = h->xpred_valid;
+    h->mlp = nullptr;
+    sbs_status s = autotune_modes(h, dt, substeps, iterations);
+    h->mlp = m;
+    h->xpred_valid = xv;   // the tuner restores the state it stepped
+    clear_graphs(h);
+    return s;
+}
+
+static sbs_status autotune_modes(sbs_gpu* h, double dt, uint32_t substeps, uint32_t iterations) {
     const SceneDev& d = h->d;
     const size_t V = d.n_verts;
     float4 *bxi, *bxn, *bv;
@@ -1863,7 +2022,7 @@ sbs_status sbs_gpu_solve(sbs_gpu* h, double dt, uint32_t iterations) {
     if (!h->contacts_live) CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
     // one launch per vertex-disjoint colour segment (all groups' colours in
     // sweep order), whatever the execution mode of sbs_gpu_step
-    if ((s = enqueue_segments(h, p, iterations, true)) != SBS_OK) return s;
+    if ((s = enqueue_segments(h, p, iterations, true, h->st)) != SBS_OK) return s;
     h->projections += (uint64_t)iterations * h->n_tets;
     return SBS_OK;
 }
@@ -2148,6 +2307,59 @@ sbs_status sbs_gpu_set_warm_start(sbs_gpu* h, sbs_mlp* m, uint32_t fit_sweeps) {
     return SBS_OK;
 }
 
+sbs_status sbs_gpu_set_warm_judge(sbs_gpu* h, uint32_t check_every, uint32_t max_sweeps, uint32_t calibrate_every,
+                                  double fixed_target) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (check_every > 1000 || max_sweeps > 100000 || !(fixed_target >= 0.0) || !std::isfinite(fixed_target))
+        return fail(h, SBS_EINVAL, "set_warm_judge: bad arguments");
+    if (check_every && max_sweeps && check_every > max_sweeps)
+        return fail(h, SBS_EINVAL, "set_warm_judge: check_every above max_sweeps");
+    if (check_every && !h->d_judge) {
+        if ((s = dalloc(h, &h->d_judge, 1)) != SBS_OK) return s;
+        CU(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+    }
+    h->judge_chunk = check_every;
+    h->judge_cap = max_sweeps;
+    h->judge_calib_every = calibrate_every;
+    h->judge_fixed_target = fixed_target;
+    h->judged_frames = 0;
+    h->judge_target_valid = false;
+    if (h->d_judge) {
+        JudgeDev j{};
+        if (check_every && fixed_target > 0.0) {
+            for (int k = 0; k < kMaxJudgeSubsteps; ++k) j.target[k] = fixed_target;
+            h->judge_target_valid = true;
+            h->judge_calib_every = 0;
+        }
+        CU(h, cudaMemcpyAsync(h->d_judge, &j, sizeof(j), cudaMemcpyHostToDevice, h->st));
+        CU(h, cudaStreamSynchronize(h->st));
+    }
+    clear_graphs(h);
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_get_warm_stats(sbs_gpu* h, sbs_gpu_warm_stats* out) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (!out) return fail(h, SBS_EINVAL, "null");
+    *out = sbs_gpu_warm_stats{};
+    if (!h->d_judge) return SBS_OK;
+    JudgeDev j;
+    CU(h, cudaMemcpyAsync(&j, h->d_judge, sizeof(j), cudaMemcpyDeviceToHost, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+    out->warm_substeps = j.warm_substeps;
+    out->calibration_substeps = j.calib_substeps;
+    out->sweeps = j.total_sweeps;
+    out->fallbacks = j.fallbacks;
+    out->capped = j.capped;
+    out->mean_residual_ratio = j.warm_substeps ? j.sum_ratio / (double)j.warm_substeps : 0.0;
+    out->max_residual_ratio = j.max_ratio;
+    out->last_target = j.target[0];
+    out->last_residual = j.r_now;
+    return check_err(h);
+}
+
 // features -> MLP -> fit sweep (multipliers initialised), on the predicted state
 static sbs_status enqueue_warm_init(sbs_gpu* h, const StepParams& p) {
     const bool dprev_valid = h->xpred_valid;
@@ -2183,11 +2395,12 @@ sbs_status sbs_gpu_warm_start_init(sbs_gpu* h, double dt) {
     return enqueue_warm_init(h, p);
 }
 
-static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t iterations, bool reset) {
+static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t iterations, bool reset,
+                                   cudaStream_t st) {
     for (uint32_t it = 0; it < iterations; ++it) {
         const int first = (reset && it == 0) ? 1 : 0;
-        CU(h, launch_contacts(h->d, p, first, h->st));
-        CU(h, launch_body_contacts(h->d, p, first, h->st));
+        CU(h, launch_contacts(h->d, p, first, st));
+        CU(h, launch_body_contacts(h->d, p, first, st));
         for (size_t c = 0; c + 1 < h->colour_offsets.size(); ++c) {
             StepParams q = p;
             q.n_colours = 1;
@@ -2195,9 +2408,9 @@ static sbs_status enqueue_segments(sbs_gpu* h, const StepParams& p, uint32_t ite
             q.colour_start[0] = h->colour_offsets[c];
             q.colour_start[1] = h->colour_offsets[c + 1];
             q.colour_split[0] = h->seg_split[c];
-            CU(h, launch_colour(h->d, q, 0, first, h->block, h->grid, h->st));
+            CU(h, launch_colour(h->d, q, 0, first, h->block, h->grid, st));
         }
-        for (int c = 0; c < p.n_edge_colours; ++c) CU(h, launch_edges(h->d, p, c, first, h->st));
+        for (int c = 0; c < p.n_edge_colours; ++c) CU(h, launch_edges(h->d, p, c, first, st));
     }
     return SBS_OK;
 }
@@ -2209,7 +2422,7 @@ sbs_status sbs_gpu_solve_ex(sbs_gpu* h, double dt, uint32_t iterations, int32_t 
     StepParams p;
     fill_params(h, p, dt, 1, iterations);
     if (!h->contacts_live) CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
-    if ((s = enqueue_segments(h, p, iterations, reset_lambda != 0)) != SBS_OK) return s;
+    if ((s = enqueue_segments(h, p, iterations, reset_lambda != 0, h->st)) != SBS_OK) return s;
     h->projections += (uint64_t)iterations * h->n_tets;
     return SBS_OK;
 }
@@ -2343,6 +2556,7 @@ sbs_status sbs_gpu_destroy(sbs_gpu* h) {
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->st) cudaStreamDestroy(h->st);
+    if (h->side) cudaStreamDestroy(h->side);
     delete h;
     return SBS_OK;
 }

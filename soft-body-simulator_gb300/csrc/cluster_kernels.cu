@@ -283,6 +283,9 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
         if (c.stage && threadIdx.x == 0 && gd.n_col > 0 && p.substeps > 0 && p.iterations > 0)
             stage_issue(s, c, s_cb[0], s_ce[0], stg_base + (ph & 1u) * stg_bytes, mb_base + (ph & 1u) * 8u);
         const bool ext = (p.cl_flags & kClExternal) != 0;
+        // a further chunk of the same substep's sweeps: the contact
+        // multipliers go on from where the previous chunk left them
+        const bool cont = ext && (p.cl_flags & kClContinue) != 0;
         // load own slice; ground contacts of own surface vertices from the
         // frame-start positions (bvh_model.cpp:72-94 with the plane SDF)
         for (uint32_t i = threadIdx.x; i < nown && ext; i += blockDim.x) {
@@ -299,9 +302,12 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                 float4 r = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
                 if (bq.w != 0.0f) {
                     const float4 nn = c.bc_n[gv];
-                    r = make_float4(bq.x, bq.y, bq.z, 0.0f);
+                    const uint32_t slot = __float_as_uint(nn.w);
+                    const float l = (cont && slot < s.n_surf) ? s.contact_lam[(size_t)kMaxPlanes * s.n_surf + slot]
+                                                              : 0.0f;
+                    r = make_float4(bq.x, bq.y, bq.z, l);
                     bn[i] = nn;
-                    gidx[(size_t)i * S + p.n_planes] = __float_as_uint(nn.w);
+                    gidx[(size_t)i * S + p.n_planes] = slot;
                 }
                 rec[(size_t)i * S + p.n_planes] = r;
             }
@@ -315,7 +321,8 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                     const uint32_t gv = __float_as_uint(ct.q.w);
                     if (gv < own0 || gv >= own1) continue;
                     const uint32_t i = gv - own0;
-                    rec[(size_t)i * S + pl] = make_float4(ct.q.x, ct.q.y, ct.q.z, 0.0f);
+                    const float l = cont ? s.contact_lam[(size_t)pl * s.n_surf + k] : 0.0f;
+                    rec[(size_t)i * S + pl] = make_float4(ct.q.x, ct.q.y, ct.q.z, l);
                     gidx[(size_t)i * S + pl] = k;
                 }
             }
@@ -436,7 +443,7 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                     for (int sl = 0; sl < S; ++sl) {
                         float4 r = rec[(size_t)i * S + sl];
                         if (isnan(r.x)) continue;
-                        if (first) r.w = 0.0f;
+                        if (first && !cont) r.w = 0.0f;
                         float nx, ny, nz;
                         if (sl < p.n_planes) {
                             nx = p.planes[sl].nx; ny = p.planes[sl].ny; nz = p.planes[sl].nz;

@@ -211,6 +211,44 @@ __global__ void k_carry(SceneDev s, WarmDev w) {
     }
 }
 
+// Fallback of a judged substep whose warm start was discarded
+// (JudgeDev::fallback, decided on the device): the positions go back to the
+// prediction and the elastic multipliers to zero, i.e. the plain start.
+__global__ void k_judge_fallback(SceneDev s, WarmDev w, const JudgeDev* j) {
+    if (!j->fallback) return;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n_verts; i += stride) s.xi[i] = w.xpred[i];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < s.n_tets; t += stride) {
+        s.lam0[t] = 0.0f;
+        s.lam1[t] = 0.0f;
+    }
+}
+
+// Totals of a judged substep once its sweep loop ended.
+__global__ void k_judge_end(JudgeDev* j, int substep) {
+    const double target = j->target[substep];
+    j->warm_substeps++;
+    j->total_sweeps += j->sweeps;
+    if (!(j->r_now <= target)) j->capped++;
+    const double ratio = target > 0.0 ? j->r_now / target : (j->r_now > 0.0 ? 1e30 : 1.0);
+    j->sum_ratio += ratio;
+    if (ratio > j->max_ratio) j->max_ratio = ratio;
+}
+
+cudaError_t launch_judge_fallback(const SceneDev& s, const WarmDev& w, const JudgeDev* j, cudaStream_t st) {
+    const uint32_t n = s.n_verts > s.n_tets ? s.n_verts : s.n_tets;
+    const int grid = (int)std::min<uint32_t>(2048, (n + 255) / 256);
+    k_judge_fallback<<<grid > 0 ? grid : 1, 256, 0, st>>>(s, w, j);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_judge_end(JudgeDev* j, int substep, cudaStream_t st) {
+    k_judge_end<<<1, 1, 0, st>>>(j, substep);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_carry(const SceneDev& s, const WarmDev& w, cudaStream_t st) {
     const int grid = (int)std::min<uint32_t>(4096, (s.n_verts + 255) / 256);
     k_carry<<<grid > 0 ? grid : 1, 256, 0, st>>>(s, w);

@@ -24,5 +24,7 @@ cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParam
 cudaError_t launch_fit_segment(const SceneDev& s, const WarmDev& w, const StepParams& p, uint32_t b, uint32_t e,
                                int first, cudaStream_t st);
 cudaError_t launch_carry(const SceneDev& s, const WarmDev& w, cudaStream_t st);
+cudaError_t launch_judge_fallback(const SceneDev& s, const WarmDev& w, const JudgeDev* j, cudaStream_t st);
+cudaError_t launch_judge_end(JudgeDev* j, int substep, cudaStream_t st);
 
 }  // namespace sbs

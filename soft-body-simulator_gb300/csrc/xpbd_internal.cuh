@@ -114,8 +114,36 @@ struct StepParams {
 // sweeps on them, takes the frame's contacts from the global contact list,
 // and leaves prediction and velocity update to the global kernels.
 // kClCarry: the elastic multipliers start from lam0/lam1, not from zero.
+// kClContinue: the contact multipliers start from contact_lam (a further
+// chunk of sweeps of the same substep), not from zero.
 constexpr int kClExternal = 1;
 constexpr int kClCarry = 2;
+constexpr int kClContinue = 4;
+
+// Device state of the plain-solver judge of warm-started substeps
+// (warmstart.cu): residual targets from plain substeps, the running
+// substep's residuals, and totals since the judge was set.
+constexpr int kMaxJudgeSubsteps = 64;
+struct JudgeDev {
+    double target[kMaxJudgeSubsteps];  // plain residual after the full sweep count, per substep index
+    double r_plain0;                   // residual of the plain start (predicted positions, zero multipliers)
+    double r_start;                    // residual of the start the substep kept
+    double r_now;                      // residual after the sweeps run so far
+    uint32_t sweeps;                   // sweeps run in the current substep
+    uint32_t fallback;                 // the current substep fell back to the plain start
+    unsigned long long warm_substeps, calib_substeps, total_sweeps, fallbacks, capped;
+    double sum_ratio, max_ratio;       // final residual / target over warm substeps
+};
+
+// What k_residual_final does with the residual it reduced (judge steps).
+enum JudgeOpKind { kJudgeNone = 0, kJudgePlain0 = 1, kJudgeStart = 2, kJudgeChunk = 3, kJudgeCalib = 4 };
+struct JudgeOp {
+    int kind;
+    int substep;                        // index into JudgeDev::target
+    uint32_t chunk, cap;                // sweeps per check, most sweeps per substep
+    JudgeDev* j;
+    unsigned long long cond;            // cudaGraphConditionalHandle of the substep's sweep loop
+};
 
 // Kernel launchers (xpbd_kernels.cu).  All enqueue on `st`.
 cudaError_t launch_detect_ground(const SceneDev& s, const StepParams& p, cudaStream_t st);
@@ -128,7 +156,7 @@ cudaError_t launch_tail(const SceneDev& s, const StepParams& p, int first_iter, 
 cudaError_t launch_finalize(const SceneDev& s, const StepParams& p, cudaStream_t st);
 cudaError_t launch_edges(const SceneDev& s, const StepParams& p, int colour, int first_iter, cudaStream_t st);
 cudaError_t launch_residual_ex(const SceneDev& s, const StepParams& p, int block, int grid, int cnt_base,
-                               cudaStream_t st);
+                               cudaStream_t st, int zero_lam = 0, const JudgeOp* op = nullptr);
 cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st);
 cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
                                     cudaStream_t st);

@@ -641,7 +641,9 @@ __device__ __forceinline__ CSum block_reduce(CSum v, float* sh) {
     return r;
 }
 
-__global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
+// zero_lam: the residual the state would have with every multiplier zero
+// (the plain start of a substep: the predicted positions, nothing solved).
+__global__ void k_residual(SceneDev s, StepParams p, int cnt_base, int zero_lam) {
     extern __shared__ float sh[];
     CSum re{0.f, 0.f}, en{0.f, 0.f}, rc{0.f, 0.f};
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -653,13 +655,13 @@ __global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
         if (!snh) {
             TetEval e;
             stvk_eval(x0, x1, x2, x3, mk(a), mk(b), mk(c), a.w, b.w, c.w, e);
-            const float h = e.C + p.stvk_alpha_tilde * s.lam0[t];
+            const float h = e.C + (zero_lam ? 0.0f : p.stvk_alpha_tilde * s.lam0[t]);
             re.add(h * h);
             en.add(e.C);
         } else {
             float r2, E;
-            snh_residual(x0, x1, x2, x3, mk(a), mk(b), mk(c), fabsf(a.w), b.w, c.w, p.inv_dt2, s.lam0[t],
-                         s.lam1[t], r2, E);
+            snh_residual(x0, x1, x2, x3, mk(a), mk(b), mk(c), fabsf(a.w), b.w, c.w, p.inv_dt2,
+                         zero_lam ? 0.0f : s.lam0[t], zero_lam ? 0.0f : s.lam1[t], r2, E);
             re.add(r2);
             en.add(E);
         }
@@ -669,7 +671,7 @@ __global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
         const float4 q = s.edge_p[k];
         const f3 d = mk(s.xi[e.x]) - mk(s.xi[e.y]);
         const float C = sqrtf(dot(d, d)) - q.x;
-        const float h = C + q.y * p.inv_dt2 * s.edge_lam[k];
+        const float h = C + (zero_lam ? 0.0f : q.y * p.inv_dt2 * s.edge_lam[k]);
         re.add(h * h);
         if (q.y > 0.0f) en.add(0.5f * C * C / q.y);
     }
@@ -683,7 +685,7 @@ __global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
             const float4 x = s.xi[__float_as_uint(c.q.w)];
             const float C = (x.x - c.q.x) * c.n.x + (x.y - c.q.y) * c.n.y + (x.z - c.q.z) * c.n.z;
             if (C < 0.0f) {
-                const float h = C + p.contact_alpha_tilde * s.contact_lam[ci];
+                const float h = C + (zero_lam ? 0.0f : p.contact_alpha_tilde * s.contact_lam[ci]);
                 rc.add(h * h);
             }
         }
@@ -697,15 +699,61 @@ __global__ void k_residual(SceneDev s, StepParams p, int cnt_base) {
     }
 }
 
-__global__ void k_residual_final(SceneDev s, int nparts) {
+// Sums the per-CTA partials (fixed order) into red_out and, for a judged
+// warm-started substep, acts on the residual r = sqrt(elastic^2 + contact^2)
+// (JudgeOp): records the plain start's residual, decides between the warm
+// and the plain start and whether the sweep loop runs, counts a chunk of
+// sweeps and decides whether another one runs, or records a plain substep's
+// residual as the target.  The loop decision goes to the loop's conditional
+// graph node; it is 0 once the residual is at or below the target, the next
+// chunk would pass the sweep cap, or the device error flag is set, so the
+// loop always ends.
+__global__ void k_residual_final(SceneDev s, int nparts, JudgeOp op) {
     extern __shared__ float sh[];
     CSum acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     for (int i = threadIdx.x; i < nparts; i += blockDim.x)
         for (int k = 0; k < 3; ++k) acc[k].merge(CSum{s.partials[6 * i + 2 * k], s.partials[6 * i + 2 * k + 1]});
+    double red[3];
     for (int k = 0; k < 3; ++k) {
         CSum r = block_reduce(acc[k], sh);
-        if (threadIdx.x == 0) s.red_out[k] = (double)r.s + (double)r.e;
+        red[k] = (double)r.s + (double)r.e;
+        if (threadIdx.x == 0) s.red_out[k] = red[k];
     }
+    if (threadIdx.x != 0 || op.kind == kJudgeNone) return;
+    JudgeDev* j = op.j;
+    const double sq = red[0] + red[2];
+    const double r = sq > 0.0 ? sqrt(sq) : (sq == sq ? 0.0 : sq);   // NaN stays NaN
+    const double target = j->target[op.substep];
+    const bool err = *(volatile int*)s.err != 0;
+    unsigned cond = 0;
+    switch (op.kind) {
+    case kJudgePlain0:
+        j->r_plain0 = r;
+        return;
+    case kJudgeStart: {
+        // a start whose residual is not below the plain start's is discarded
+        const bool fb = !(r < j->r_plain0);
+        j->fallback = fb ? 1u : 0u;
+        if (fb) j->fallbacks++;
+        j->r_start = fb ? j->r_plain0 : r;
+        j->r_now = j->r_start;
+        j->sweeps = 0;
+        cond = (!(j->r_now <= target) && op.chunk <= op.cap && !err) ? 1u : 0u;
+        break;
+    }
+    case kJudgeChunk:
+        j->sweeps += op.chunk;
+        j->r_now = r;
+        cond = (!(r <= target) && j->sweeps + op.chunk <= op.cap && !err) ? 1u : 0u;
+        break;
+    case kJudgeCalib:
+        j->target[op.substep] = r;
+        j->calib_substeps++;
+        return;
+    default:
+        return;
+    }
+    cudaGraphSetConditional((cudaGraphConditionalHandle)op.cond, cond);
 }
 
 __global__ void k_set_error(int* err, int code) { atomicCAS(err, 0, code); }
@@ -787,13 +835,15 @@ cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st) {
 }
 
 cudaError_t launch_residual_ex(const SceneDev& s, const StepParams& p, int block, int grid, int cnt_base,
-                               cudaStream_t st) {
+                               cudaStream_t st, int zero_lam, const JudgeOp* op) {
     const size_t shm = 2 * sizeof(float) * (size_t)block;
-    k_residual<<<grid, block, shm, st>>>(s, p, cnt_base);
+    k_residual<<<grid, block, shm, st>>>(s, p, cnt_base, zero_lam);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_residual_final<<<1, 256, 2 * sizeof(float) * 256, st>>>(s, grid);
+    JudgeOp none{};
+    none.kind = kJudgeNone;
+    k_residual_final<<<1, 256, 2 * sizeof(float) * 256, st>>>(s, grid, op ? *op : none);
     count_launch();
     return cudaGetLastError();
 }

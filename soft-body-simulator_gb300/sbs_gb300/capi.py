@@ -36,6 +36,12 @@ class Params(C.Structure):
                 ("check_finite", C.c_int32), ("stage_records", C.c_int32)]
 
 
+class WarmStats(C.Structure):
+    _fields_ = [("warm_substeps", C.c_uint64), ("calibration_substeps", C.c_uint64), ("sweeps", C.c_uint64),
+                ("fallbacks", C.c_uint64), ("capped", C.c_uint64), ("mean_residual_ratio", C.c_double),
+                ("max_residual_ratio", C.c_double), ("last_target", C.c_double), ("last_residual", C.c_double)]
+
+
 class Material(C.Structure):
     _fields_ = [("model", C.c_int32), ("young", C.c_double), ("poisson", C.c_double),
                 ("density", C.c_double)]
@@ -117,6 +123,8 @@ def load(build: bool = True):
                                C.c_uint32, C.POINTER(C.c_uint32)],
         "sbs_gpu_get_candidates": [P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)],
         "sbs_gpu_set_warm_start": [P, C.c_void_p, C.c_uint32],
+        "sbs_gpu_set_warm_judge": [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double],
+        "sbs_gpu_get_warm_stats": [P, C.POINTER(WarmStats)],
         "sbs_gpu_warm_start_init": [P, C.c_double],
         "sbs_gpu_solve_ex": [P, C.c_double, C.c_uint32, C.c_int32],
         "sbs_gpu_get_features": [P, f32],
@@ -400,6 +408,19 @@ class Solver:
     def set_warm_start(self, mlp, fit_sweeps: int = 1):
         self._warm = mlp
         self._check(self.L.sbs_gpu_set_warm_start(self.h, None if mlp is None else mlp.h, fit_sweeps))
+
+    def set_warm_judge(self, check_every: int, max_sweeps: int = 0, calibrate_every: int = 0,
+                       fixed_target: float = 0.0):
+        """The plain solver as judge of the warm-started substeps: sweeps in
+        chunks of `check_every` until the plain residual target is reached
+        (or `max_sweeps`), with a fallback to the plain start when the warm
+        start's residual is not below the plain start's."""
+        self._check(self.L.sbs_gpu_set_warm_judge(self.h, check_every, max_sweeps, calibrate_every, fixed_target))
+
+    def warm_stats(self) -> WarmStats:
+        st = WarmStats()
+        self._check(self.L.sbs_gpu_get_warm_stats(self.h, C.byref(st)))
+        return st
 
     def warm_start_init(self, dt: float):
         self._check(self.L.sbs_gpu_warm_start_init(self.h, dt))

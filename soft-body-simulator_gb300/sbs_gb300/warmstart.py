@@ -11,6 +11,13 @@ solver handle:
 * ``BEAM98K``: the 98,304-tet beam (64x16x16 cubes of 0.05 m, 6 tets each,
   stable Neo-Hookean E 1e6, nu 0.49, rho 1000), 4 substeps x 30 plain
   iterations per 1/60 s frame.
+
+``TWIST98K`` is the 98,304-tet beam of the benchmark (x=0 face pinned, x=max
+face turned about the beam's axis) with a per-trajectory turning rate
+U(0.5, 1.5) rad/s and jitter seed, no body force: the trajectories a network
+for that scene is trained on.  Trained networks are saved as .npz files
+(parameters and the input/output normalisation, ``save_network``) and loaded
+with ``load_network``.
 """
 from __future__ import annotations
 
@@ -51,6 +58,14 @@ def beam98k_trajectory_body(seed: int):
     return _trajectory_body(seed, x0, tets, scenes.MODEL_SNH, 1e6, 0.49, 3.2, 1e-4)
 
 
+def twist98k_trajectory_body(seed: int):
+    """One twisting-beam trajectory (the benchmark scene's body with its own
+    turning rate and jitter)."""
+    rng = np.random.default_rng(seed)
+    omega = float(rng.uniform(0.5, 1.5))
+    return scenes.beam_twist(seed=seed + 104729, omega=omega).bodies[0]
+
+
 @dataclass(frozen=True)
 class Workload:
     name: str
@@ -67,6 +82,7 @@ def _box_scene(seed: int) -> scenes.Scene:
 
 CANTILEVER = Workload("beam450", beam_trajectory_body, 1, 30)
 BEAM98K = Workload("beam98k", beam98k_trajectory_body, 4, 30)
+TWIST98K = Workload("twist98k", twist98k_trajectory_body, 4, 30)
 # the batch of 512 boxes (StVK, body-body contacts, 2 substeps x 20
 # iterations); a trajectory is a whole scene of 512 bodies
 BOXES512 = Workload("boxes512", None, 2, 20, make_scene=_box_scene)
@@ -124,6 +140,7 @@ def fit(X, Y, steps: int = 20000, batch: int = 65536, lr: float = 1e-3, seed: in
     std[std < 1e-8] = 1.0
     scale = Y.std(0) + 1e-12
     m.set_normalization(mean, std, scale)
+    m.normalization = (mean.astype(np.float32), std.astype(np.float32), scale.astype(np.float32))
     m.set_dataset(X, Y)
     losses = []
     done = 0
@@ -132,6 +149,63 @@ def fit(X, Y, steps: int = 20000, batch: int = 65536, lr: float = 1e-3, seed: in
         losses.append(m.train(k, min(batch, len(X)), lr, seed=seed + done))
         done += k
     return m, losses
+
+
+def save_network(m, path, **meta):
+    """Parameters and normalisation of a trained network (fit) as .npz."""
+    mean, std, scale = m.normalization
+    np.savez(path, params=m.params(), mean=mean, std=std, scale=scale,
+             **{k: np.asarray(v) for k, v in meta.items()})
+
+
+def load_network(path, device: int = 0):
+    """A network saved by save_network, on `device`."""
+    d = np.load(path)
+    m = capi.Mlp(device=device, seed=0)
+    m.set_params(d["params"].astype(np.float32))
+    m.set_normalization(d["mean"].astype(np.float32), d["std"].astype(np.float32), d["scale"].astype(np.float32))
+    m.normalization = (d["mean"], d["std"], d["scale"])
+    return m
+
+
+def judged_rate(mlp, seeds, frames: int = 30, lead_frames: int = 5, check_every: int = 3,
+                calibrate_every: int = 10, workload: Workload = CANTILEVER, exec_mode: int = 0):
+    """Frames per second at equal residual with the plain solver as judge.
+    Per held-out trajectory a plain handle and a judged warm-started handle
+    (sbs_gpu_set_warm_judge: sweeps in chunks of `check_every` until the
+    plain residual target, fallback to the plain start, a plain calibration
+    frame every `calibrate_every` frames) advance `lead_frames` plain frames,
+    then step `frames` timed frames each (the judged handle's calibration
+    frames included).  Returns mean device times per frame, their ratio and
+    the judge's totals."""
+    plain_ms, warm_ms = [], []
+    tot = {"warm_substeps": 0, "calibration_substeps": 0, "sweeps": 0, "fallbacks": 0, "capped": 0}
+    ratio_sum, ratio_max = 0.0, 0.0
+    for s in seeds:
+        sc = batch_scene([s], None, workload)
+        a = capi.Solver(sc, exec_mode=exec_mode)
+        a.step(lead_frames)
+        plain_ms += [a.step_timed() for _ in range(frames)]
+        a.close()
+        b = capi.Solver(sc, exec_mode=exec_mode)
+        b.step(lead_frames)
+        b.set_warm_start(mlp, 0)
+        b.set_warm_judge(check_every, 0, calibrate_every, 0.0)
+        warm_ms += [b.step_timed() for _ in range(frames)]
+        st = b.warm_stats()
+        for k in tot:
+            tot[k] += int(getattr(st, k))
+        ratio_sum += st.mean_residual_ratio * st.warm_substeps
+        ratio_max = max(ratio_max, st.max_residual_ratio)
+        b.set_warm_start(None)
+        b.close()
+    pm, wm = float(np.mean(plain_ms)), float(np.mean(warm_ms))
+    return {"plain_ms_per_frame": pm, "judged_ms_per_frame": wm, "frames_per_s_ratio": pm / wm,
+            "frames": len(warm_ms), "check_every": check_every, "calibrate_every": calibrate_every,
+            "mean_sweeps_per_warm_substep": tot["sweeps"] / max(1, tot["warm_substeps"]),
+            "plain_sweeps": sc.iterations,
+            "mean_residual_ratio": ratio_sum / max(1, tot["warm_substeps"]), "max_residual_ratio": ratio_max,
+            **tot}
 
 
 def residual_after(g, dt):
@@ -255,7 +329,7 @@ def main(argv=None):
     import time
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="beam450", choices=["beam450", "beam98k", "boxes512"])
+    ap.add_argument("--workload", default="beam450", choices=["beam450", "beam98k", "twist98k", "boxes512"])
     ap.add_argument("--train-seeds", type=int, default=256, help="training trajectories")
     ap.add_argument("--bodies-per-handle", type=int, default=64, help="trajectories run as one handle's bodies")
     ap.add_argument("--frames", type=int, default=60)
@@ -269,8 +343,13 @@ def main(argv=None):
                     help="comma list: also time frames with these warm-started iterations per substep")
     ap.add_argument("--rate-seeds", type=int, default=4)
     ap.add_argument("--rate-frames", type=int, default=30)
+    ap.add_argument("--judge-seeds", type=int, default=0,
+                    help="also time judged warm-started frames against plain ones on this many trajectories")
+    ap.add_argument("--judge-check", type=int, default=3, help="sweeps between the judge's residual checks")
+    ap.add_argument("--judge-calibrate", type=int, default=10, help="a plain calibration frame every N frames")
+    ap.add_argument("--save", default="", help="write the trained network to this .npz file")
     args = ap.parse_args(argv)
-    wl = {"beam450": CANTILEVER, "beam98k": BEAM98K, "boxes512": BOXES512}[args.workload]
+    wl = {"beam450": CANTILEVER, "beam98k": BEAM98K, "twist98k": TWIST98K, "boxes512": BOXES512}[args.workload]
     if wl.make_scene is not None:
         args.bodies_per_handle = 1
     t0 = time.perf_counter()
@@ -298,6 +377,13 @@ def main(argv=None):
                                      "fallbacks": int(sum(r["fallback"] for r in res)),
                                      "same_start": all(r["same_start"] for r in res),
                                      "sweep_fraction": float(its.mean() / wl.iterations)}
+    if args.save:
+        save_network(m, args.save, workload=wl.name, train_trajectories=args.train_seeds, frames=args.frames,
+                     keep=args.keep, steps=args.steps, loss_first=losses[0], loss_last=losses[-1])
+    if args.judge_seeds:
+        line["judged"] = judged_rate(m, list(range(60000, 60000 + args.judge_seeds)), frames=args.rate_frames,
+                                     lead_frames=args.eval_frame, check_every=args.judge_check,
+                                     calibrate_every=args.judge_calibrate, workload=wl)
     if args.rate_k:
         line["frame_rate"] = frame_rate(m, list(range(60000, 60000 + args.rate_seeds)),
                                         [int(v) for v in args.rate_k.split(",")], frames=args.rate_frames,

@@ -6,8 +6,8 @@ FP32 noise floor beside it.
 The sequential Gauss-Seidel loop amplifies rounding differences by x3-30
 per sweep, so no FP32 run can track the FP64 oracle to a fixed bound over
 many frames; the yardstick is the spread between the oracle and the oracle
-restarted from FP32-rounded initial positions (oracle.noise_floor).  The
-GPU must stay within 20x of it.  Run with -s to see the per-configuration
+restarted from FP32-rounded initial positions (oracle.noise_floor, the
+larger of two nudge seeds).  The GPU must stay within 2x of it.  Run with -s to see the per-configuration
 errors (max vertex error / bounding-box diagonal).
 """
 import os
@@ -41,8 +41,8 @@ def test_config_one_frame_vs_oracle(capi_mod, oracle_mod, name):
     assert np.all(np.isfinite(x))
     diag = sc.bbox_diag()
     err = float(np.abs(x - o.get()).max())
-    floor = oracle_mod.noise_floor(sc, 1, order, off, threads=threads)
+    floor = oracle_mod.noise_floor(sc, 1, order, off, threads=threads, n_seeds=2)
     mode = ["auto", "graph", "persistent", "cluster", "wavefront"][g.stats().exec_mode]
     print(f"\n{name}: mode {mode}, GPU vs FP64 oracle {err / diag:.3e} x diag, "
           f"oracle FP32 noise floor {floor / diag:.3e} x diag, ratio {err / max(floor, 1e-30):.2f}")
-    assert err < 20 * floor + 1e-6 * diag
+    assert err < 2 * floor + 1e-6 * diag

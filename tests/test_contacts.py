@@ -134,8 +134,8 @@ def test_body_contacts_every_mode(capi_mod, oracle_mod, mode):
     o.step(1)
     assert g.stats().n_body_contacts == o.L.orc_n_body_contacts(o.h)
     order, off = g.tet_order()
-    floor = oracle_mod.noise_floor(sc, 1, order, off)
-    assert np.abs(g.positions() - o.get()).max() < 20 * floor + 1e-7
+    floor = oracle_mod.noise_floor(sc, 1, order, off, n_seeds=2)
+    assert np.abs(g.positions() - o.get()).max() < 2 * floor + 1e-7
 
 
 @pytest.mark.gpu

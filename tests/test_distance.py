@@ -153,9 +153,11 @@ def test_gpu_springs_one_sweep(capi_mod, oracle_mod, mode, beta):
     xg = g.get_predicted(-1).astype(np.float64)
     xo = o.get(oracle_mod.FIELD_XI)
     # nearly rigid springs amplify rounding within one sweep (x50 measured):
-    # the floor is the oracle's own spread under a 1e-7 m perturbation
+    # the floor is the oracle's own spread under one 1e-7 m perturbation of
+    # the start, while the GPU rounds every operation of the sweep in FP32
+    # (measured 2.25x that floor)
     floor = one_sweep_floor(sc, oracle_mod, g, x0, v0)
-    assert np.abs(xg - xo).max() < max(SWEEP_TOL * sc.bbox_diag(), 20 * floor)
+    assert np.abs(xg - xo).max() < max(SWEEP_TOL * sc.bbox_diag(), 4 * floor)
     lg, lo = g.distance_lambdas(), o.distance_lambdas()
     assert np.abs(lg - lo).max() <= 1e-2 * np.abs(lo).max() + 1e-12
     g.close()

@@ -7,7 +7,8 @@ whole frames the sequential loop amplifies rounding differences (a 1e-12 m
 perturbation grows to 1e-4 m within a frame of the 450-tet beam, see
 test_oracle.py), so multi-frame positions are compared against the oracle's
 own noise floor: the spread between the oracle and the oracle restarted from
-FP32-rounded initial positions.
+FP32-rounded initial positions (the larger of two nudge seeds); the GPU must
+stay within 2x of it.
 """
 import numpy as np
 import pytest
@@ -45,7 +46,7 @@ def sweeps(g, o, oracle, dt, k):
 def noise_floor(scene, oracle, frames, seed=0):
     from sbs_gb300 import capi
     order, off = capi.plan_sweep(scene)
-    return oracle.noise_floor(scene, frames, order, off, seed)
+    return oracle.noise_floor(scene, frames, order, off, seed, n_seeds=2)
 
 
 @pytest.mark.parametrize("pre", [0, 5])
@@ -119,7 +120,7 @@ def test_reference_meshes_first_frame(capi_mod, oracle_mod, name):
     g.step(1)
     err = np.abs(g.positions() - d[f"{name}_x1"]).max() / sc.bbox_diag()
     floor = noise_floor(sc, oracle_mod, 1) / sc.bbox_diag()
-    assert err < max(20 * floor, SWEEP_TOL)
+    assert err < max(2 * floor, SWEEP_TOL)
 
 
 def test_beam450_frames_within_noise_floor(capi_mod, oracle_mod):
@@ -129,7 +130,7 @@ def test_beam450_frames_within_noise_floor(capi_mod, oracle_mod):
     o.step(1)
     err = float(np.abs(g.positions() - o.get()).max())
     floor = noise_floor(sc, oracle_mod, 1)
-    assert err < 20 * floor + 1e-7
+    assert err < 2 * floor + 1e-7
 
 
 def test_beam98k_first_frame(capi_mod, oracle_mod):
@@ -139,8 +140,9 @@ def test_beam98k_first_frame(capi_mod, oracle_mod):
     o.step(1)
     x = g.positions()
     assert np.all(np.isfinite(x))
-    err = float(np.abs(x - o.get()).max()) / sc.bbox_diag()
-    assert err < 1e-3
+    err = float(np.abs(x - o.get()).max())
+    order, off = g.tet_order()
+    assert err < 2 * oracle_mod.noise_floor(sc, 1, order, off, threads=16, n_seeds=2) + 1e-7
     b = sc.bodies[0]
     assert np.array_equal(x[b.pinned], b.x0[b.pinned].astype(np.float32))
 
@@ -200,7 +202,7 @@ def test_graph_and_persistent_agree(capi_mod, oracle_mod):
     a.step(1)
     b.step(1)
     floor = noise_floor(sc, oracle_mod, 1)
-    assert np.abs(a.positions() - b.positions()).max() < 20 * floor + 1e-7
+    assert np.abs(a.positions() - b.positions()).max() < 2 * floor + 1e-7
 
 
 @pytest.mark.parametrize("make,frames", [(scenes.beam_c1, 1), (lambda: scenes.beam_twist(16, 4, 4, 0.05), 1)])
@@ -211,7 +213,7 @@ def test_wavefront_matches_oracle(capi_mod, oracle_mod, make, frames):
     g.step(frames)
     o.step(frames)
     floor = noise_floor(sc, oracle_mod, frames)
-    assert np.abs(g.positions() - o.get()).max() < 20 * floor + 1e-7
+    assert np.abs(g.positions() - o.get()).max() < 2 * floor + 1e-7
 
 
 def test_wavefront_with_contacts_and_springs(capi_mod, oracle_mod):
@@ -225,7 +227,7 @@ def test_wavefront_with_contacts_and_springs(capi_mod, oracle_mod):
     b.step(3)
     floor = noise_floor(sc, oracle_mod, 3)
     assert a.stats().n_contacts > 0
-    assert np.abs(a.positions() - b.positions()).max() < 20 * floor + 1e-7
+    assert np.abs(a.positions() - b.positions()).max() < 2 * floor + 1e-7
     hb = scenes.hanging_block()
     a = capi_mod.Solver(hb, exec_mode=capi_mod.EXEC_WAVEFRONT)
     b = capi_mod.Solver(hb, exec_mode=1)
@@ -316,7 +318,7 @@ def test_cluster_mode_one_frame(capi_mod, oracle_mod, make):
     g.step(1)
     o.step(1)
     err = float(np.abs(g.positions() - o.get()).max())
-    assert err < 20 * noise_floor(sc, oracle_mod, 1) + 1e-7
+    assert err < 2 * noise_floor(sc, oracle_mod, 1) + 1e-7
 
 
 def test_cluster_mode_contacts_and_residual(capi_mod, oracle_mod):
@@ -353,7 +355,7 @@ def test_cluster_mode_batch_of_bodies(capi_mod, oracle_mod):
     g.step(1)
     o.step(1)
     err = float(np.abs(g.positions() - o.get()).max())
-    assert err < 20 * oracle_mod.noise_floor(sc, 1, order, off) + 1e-7
+    assert err < 2 * oracle_mod.noise_floor(sc, 1, order, off, n_seeds=2) + 1e-7
 
 
 def test_cluster_mode_deterministic(capi_mod):

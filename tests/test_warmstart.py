@@ -125,8 +125,8 @@ def test_warm_start_cluster_matches_graph(capi_mod, oracle_mod, fit_sweeps):
     xa, xb = a.positions(), b.positions()
     assert np.isfinite(xa).all()
     order, off = capi_mod.plan_sweep(sc)
-    floor = oracle_mod.noise_floor(sc, 3, order, off)
-    assert np.abs(xa - xb).max() < 20 * floor + 1e-6 * sc.bbox_diag()
+    floor = oracle_mod.noise_floor(sc, 3, order, off, n_seeds=2)
+    assert np.abs(xa - xb).max() < 2 * floor + 1e-6 * sc.bbox_diag()
     # the cluster frames ran (one launch per substep plus the global kernels)
     assert a.stats().exec_mode == capi_mod.EXEC_CLUSTER
     a.set_warm_start(None)

@@ -95,8 +95,7 @@ def test_noalloc_many_blocks_match_solver(capi_mod):
     sc = scenes.beam_twist()
     sc.ground = ((0.0, 1.0, 0.0), -0.3)           # plane y = 0.3 cuts the beam's 0.8 m height
     g = capi_mod.Solver(sc)
-    g.step(1)
-    g.detect_contacts()
+    g.detect_contacts()                           # at the initial state, before any frame lifts the beam
     v_ref, qn_ref = g.contacts()
     surf = g.surface()
     assert len(surf) > 4 * 256 and len(v_ref) > 1000
