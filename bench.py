@@ -14,6 +14,12 @@ per 1/60 s frame), i.e. 11,796,480 tet projections.
   roofline the frame kernel's algorithmic bytes per launch / its event time.
   cpu_baseline  the FP64 CPU oracle (a restatement of the reference's
            sequential loop) on a bounded sample, single thread, tet list order.
+  warm_start  the learned warm start with the plain solver as judge on the
+           same workload: frames/s against the plain frames above at equal
+           residual (every substep sweeps until the residual of a plain
+           substep with the full sweep count, recorded by plain calibration
+           frames that are timed too; warm starts worse than the plain start
+           fall back to it).
 
 --impl reference times that CPU restatement with every host thread on the
 same workload: the oracle plans its own colours (first-fit in list order) and
@@ -65,6 +71,58 @@ TRAFFIC = {
     ("beam-98304-snh-twist", "k_cluster_frame"): 7.01e6,
     ("block-2621440-snh", "k_frame_t<false>"): 22.876e9 + 2.582e9,
 }
+
+
+# Trained warm-start networks (sbs_gb300.warmstart.save_network) per workload
+WARM_NETWORKS = {"beam98k": ROOT / "soft-body-simulator_gb300" / "sbs_gb300" / "networks" / "twist98k.npz"}
+
+
+def warm_leg(scene, args, device, flush, plain_ms, exec_mode, net_path):
+    """The learned warm start with the plain solver as judge
+    (sbs_gpu_set_warm_judge) on the same workload: after 3 plain frames, K
+    frames with the network attached, each substep sweeping in chunks until
+    the plain solver's residual after its full sweep count (recorded by a
+    plain calibration frame every `--warm-calibrate` frames, which are timed
+    too) or the cap.  Device time per frame by CUDA events, L2 flushed
+    before every frame, against the plain frames timed above."""
+    import numpy as np
+    import torch
+    from sbs_gb300 import capi, warmstart
+    m = warmstart.load_network(net_path, device)
+    w = capi.Solver(scene, device=device, exec_mode=exec_mode)
+    w.step(3)
+    w.set_warm_start(m, 0)
+    w.set_warm_judge(args.warm_check, 0, args.warm_calibrate, 0.0)
+    w.step(2)                                  # captures the calibration and the judged frame graphs
+    w.set_warm_judge(args.warm_check, 0, args.warm_calibrate, 0.0)   # totals from here
+    ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms.append(w.step_timed())
+    st = w.warm_stats()
+    x = w.positions()
+    w.set_warm_start(None)
+    w.close()
+    m.close()
+    d = dict(np.load(net_path))
+    wm = float(np.mean(ms))
+    return {
+        "network": f"{net_path.name}: trained on {int(d['train_trajectories'])} plain-solver trajectories x "
+                   f"{int(d['frames'])} frames of {str(d['workload'])}, {int(d['steps'])} Adam steps",
+        "judge": {"check_every": args.warm_check, "calibrate_every": args.warm_calibrate,
+                  "max_sweeps": scene.iterations,
+                  "target": "residual of a plain substep with the full sweep count (calibration frames)"},
+        "frames": len(ms), "ms_per_frame": wm, "plain_ms_per_frame": plain_ms,
+        "frames_per_s_ratio": plain_ms / wm,
+        "warm_substeps": int(st.warm_substeps), "calibration_substeps": int(st.calibration_substeps),
+        "mean_sweeps_per_warm_substep": st.sweeps / max(1, st.warm_substeps),
+        "sweep_fraction": st.sweeps / max(1, st.warm_substeps) / scene.iterations,
+        "fallbacks": int(st.fallbacks), "capped": int(st.capped),
+        "mean_residual_ratio": st.mean_residual_ratio, "max_residual_ratio": st.max_residual_ratio,
+        "finite": bool(np.isfinite(x).all()),
+        "frame_ms_samples": ms,
+    }
 
 
 def workload(name: str):
@@ -271,6 +329,9 @@ def main():
     ap.add_argument("--cpu-budget", type=int, default=25_000_000,
                     help="tet projections in the single-thread CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-warm", action="store_true", help="skip the judged warm-start leg")
+    ap.add_argument("--warm-check", type=int, default=3, help="sweeps between the judge's residual checks")
+    ap.add_argument("--warm-calibrate", type=int, default=5, help="a plain calibration frame every N frames")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -341,6 +402,11 @@ def main():
     h2d = V * 12 * 2   # x and v, 3 floats per vertex (permuted on the device)
     d2h = V * 12 * 2   # x and v
 
+    warm = None
+    net = WARM_NETWORKS.get(args.workload)
+    if net is not None and not args.no_warm:
+        warm = warm_leg(scene, args, device, flush, ms_per_frame, solver.stats().exec_mode, net)
+
     if rank != 0:
         solver.close()
         if pg:
@@ -403,6 +469,7 @@ def main():
         "cpu_baseline": cpu,
         "gpu_launches": timed_launches,
         "clocks": clk,
+        "warm_start": warm,
     }
     print(json.dumps(line), flush=True)
     solver.close()

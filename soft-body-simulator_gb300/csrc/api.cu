@@ -1709,7 +1709,22 @@ static sbs_status enqueue_judged_frame(sbs_gpu* h, const StepParams& p, uint32_t
             op.j = h->d_judge;
             if ((s = enqueue_judge_residual(h, p, 1, op, h->st)) != SBS_OK) return s;
             if ((s = enqueue_warm_init(h, p)) != SBS_OK) return s;
-            if ((s = enqueue_judge_loop(h, p, (int)sub)) != SBS_OK) return s;
+            if (h->exec_mode == SBS_EXEC_CLUSTER && h->cl_grid == 1 && h->cd.n_groups == 1) {
+                // one cluster holds the whole scene: the judge runs inside its
+                // kernel, one launch per substep (residual checks reduced
+                // across the cluster's shared memory)
+                StepParams q = p;
+                q.substeps = 1;
+                q.cl_flags = kClExternal | kClCarry | kClJudge;
+                q.judge = h->d_judge;
+                q.judge_xpred = h->wd.xpred;
+                q.judge_chunk = h->judge_chunk;
+                q.judge_cap = h->judge_cap ? h->judge_cap : (uint32_t)p.iterations;
+                q.judge_substep = (int)sub;
+                CU(h, launch_cluster_frame(h->d, h->cd, q, h->sim_time, h->cl_grid, h->cl_block, h->cl_smem, h->st));
+            } else if ((s = enqueue_judge_loop(h, p, (int)sub)) != SBS_OK) {
+                return s;
+            }
         }
         CU(h, launch_finalize(h->d, p, h->st));
     }

@@ -224,6 +224,98 @@ __device__ __forceinline__ void project_tet_dsmem(const ClusterDev& c, const Ste
     }
 }
 
+// ---- plain-solver judge inside the kernel (kClJudge) ----
+// Residual of the group's constraints, sqrt(sum (C + alpha~ lambda)^2) over
+// the tets and the contacts, at the positions in the cluster's slices and the
+// multipliers in shared memory: each CTA sums its own tets and contact
+// vertices (compensated FP32; per thread, then per warp by shuffles, then
+// the warps in order), publishes (sum, error, flag) in its shared memory, and
+// after a cluster barrier every CTA adds the CTAs' partials in rank order, so
+// every CTA gets the same value and takes the same loop decision.  `flag`
+// carries a CTA's view of the device error flag (a staging wait that ran
+// out), made cluster-uniform the same way; the result is then NaN.
+struct ClPart {
+    float s, e, flag, pad;
+};
+
+__device__ __forceinline__ float cl_tet_res2(const ClTet& T, const StepParams& p, float l0, float l1) {
+    const float4 q0 = ld_dsmem(T.a0), q1 = ld_dsmem(T.a1), q2 = ld_dsmem(T.a2), q3 = ld_dsmem(T.a3);
+    const f3 x0 = mk(q0), x1 = mk(q1), x2 = mk(q2), x3 = mk(q3);
+    if (T.snh) {
+        float r2, E;
+        snh_residual(x0, x1, x2, x3, mk(T.a), mk(T.b), mk(T.c), fabsf(T.a.w), T.b.w, T.c.w, p.inv_dt2, l0, l1, r2,
+                     E);
+        return r2;
+    }
+    TetEval e;
+    stvk_eval(x0, x1, x2, x3, mk(T.a), mk(T.b), mk(T.c), T.a.w, T.b.w, T.c.w, e);
+    const float h = e.C + p.stvk_alpha_tilde * l0;
+    return h * h;
+}
+
+__device__ __forceinline__ double cl_residual(const SceneDev& s, const ClusterDev& c, const StepParams& p,
+                                              uint32_t n_col, const uint32_t* cb, const uint32_t* ce,
+                                              const uint32_t* lbase, const float* lam_s, const uint32_t* clist,
+                                              uint32_t ncont, const float4* xi, const float4* rec, const float4* bn,
+                                              int S, uint32_t xi_base, bool bad, ClPart* part, CSum* warp_sum,
+                                              double* out) {
+    CSum acc{0.f, 0.f};
+    for (uint32_t col = 0; col < n_col; ++col) {
+        const uint32_t b = cb[col], e = ce[col];
+        const float* lb = lam_s + lbase[col] - b;
+        for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
+            acc.add(cl_tet_res2(cl_load_tet(s, c, tt, xi_base), p, lb[tt], lb[tt + c.lcap]));
+    }
+    for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
+        const uint32_t i = clist[k];
+        const float4 x = xi[i];
+        for (int sl = 0; sl < S; ++sl) {
+            const float4 r = rec[(size_t)i * S + sl];
+            if (isnan(r.x)) continue;
+            float nx, ny, nz;
+            if (sl < p.n_planes) {
+                nx = p.planes[sl].nx; ny = p.planes[sl].ny; nz = p.planes[sl].nz;
+            } else {
+                const float4 nn = bn[i];
+                nx = nn.x; ny = nn.y; nz = nn.z;
+            }
+            const float C_ = (x.x - r.x) * nx + (x.y - r.y) * ny + (x.z - r.z) * nz;
+            if (C_ < 0.0f) {
+                const float h = C_ + p.contact_alpha_tilde * r.w;
+                acc.add(h * h);
+            }
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        CSum o{__shfl_down_sync(0xffffffffu, acc.s, off), __shfl_down_sync(0xffffffffu, acc.e, off)};
+        acc.merge(o);
+    }
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    if (lane == 0) warp_sum[wid] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        CSum t = warp_sum[0];
+        for (uint32_t w = 1; w < (blockDim.x + 31) / 32; ++w) t.merge(warp_sum[w]);
+        const bool b = bad || *(volatile int*)s.err != 0;
+        *part = ClPart{t.s, t.e, b ? 1.0f : 0.0f, 0.0f};
+    }
+    cluster_sync();
+    if (threadIdx.x == 0) {
+        const uint32_t a = smem_addr(part);
+        CSum t{0.f, 0.f};
+        bool any_bad = false;
+        for (uint32_t r = 0; r < c.cluster_size; ++r) {
+            const float4 q = ld_dsmem(map_rank(a, r));
+            t.merge(CSum{q.x, q.y});
+            any_bad |= q.z != 0.0f;
+        }
+        const double sq = (double)t.s + (double)t.e;
+        *out = any_bad ? __longlong_as_double(0x7ff8000000000000ll) : (sq > 0.0 ? sqrt(sq) : 0.0);
+    }
+    __syncthreads();
+    return *out;
+}
+
 // Shared memory per CTA: two staging buffers for the tet records of one
 // colour phase (4 * c.stage float4 each: packed ids, DmInv rows; filled one
 // phase ahead while the current phase projects), xi[slice], xn[slice],
@@ -231,6 +323,9 @@ __device__ __forceinline__ void project_tet_dsmem(const ClusterDev& c, const Ste
 // contact records rec[slice * n_planes] (q.xyz, lambda; q.x = NaN when the
 // vertex has no contact with that plane), their slots in the global contact
 // list gidx[slice * n_planes], and the CTA's contact vertex list clist[slice].
+// JUDGE: the kernel of judged warm-started substeps (kClJudge); the plain
+// instantiation carries none of the judge's code.
+template <bool JUDGE>
 __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, ClusterDev c, StepParams p,
                                                                      double t0) {
     extern __shared__ float4 sm[];
@@ -253,6 +348,9 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
     // group, kept on chip: they head every colour phase's dependency chain
     __shared__ uint32_t s_cb[kMaxColours], s_ce[kMaxColours], s_lb[kMaxColours];
     __shared__ __align__(8) unsigned long long s_mb[2];   // one mbarrier per staging buffer
+    __shared__ __align__(16) ClPart s_part;               // the judge's residual partial of this CTA
+    __shared__ CSum s_wsum[kClusterMaxBlock / 32];
+    __shared__ double s_res;
     const uint32_t xi_base = smem_addr(xi);
     const uint32_t stg_base = smem_addr(stg), stg_bytes = c.stage * 64u, mb_base = smem_addr(s_mb);
     // colour phases run so far (all groups): staging buffer ph & 1, whose
@@ -280,7 +378,9 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
         }
         __syncthreads();
         // the group's first colour phase: its records arrive while the slice loads
-        if (c.stage && threadIdx.x == 0 && gd.n_col > 0 && p.substeps > 0 && p.iterations > 0)
+        // (judged substeps issue it at the start of each chunk of sweeps instead)
+        constexpr bool judged = JUDGE;
+        if (c.stage && threadIdx.x == 0 && gd.n_col > 0 && p.substeps > 0 && p.iterations > 0 && !judged)
             stage_issue(s, c, s_cb[0], s_ce[0], stg_base + (ph & 1u) * stg_bytes, mb_base + (ph & 1u) * 8u);
         const bool ext = (p.cl_flags & kClExternal) != 0;
         // a further chunk of the same substep's sweeps: the contact
@@ -433,7 +533,43 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                 xi[i] = make_float4(x.x + v.x * p.dt, x.y + v.y * p.dt, x.z + v.z * p.dt, w);
             }
             cluster_sync();
-            for (int it = 0; it < p.iterations; ++it) {
+            // Sweeps: p.iterations of them, or under the judge chunks of
+            // judge_chunk until the residual reaches the target.
+            const uint32_t chunk = judged ? p.judge_chunk : 1u;
+            bool go = chunk > 0;
+            uint32_t done = 0;       // sweeps run in this substep
+            bool fb = false;
+            double r_now = 0.0, target = 0.0;
+            if (judged) {
+                target = p.judge->target[p.judge_substep];
+                const double r_plain0 = p.judge->r_plain0;
+                const double r_warm = cl_residual(s, c, p, gd.n_col, s_cb, s_ce, s_lb, lam_s, clist, ncont, xi, rec,
+                                                  bn, S, xi_base, stage_bad, &s_part, s_wsum, &s_res);
+                // a warm start not below the plain start's residual is discarded
+                fb = !(r_warm < r_plain0);
+                if (fb) {
+                    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) xi[i] = p.judge_xpred[own0 + i];
+                    for (uint32_t col = 0; col < gd.n_col; ++col) {
+                        const uint32_t b = s_cb[col], e = s_ce[col];
+                        float* lb = lam_s + s_lb[col] - b;
+                        for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x) {
+                            lb[tt] = 0.0f;
+                            lb[tt + c.lcap] = 0.0f;
+                        }
+                    }
+                    cluster_sync();
+                }
+                r_now = fb ? r_plain0 : r_warm;
+                go = !(r_now <= target) && chunk <= p.judge_cap;
+            }
+            for (int it = 0; judged ? go : it < p.iterations; ++it) {
+                const uint32_t kin = judged ? (uint32_t)it % chunk : 0u;   // sweep within the chunk
+                if (judged && kin == 0 && c.stage && threadIdx.x == 0 && gd.n_col > 0) {
+                    // the chunk's first colour phase: its records into the buffer
+                    // whose readers all passed a cluster barrier behind us
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    stage_issue(s, c, s_cb[0], s_ce[0], stg_base + (ph & 1u) * stg_bytes, mb_base + (ph & 1u) * 8u);
+                }
                 const bool first = it == 0;                                 // contacts start from 0
                 const bool first_lam = first && !(p.cl_flags & kClCarry);  // elastic multipliers
                 // contacts: own vertices only (collision_constraint.cpp:21-41)
@@ -471,8 +607,10 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                     float* lb = lam_s + s_lb[col] - b;
                     if (c.stage) {
                         const uint32_t buf = ph & 1u;
-                        if (threadIdx.x == 0 &&
-                            !(sub + 1 == p.substeps && it + 1 == p.iterations && col + 1 == gd.n_col)) {
+                        const bool last_phase = judged ? (kin + 1 == chunk && col + 1 == gd.n_col)
+                                                       : (sub + 1 == p.substeps && it + 1 == p.iterations &&
+                                                          col + 1 == gd.n_col);
+                        if (threadIdx.x == 0 && !last_phase) {
                             // next phase's records into the other buffer, whose
                             // readers all passed the cluster barrier behind us
                             const uint32_t nc = col + 1 == gd.n_col ? 0u : col + 1;
@@ -501,6 +639,26 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                     }
                     cluster_sync();
                 }
+                if (judged && kin + 1 == chunk) {
+                    done += chunk;
+                    r_now = cl_residual(s, c, p, gd.n_col, s_cb, s_ce, s_lb, lam_s, clist, ncont, xi, rec, bn, S,
+                                        xi_base, stage_bad, &s_part, s_wsum, &s_res);
+                    go = !(r_now <= target) && done + chunk <= p.judge_cap && !isnan(r_now);
+                }
+            }
+            if (judged && rank == 0 && threadIdx.x == 0) {
+                // the judge's totals (as k_judge_end), and the substep's record
+                JudgeDev* j = p.judge;
+                j->fallback = fb ? 1u : 0u;
+                if (fb) j->fallbacks++;
+                j->sweeps = done;
+                j->r_now = r_now;
+                j->warm_substeps++;
+                j->total_sweeps += done;
+                if (!(r_now <= target)) j->capped++;
+                const double ratio = target > 0.0 ? r_now / target : (r_now > 0.0 ? 1e30 : 1.0);
+                j->sum_ratio += ratio;
+                if (ratio > j->max_ratio) j->max_ratio = ratio;
             }
             // velocity update of own vertices (timestep.cpp:48-57)
             for (uint32_t i = threadIdx.x; i < nown && !ext; i += blockDim.x) {
@@ -552,18 +710,25 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
 // to the kernel's static shared memory rather than to this scene's need: a
 // later handle needing less must not make an earlier handle's launch invalid
 // (measured: no change in the frame time).
-cudaError_t cluster_configure(int block, size_t smem) {
-    (void)block;
-    cudaError_t e = cudaFuncSetAttribute(k_cluster_frame, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+template <bool JUDGE>
+static cudaError_t cluster_configure_one(size_t smem) {
+    cudaError_t e = cudaFuncSetAttribute(k_cluster_frame<JUDGE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
     int dev = 0, optin = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
     cudaFuncAttributes fa;
-    if ((e = cudaFuncGetAttributes(&fa, k_cluster_frame)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, k_cluster_frame<JUDGE>)) != cudaSuccess) return e;
     const size_t max_dyn = (size_t)optin > fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
     if (smem > max_dyn) return cudaErrorInvalidValue;
-    return cudaFuncSetAttribute(k_cluster_frame, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dyn);
+    return cudaFuncSetAttribute(k_cluster_frame<JUDGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dyn);
+}
+
+cudaError_t cluster_configure(int block, size_t smem) {
+    (void)block;
+    cudaError_t e = cluster_configure_one<false>(smem);
+    if (e != cudaSuccess) return e;
+    return cluster_configure_one<true>(smem);
 }
 
 cudaError_t cluster_max_active(int cluster_size, int block, size_t smem, int* n) {
@@ -578,7 +743,7 @@ cudaError_t cluster_max_active(int cluster_size, int block, size_t smem, int* n)
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaOccupancyMaxActiveClusters(n, (void*)k_cluster_frame, &cfg);
+    return cudaOccupancyMaxActiveClusters(n, (void*)k_cluster_frame<false>, &cfg);
 }
 
 cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const StepParams& p, double t0,
@@ -596,7 +761,8 @@ cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const S
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     count_launch();
-    return cudaLaunchKernelEx(&cfg, k_cluster_frame, s, c, p, t0);
+    if (p.cl_flags & kClJudge) return cudaLaunchKernelEx(&cfg, k_cluster_frame<true>, s, c, p, t0);
+    return cudaLaunchKernelEx(&cfg, k_cluster_frame<false>, s, c, p, t0);
 }
 
 __global__ void k_store_time(double* t, double v) { *t = v; }

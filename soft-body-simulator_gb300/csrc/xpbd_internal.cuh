@@ -106,7 +106,12 @@ struct StepParams {
     uint32_t colour_split[kMaxColours];  // first SNH tet of each colour
     int n_edge_colours;
     uint32_t edge_start[kMaxEdgeColours + 1];
-    int cl_flags;                // cluster mode, one warm-started substep: kClExternal | kClCarry
+    int cl_flags;                // cluster mode, one warm-started substep: kClExternal | kClCarry | ...
+    // kClJudge: the plain-solver judge inside the cluster kernel
+    struct JudgeDev* judge;
+    const float4* judge_xpred;   // predicted positions (the plain start) of the substep
+    uint32_t judge_chunk, judge_cap;
+    int judge_substep;
 };
 
 // k_cluster_frame flags.  kClExternal: the substep's positions come
@@ -116,9 +121,15 @@ struct StepParams {
 // kClCarry: the elastic multipliers start from lam0/lam1, not from zero.
 // kClContinue: the contact multipliers start from contact_lam (a further
 // chunk of sweeps of the same substep), not from zero.
+// kClJudge (with kClExternal | kClCarry, one cluster running the only group):
+// the plain-solver judge runs inside the kernel - the warm start's residual
+// against the plain start's (JudgeDev::r_plain0), the fallback, and sweeps
+// in chunks of judge_chunk until the residual is at or below the target or
+// the next chunk would pass judge_cap (iterations is then unused).
 constexpr int kClExternal = 1;
 constexpr int kClCarry = 2;
 constexpr int kClContinue = 4;
+constexpr int kClJudge = 8;
 
 // Device state of the plain-solver judge of warm-started substeps
 // (warmstart.cu): residual targets from plain substeps, the running

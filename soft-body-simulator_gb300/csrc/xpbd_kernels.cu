@@ -608,19 +608,6 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
 // Residual and energy with compensated FP32 sums (Neumaier's variant of
 // Kahan summation; pairs combined with Knuth's two-sum).
 
-struct CSum {
-    float s, e;
-    __device__ __forceinline__ void add(float x) {
-        const float t = s + x;
-        if (fabsf(s) >= fabsf(x)) e += (s - t) + x;
-        else e += (x - t) + s;
-        s = t;
-    }
-    __device__ __forceinline__ void merge(const CSum& o) {
-        add(o.s);
-        e += o.e;
-    }
-};
 
 __device__ __forceinline__ CSum block_reduce(CSum v, float* sh) {
     // sh: 2 * blockDim.x floats

@@ -245,6 +245,22 @@ __device__ __forceinline__ bool snh_step(f3 x0, f3 x1, f3 x2, f3 x3, f3 r0, f3 r
 }
 
 // Residual terms of one SNH tet at the current positions.
+// Compensated FP32 sum (Neumaier's variant of Kahan summation; pairs
+// combined with Knuth's two-sum) for residuals and energies.
+struct CSum {
+    float s, e;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        if (fabsf(s) >= fabsf(x)) e += (s - t) + x;
+        else e += (x - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ void merge(const CSum& o) {
+        add(o.s);
+        e += o.e;
+    }
+};
+
 __device__ __forceinline__ void snh_residual(f3 x0, f3 x1, f3 x2, f3 x3, f3 r0, f3 r1, f3 r2, float aV0,
                                              float mu, float lam, float inv_dt2, float lamD, float lamH,
                                              float& res2, float& energy) {
