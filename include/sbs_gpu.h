@@ -130,6 +130,15 @@ sbs_status sbs_gpu_add_body(sbs_gpu* h, const double* x0, const double* x_init, 
                             const uint32_t* tets, uint32_t n_tets, const sbs_gpu_material* mat,
                             const double* mass, int32_t* body_id);
 
+/* A colouring of a body's tets (colours [n_tets of the body], each < 128)
+ * for the sweep order, set before sbs_gpu_finalize: tets of one colour must
+ * share no vertex (SBS_EINVAL at finalize otherwise).  When every tet of the
+ * scene (or of a cluster group) has one and it needs no more colours than
+ * the library's own colouring, it replaces that colouring; e.g. the lattice
+ * colouring of a structured grid, which reaches the lower bound set by the
+ * tets meeting at one vertex.  The reference has no counterpart: it projects
+ * constraints in list order (gauss_seidel_solver.cpp:32-35). */
+sbs_status sbs_gpu_set_tet_colours(sbs_gpu* h, int32_t body, const uint32_t* colours);
 /* Pins vertices (w = 0), as setting particle_t::mass() = 0 does (main.cpp:158-165,
  * particle.cpp:39-49). */
 sbs_status sbs_gpu_pin_vertices(sbs_gpu* h, int32_t body, const uint32_t* verts, uint32_t n);
@@ -313,14 +322,16 @@ sbs_status sbs_gpu_get_stats(sbs_gpu* h, sbs_gpu_stats* st);
  * for this tet list - tets coloured so that no two tets of a colour share a
  * vertex, colours by decreasing size, tets of a colour by model then by the
  * Morton code of the rest centroid.  x0 [3*n_verts], tets [4*n_tets],
- * models [n_tets] or NULL (all StVK); order [n_tets]; offsets [n_colours+1]
+ * models [n_tets] or NULL (all StVK); colours [n_tets] or NULL: a caller's
+ * colouring as sbs_gpu_set_tet_colours takes it (-1: none); order [n_tets];
+ * offsets [n_colours+1]
  * (cap_offsets entries available).  For several bodies pass them
  * concatenated in add order.  The reference has no counterpart: it projects
  * constraints in list order (gauss_seidel_solver.cpp:32-35); permuting its
  * list to this order gives the same sweep as the GPU. */
 sbs_status sbs_gpu_plan_sweep(const double* x0, uint32_t n_verts, const uint32_t* tets, uint32_t n_tets,
-                              const int32_t* models, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
-                              uint32_t* n_colours);
+                              const int32_t* models, const int32_t* colours, uint32_t* order, uint32_t* offsets,
+                              uint32_t cap_offsets, uint32_t* n_colours);
 
 /* Plane-contact detection for callers that cannot allocate device memory.
  * No counterpart in the reference (which has no GPU code); it is the ground

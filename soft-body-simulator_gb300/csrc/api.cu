@@ -67,6 +67,7 @@ struct sbs_gpu {
     std::vector<uint8_t> user_mass;
     std::vector<uint32_t> tets;          // 4 per tet, old global ids
     std::vector<int32_t> tet_model;
+    std::vector<int32_t> tet_hint;       // caller's colour per tet, -1 none (sbs_gpu_set_tet_colours)
     std::vector<double> tet_mu, tet_lam, tet_density;
     std::vector<BodyHost> bodies;
     std::vector<int32_t> kin_group;      // per old vertex, -1 free
@@ -393,8 +394,42 @@ static int colour_tets(const std::vector<uint32_t>& tets, uint32_t n_verts, cons
 // Morton code).  `model` may be null (all StVK).  Outputs: order[k] = tet id
 // projected k-th, offsets (K+1 colour starts), split[c] = first SNH slot of
 // colour c.  Returns the colour count K or -1.
+// A caller's colouring (hint[t] for every tet, e.g. the lattice colouring of
+// a structured grid, which reaches the lower bound of tets meeting at a
+// vertex where the greedy heuristics do not): -1 if some tet has none; -2 if
+// two tets of one colour share a vertex or a colour is >= kMaxColours;
+// otherwise the colour count, with the colours compacted to 0..K-1.
+static int hint_colouring(const uint32_t* tets, uint32_t T, uint32_t V, const int32_t* hint,
+                          std::vector<int32_t>& colour) {
+    if (!hint) return -1;
+    int32_t mx = -1;
+    for (uint32_t t = 0; t < T; ++t) {
+        if (hint[t] < 0) return -1;
+        if (hint[t] >= kMaxColours) return -2;
+        mx = std::max(mx, hint[t]);
+    }
+    std::vector<int32_t> remap(mx + 1, -1);
+    int K = 0;
+    for (uint32_t t = 0; t < T; ++t)
+        if (remap[hint[t]] < 0) remap[hint[t]] = K++;
+    colour.assign(T, 0);
+    std::vector<std::array<uint64_t, 2>> vm(V, {0ull, 0ull});
+    for (uint32_t t = 0; t < T; ++t) {
+        const int c = remap[hint[t]];
+        const uint64_t bit = 1ull << (c & 63);
+        for (int k = 0; k < 4; ++k) {
+            uint64_t& w = vm[tets[4ull * t + k]][c >> 6];
+            if (w & bit) return -2;
+            w |= bit;
+        }
+        colour[t] = c;
+    }
+    return K;
+}
+
 static int plan_sweep(const double* x0, uint32_t V, const uint32_t* tets, uint32_t T, const int32_t* model,
-                      std::vector<uint32_t>& order, std::vector<uint32_t>& offsets, std::vector<uint32_t>& split) {
+                      std::vector<uint32_t>& order, std::vector<uint32_t>& offsets, std::vector<uint32_t>& split,
+                      const int32_t* hint = nullptr, bool* bad_hint = nullptr) {
     auto mdl = [&](uint32_t t) { return model ? model[t] : (int32_t)SBS_MODEL_STVK; };
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (uint32_t i = 0; i < V; ++i)
@@ -413,8 +448,15 @@ static int plan_sweep(const double* x0, uint32_t V, const uint32_t* tets, uint32
     std::iota(morder.begin(), morder.end(), 0u);
     std::stable_sort(morder.begin(), morder.end(), [&](uint32_t a, uint32_t b) { return tm[a] < tm[b]; });
     std::vector<uint32_t> tv(tets, tets + 4ull * T);
-    std::vector<int32_t> colour;
-    const int K = colour_tets(tv, V, morder, colour);
+    std::vector<int32_t> colour, hinted;
+    int K = colour_tets(tv, V, morder, colour);
+    const int Kh = hint_colouring(tets, T, V, hint, hinted);
+    if (bad_hint) *bad_hint = Kh == -2;
+    if (Kh > 0 && (K < 0 || Kh <= K)) {
+        // the caller's colouring needs no more colours than the heuristics
+        K = Kh;
+        colour.swap(hinted);
+    }
     if (K < 0) return -1;
     std::vector<uint32_t> csize(K, 0);
     for (uint32_t t = 0; t < T; ++t) csize[colour[t]]++;
@@ -449,13 +491,15 @@ static int plan_sweep(const double* x0, uint32_t V, const uint32_t* tets, uint32
 extern "C" {
 
 sbs_status sbs_gpu_plan_sweep(const double* x0, uint32_t n_verts, const uint32_t* tets, uint32_t n_tets,
-                              const int32_t* models, uint32_t* order, uint32_t* offsets, uint32_t cap_offsets,
-                              uint32_t* n_colours) {
+                              const int32_t* models, const int32_t* colours, uint32_t* order, uint32_t* offsets,
+                              uint32_t cap_offsets, uint32_t* n_colours) {
     if (!x0 || !tets || n_verts == 0 || n_tets == 0) return fail(nullptr, SBS_EINVAL, "plan: null/empty");
     for (uint64_t i = 0; i < 4ull * n_tets; ++i)
         if (tets[i] >= n_verts) return fail(nullptr, SBS_EINVAL, "plan: vertex index out of range");
     std::vector<uint32_t> ord, off, split;
-    const int K = plan_sweep(x0, n_verts, tets, n_tets, models, ord, off, split);
+    bool bad = false;
+    const int K = plan_sweep(x0, n_verts, tets, n_tets, models, ord, off, split, colours, &bad);
+    if (bad) return fail(nullptr, SBS_EINVAL, "plan: two tets of one given colour share a vertex");
     if (K < 0) return fail(nullptr, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
     if (n_colours) *n_colours = (uint32_t)K;
     if (order) std::copy(ord.begin(), ord.end(), order);
@@ -582,11 +626,23 @@ sbs_status sbs_gpu_add_body(sbs_gpu* h, const double* x0, const double* x_init, 
     for (uint64_t i = 0; i < 4ull * n_tets; ++i) h->tets.push_back(b.v0 + tets[i]);
     for (uint32_t t = 0; t < n_tets; ++t) {
         h->tet_model.push_back(mat->model);
+        h->tet_hint.push_back(-1);
         h->tet_mu.push_back(mu);
         h->tet_lam.push_back(lam);
     }
     h->bodies.push_back(std::move(b));
     if (body_id) *body_id = (int32_t)h->bodies.size() - 1;
+    return SBS_OK;
+}
+
+sbs_status sbs_gpu_set_tet_colours(sbs_gpu* h, int32_t body, const uint32_t* colours) {
+    if (!h || !colours) return fail(h, SBS_EINVAL, "set_tet_colours: null");
+    if (h->finalized) return fail(h, SBS_ESTATE, "set_tet_colours after finalize");
+    if (body < 0 || body >= (int32_t)h->bodies.size()) return fail(h, SBS_EINVAL, "body id");
+    const BodyHost& b = h->bodies[body];
+    for (uint32_t t = 0; t < b.nt; ++t)
+        if (colours[t] >= (uint32_t)kMaxColours) return fail(h, SBS_EINVAL, "set_tet_colours: colour >= 128");
+    for (uint32_t t = 0; t < b.nt; ++t) h->tet_hint[b.t0 + t] = (int32_t)colours[t];
     return SBS_OK;
 }
 
@@ -969,7 +1025,10 @@ plan_again:
             std::vector<uint32_t> lt(4ull * nt);
             for (uint64_t i = 0; i < 4ull * nt; ++i) lt[i] = h->tets[4ull * t0 + i] - ov0;
             std::vector<uint32_t> ord, off, spl;
-            const int Kg = plan_sweep(&h->x0[3ull * ov0], onv, lt.data(), nt, &h->tet_model[t0], ord, off, spl);
+            bool bad = false;
+            const int Kg = plan_sweep(&h->x0[3ull * ov0], onv, lt.data(), nt, &h->tet_model[t0], ord, off, spl,
+                                      &h->tet_hint[t0], &bad);
+            if (bad) return fail(h, SBS_EINVAL, "two tets of one given colour share a vertex");
             if (Kg < 0) return fail(h, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
             const uint32_t base = (uint32_t)h->tet_order.size();
             GroupDesc g;
@@ -989,8 +1048,10 @@ plan_again:
         h->global_modes = false;   // tets are group-major: only the cluster mode runs them
         h->n_colours = (uint32_t)(h->colour_offsets.size() - 1);
     } else {
+        bool bad = false;
         K = plan_sweep(h->x0.data(), V, h->tets.data(), T, h->tet_model.data(), h->tet_order, h->colour_offsets,
-                       split);
+                       split, h->tet_hint.data(), &bad);
+        if (bad) return fail(h, SBS_EINVAL, "two tets of one given colour share a vertex");
         if (K < 0) return fail(h, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
         h->n_colours = (uint32_t)K;
         h->global_modes = true;
@@ -1013,10 +1074,13 @@ plan_again:
         for (size_t c = 0; c + 1 < gcol_start.size(); ++c) maxc = std::max(maxc, gcol_start[c + 1] - gcol_start[c]);
         while (h->cl_size < 16 && (uint64_t)h->cl_size * 256 < maxc) h->cl_size *= 2;
     }
-    // cluster mode: give every tet to the CTA whose vertex slice holds most
-    // of its vertices (gathers then mostly hit the CTA's own shared memory);
-    // within a colour tets are reordered by owner, which leaves each
-    // colour's tet set - and so the sweep - unchanged
+    // cluster mode: give every tet to a CTA whose vertex slice holds some of
+    // its vertices - the one holding most of them (gathers then mostly hit
+    // the CTA's own shared memory) unless that CTA already has its share
+    // (ceil(colour size / C)) of the colour and another candidate has fewer,
+    // tets with a single candidate placed first: a colour phase lasts as long
+    // as its busiest CTA.  Within a colour tets are reordered by owner,
+    // which leaves each colour's tet set - and so the sweep - unchanged
     std::vector<uint32_t> crs, lbs;
     if (h->cl_feasible) {
         const uint32_t C = (uint32_t)h->cl_size;
@@ -1032,17 +1096,38 @@ plan_again:
             for (uint32_t col = 0; col < g.n_col; ++col) {
                 const uint32_t b = gcol_start[g.col_base + col], e = gcol_start[g.col_base + col + 1];
                 std::vector<std::vector<uint32_t>> by(C);
+                const uint32_t share = (e - b + C - 1) / C;
+                std::vector<uint32_t> load(C, 0), maj(e - b);
+                std::vector<std::array<uint32_t, 4>> cand(e - b);
+                std::vector<uint8_t> ncand(e - b);
                 for (uint32_t k = b; k < e; ++k) {
                     const uint32_t* q = &h->tets[4ull * h->tet_order[k]];
                     uint32_t r[4], best = 0, bestn = 0;
                     for (int i = 0; i < 4; ++i) r[i] = (old_to_new[q[i]] - g.v0) / slice;
+                    uint8_t nc = 0;
                     for (int i = 0; i < 4; ++i) {
                         uint32_t n = 0;
                         for (int j = 0; j < 4; ++j) n += r[j] == r[i];
                         if (n > bestn || (n == bestn && r[i] < best)) { best = r[i]; bestn = n; }
+                        bool seen = false;
+                        for (int j = 0; j < nc; ++j) seen |= cand[k - b][j] == r[i];
+                        if (!seen) cand[k - b][nc++] = r[i];
                     }
-                    by[best].push_back(h->tet_order[k]);
+                    maj[k - b] = best;
+                    ncand[k - b] = nc;
                 }
+                std::vector<uint32_t> owner_of(e - b);
+                for (int pass = 0; pass < 2; ++pass)   // single-candidate tets, then the rest
+                    for (uint32_t i = 0; i < e - b; ++i) {
+                        if ((ncand[i] == 1) != (pass == 0)) continue;
+                        uint32_t o = maj[i];
+                        if (load[o] >= share)
+                            for (int j = 0; j < ncand[i]; ++j)
+                                if (load[cand[i][j]] < load[o]) o = cand[i][j];
+                        owner_of[i] = o;
+                        load[o]++;
+                    }
+                for (uint32_t k = b; k < e; ++k) by[owner_of[k - b]].push_back(h->tet_order[k]);
                 uint32_t k = b;
                 for (uint32_t rr = 0; rr < C; ++rr) {
                     crs.push_back(k);
@@ -1675,6 +1760,22 @@ static sbs_status enqueue_judge_loop(sbs_gpu* h, const StepParams& p, int sub) {
 
 static sbs_status enqueue_judged_frame(sbs_gpu* h, const StepParams& p, uint32_t substeps, uint32_t iterations,
                                        bool calibrate) {
+    if (calibrate && h->exec_mode == SBS_EXEC_CLUSTER && h->cl_grid == 1 && h->cd.n_groups == 1) {
+        // one cluster holds the scene: the plain frame kernel itself records
+        // each substep's final residual and prediction (kClCalibrate)
+        StepParams q = p;
+        q.cl_flags = kClCalibrate;
+        q.judge = h->d_judge;
+        q.judge_xpred = h->wd.xpred;
+        CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+        if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
+        CU(h, launch_cluster_frame(h->d, h->cd, q, h->sim_time, h->cl_grid, h->cl_block, h->cl_smem, h->st));
+        CU(h, launch_end_frame(h->d, h->st));
+        double t_end = h->sim_time;
+        for (uint32_t k = 0; k < substeps; ++k) t_end += p.dt_d;
+        CU(h, launch_store_time(h->d.time, t_end, h->st));
+        return SBS_OK;
+    }
     CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
     CU(h, launch_detect_ground(h->d, p, h->st));
     if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
@@ -1769,8 +1870,15 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
             return fail(h, SBS_EINVAL, "judged frames take at most 64 substeps");
         const bool calibrate = !h->judge_target_valid ||
                                (h->judge_calib_every > 0 && h->judged_frames % h->judge_calib_every == 0);
-        const GraphKey key{dt, substeps, iterations, calibrate ? 3 : (h->xpred_valid ? 2 : 1)};
-        sbs_status s = run_graph(h, key, [&]() { return enqueue_judged_frame(h, p, substeps, iterations, calibrate); });
+        sbs_status s;
+        if (calibrate && h->exec_mode == SBS_EXEC_CLUSTER && h->cl_grid == 1 && h->cd.n_groups == 1) {
+            // one launch of the frame kernel, which takes the frame's start
+            // time as a parameter: launched directly, like the plain frame
+            s = enqueue_judged_frame(h, p, substeps, iterations, true);
+        } else {
+            const GraphKey key{dt, substeps, iterations, calibrate ? 3 : (h->xpred_valid ? 2 : 1)};
+            s = run_graph(h, key, [&]() { return enqueue_judged_frame(h, p, substeps, iterations, calibrate); });
+        }
         if (s) return s;
         h->xpred_valid = true;
         h->judged_frames++;
@@ -1863,7 +1971,7 @@ static sbs_status autotune_modes(sbs_gpu* h, double dt, uint32_t substeps, uint3
         maxc = std::max(maxc, h->colour_offsets[c + 1] - h->colour_offsets[c]);
     const int need = std::max(1, (int)((maxc + 31) / 32));
     if (h->cl_feasible)
-        for (int blk : {256, 512}) cands.push_back({SBS_EXEC_CLUSTER, blk, 0});
+        for (int blk : {256, 320, 384, 512}) cands.push_back({SBS_EXEC_CLUSTER, blk, 0});
     for (int blk : {128, 256}) {
         if (!h->global_modes) break;
         int occ = 0;

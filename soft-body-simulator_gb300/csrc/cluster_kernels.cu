@@ -379,7 +379,10 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
         __syncthreads();
         // the group's first colour phase: its records arrive while the slice loads
         // (judged substeps issue it at the start of each chunk of sweeps instead)
-        constexpr bool judged = JUDGE;
+        // a judged substep (kClJudge), or a calibration frame (kClCalibrate):
+        // plain substeps that record their final residuals as the targets
+        const bool calib = JUDGE && (p.cl_flags & kClCalibrate) != 0;
+        const bool judged = JUDGE && !calib;
         if (c.stage && threadIdx.x == 0 && gd.n_col > 0 && p.substeps > 0 && p.iterations > 0 && !judged)
             stage_issue(s, c, s_cb[0], s_ce[0], stg_base + (ph & 1u) * stg_bytes, mb_base + (ph & 1u) * 8u);
         const bool ext = (p.cl_flags & kClExternal) != 0;
@@ -532,6 +535,10 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                 vv[i] = v;
                 xi[i] = make_float4(x.x + v.x * p.dt, x.y + v.y * p.dt, x.z + v.z * p.dt, w);
             }
+            if (calib) {
+                // the prediction, for the next warm substep's previous-displacement feature
+                for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) p.judge_xpred[own0 + i] = xi[i];
+            }
             cluster_sync();
             // Sweeps: p.iterations of them, or under the judge chunks of
             // judge_chunk until the residual reaches the target.
@@ -644,6 +651,14 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                     r_now = cl_residual(s, c, p, gd.n_col, s_cb, s_ce, s_lb, lam_s, clist, ncont, xi, rec, bn, S,
                                         xi_base, stage_bad, &s_part, s_wsum, &s_res);
                     go = !(r_now <= target) && done + chunk <= p.judge_cap && !isnan(r_now);
+                }
+            }
+            if (calib) {
+                const double r = cl_residual(s, c, p, gd.n_col, s_cb, s_ce, s_lb, lam_s, clist, ncont, xi, rec, bn, S,
+                                             xi_base, stage_bad, &s_part, s_wsum, &s_res);
+                if (rank == 0 && threadIdx.x == 0) {
+                    p.judge->target[sub < kMaxJudgeSubsteps ? sub : kMaxJudgeSubsteps - 1] = r;
+                    p.judge->calib_substeps++;
                 }
             }
             if (judged && rank == 0 && threadIdx.x == 0) {
@@ -761,7 +776,7 @@ cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const S
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     count_launch();
-    if (p.cl_flags & kClJudge) return cudaLaunchKernelEx(&cfg, k_cluster_frame<true>, s, c, p, t0);
+    if (p.cl_flags & (kClJudge | kClCalibrate)) return cudaLaunchKernelEx(&cfg, k_cluster_frame<true>, s, c, p, t0);
     return cudaLaunchKernelEx(&cfg, k_cluster_frame<false>, s, c, p, t0);
 }
 

@@ -109,7 +109,7 @@ struct StepParams {
     int cl_flags;                // cluster mode, one warm-started substep: kClExternal | kClCarry | ...
     // kClJudge: the plain-solver judge inside the cluster kernel
     struct JudgeDev* judge;
-    const float4* judge_xpred;   // predicted positions (the plain start) of the substep
+    float4* judge_xpred;         // predicted positions (the plain start) of the substep
     uint32_t judge_chunk, judge_cap;
     int judge_substep;
 };
@@ -130,6 +130,10 @@ constexpr int kClExternal = 1;
 constexpr int kClCarry = 2;
 constexpr int kClContinue = 4;
 constexpr int kClJudge = 8;
+// kClCalibrate (one cluster running the only group, a plain frame): after
+// each substep's sweeps the residual goes to JudgeDev::target[substep], and
+// each substep's prediction to judge_xpred.
+constexpr int kClCalibrate = 16;
 
 // Device state of the plain-solver judge of warm-started substeps
 // (warmstart.cu): residual targets from plain substeps, the running

@@ -120,7 +120,8 @@ def load(build: bool = True):
         "sbs_gpu_get_stats": [P, C.POINTER(Stats)],
         "sbs_gpu_destroy": [P],
         "sbs_gpu_plan_sweep": [f64, C.c_uint32, u32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
-                               C.c_uint32, C.POINTER(C.c_uint32)],
+                               C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)],
+        "sbs_gpu_set_tet_colours": [P, C.c_int32, u32],
         "sbs_gpu_get_candidates": [P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)],
         "sbs_gpu_set_warm_start": [P, C.c_void_p, C.c_uint32],
         "sbs_gpu_set_warm_judge": [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double],
@@ -212,21 +213,25 @@ def sdf_from_mesh(verts, tris, lo, hi, cells) -> np.ndarray:
 
 def plan_sweep(scene):
     """Sweep order of a scene computed by the library's host code (no GPU):
-    (order, offsets) with bodies concatenated in add order."""
+    (order, offsets) with bodies concatenated in add order; the bodies'
+    colourings (Body.colours) are used as sbs_gpu_finalize uses them."""
     L = load()
     x0 = np.ascontiguousarray(np.concatenate([b.x0 for b in scene.bodies]), np.float64).ravel()
-    tets, models, off = [], [], 0
+    tets, models, hints, off = [], [], [], 0
     for b in scene.bodies:
         tets.append(b.tets.astype(np.uint32) + off)
         models.append(np.full(len(b.tets), b.model, np.int32))
+        hints.append(np.full(len(b.tets), -1, np.int32) if getattr(b, "colours", None) is None
+                     else np.asarray(b.colours, np.int32))
         off += len(b.x0)
     tets = np.ascontiguousarray(np.concatenate(tets), np.uint32).ravel()
     models = np.ascontiguousarray(np.concatenate(models), np.int32)
+    hints = np.ascontiguousarray(np.concatenate(hints), np.int32)
     n = C.c_uint32()
     T = len(models)
     order = np.zeros(T, np.uint32)
     offsets = np.zeros(129, np.uint32)
-    st = L.sbs_gpu_plan_sweep(x0, len(x0) // 3, tets, T, models.ctypes.data, order.ctypes.data,
+    st = L.sbs_gpu_plan_sweep(x0, len(x0) // 3, tets, T, models.ctypes.data, hints.ctypes.data, order.ctypes.data,
                               offsets.ctypes.data, len(offsets), C.byref(n))
     if st != SBS_OK:
         raise SbsError(st, L.sbs_gpu_last_error(None).decode())
@@ -259,6 +264,8 @@ class Solver:
             mass = None if b.mass is None else np.ascontiguousarray(b.mass, np.float64)
             self._check(L.sbs_gpu_add_body(h, x0, _ptr(xi), len(b.x0), tets, len(b.tets),
                                            C.byref(mat), _ptr(mass), C.byref(bid)))
+            if getattr(b, "colours", None) is not None:
+                self._check(L.sbs_gpu_set_tet_colours(h, bid, np.ascontiguousarray(b.colours, np.uint32)))
             if len(b.pinned):
                 self._check(L.sbs_gpu_pin_vertices(h, bid, np.ascontiguousarray(b.pinned, np.uint32),
                                                    len(b.pinned)))

@@ -61,9 +61,23 @@ def test_plan_sweep_is_a_valid_colouring():
 
 
 def test_plan_sweep_colour_count_98k_beam():
-    order, off = capi.plan_sweep(scenes.beam_twist())
+    order, off = capi.plan_sweep(scenes.beam_twist(lattice=False))
     # interior vertices of the 6-tet split touch 24 tets: at least 24 colours
     assert 24 <= len(off) - 1 <= 40
+    # the grid's lattice colouring reaches the bound, 4096 tets per colour
+    order, off = capi.plan_sweep(scenes.beam_twist())
+    assert len(off) - 1 == 24 and np.all(np.diff(off) == 4096)
+    t = scenes.beam_twist().bodies[0].tets
+    for c in range(24):
+        v = t[order[off[c]:off[c + 1]]].ravel()
+        assert len(np.unique(v)) == len(v)
+
+
+def test_plan_sweep_rejects_a_bad_colouring():
+    sc = scenes.beam_twist(8, 4, 4, 0.05)
+    sc.bodies[0].colours = np.zeros(len(sc.bodies[0].tets), np.uint32)   # one colour: tets share vertices
+    with pytest.raises(capi.SbsError):
+        capi.plan_sweep(sc)
 
 
 def test_plan_sweep_rejects_bad_indices():
@@ -71,7 +85,7 @@ def test_plan_sweep_rejects_bad_indices():
     x0 = np.zeros(12)
     tets = np.array([0, 1, 2, 7], np.uint32)
     n = C.c_uint32()
-    assert L.sbs_gpu_plan_sweep(x0, 4, tets, 1, None, None, None, 0, C.byref(n)) == capi.SBS_EINVAL
+    assert L.sbs_gpu_plan_sweep(x0, 4, tets, 1, None, None, None, None, 0, C.byref(n)) == capi.SBS_EINVAL
 
 
 def test_plan_sweep_reports_colour_overflow():
@@ -91,7 +105,7 @@ def test_plan_sweep_reports_colour_overflow():
     cnt = C.c_uint32()
     order = np.zeros(n, np.uint32)
     off = np.zeros(129, np.uint32)
-    st = L.sbs_gpu_plan_sweep(x0, len(x0) // 3, tets, n, None, order.ctypes.data, off.ctypes.data, len(off),
+    st = L.sbs_gpu_plan_sweep(x0, len(x0) // 3, tets, n, None, None, order.ctypes.data, off.ctypes.data, len(off),
                               C.byref(cnt))
     assert st == capi.SBS_ECOLOUR
 

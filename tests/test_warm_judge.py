@@ -104,3 +104,26 @@ def test_judged_warm_start_reaches_the_plain_residual_in_fewer_sweeps(capi_mod, 
         g.close()
     print(f"\njudged cantilever: {sweeps / subs:.1f} sweeps per substep (plain 30), {capped} of {subs} capped")
     assert sweeps / subs < 0.6 * 30
+
+
+def test_judged_cluster_frames_keep_prescribed_motion(capi_mod):
+    """Calibration frames run the frame kernel itself (kinematic targets from
+    the frame's start time), judged frames the per-substep kernel: over
+    several frames of both the x=max face stays on its analytic rotation."""
+    sc = scenes.beam_twist(16, 4, 4, 0.05)
+    g = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_CLUSTER)
+    m = capi_mod.Mlp(device=0, seed=0)
+    m.set_params(np.zeros(m.n_params, np.float32))
+    g.step(1)
+    g.set_warm_start(m, 0)
+    g.set_warm_judge(3, 0, 2, 0.0)            # calibration frames 0, 2, 4
+    g.step(6)
+    st = g.warm_stats()
+    assert st.calibration_substeps == 3 * sc.substeps and st.warm_substeps == 3 * sc.substeps
+    b = sc.bodies[0]
+    ang = b.kin_omega * 7 * sc.frame_dt
+    R = np.array([[1, 0, 0], [0, np.cos(ang), -np.sin(ang)], [0, np.sin(ang), np.cos(ang)]])
+    c = np.array(b.kin_center)
+    want = (b.x0[b.kin_verts] - c) @ R.T + c
+    assert np.abs(g.positions()[b.kin_verts] - want).max() < 1e-6
+    assert np.isfinite(g.positions()).all()
