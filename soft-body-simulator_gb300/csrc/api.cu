@@ -1074,13 +1074,18 @@ plan_again:
         for (size_t c = 0; c + 1 < gcol_start.size(); ++c) maxc = std::max(maxc, gcol_start[c + 1] - gcol_start[c]);
         while (h->cl_size < 16 && (uint64_t)h->cl_size * 256 < maxc) h->cl_size *= 2;
     }
-    // cluster mode: give every tet to a CTA whose vertex slice holds some of
-    // its vertices - the one holding most of them (gathers then mostly hit
-    // the CTA's own shared memory) unless that CTA already has its share
-    // (ceil(colour size / C)) of the colour and another candidate has fewer,
-    // tets with a single candidate placed first: a colour phase lasts as long
-    // as its busiest CTA.  Within a colour tets are reordered by owner,
-    // which leaves each colour's tet set - and so the sweep - unchanged
+    // cluster mode: every tet goes to the CTA whose vertex slice holds most
+    // of its vertices (gathers then mostly hit the CTA's own shared memory).
+    // A colour phase lasts as long as its busiest CTA, so when that leaves a
+    // CTA more tets than 256 threads (or an even split's share, ceil(colour
+    // size / C), rounded up to warps) cover in one pass, the colour is split
+    // evenly: its tets ordered by that
+    // majority CTA and, inside it, from those with most vertices in the
+    // previous CTA's slice to those with most in the next one, then cut into
+    // C consecutive runs - the tets that change CTA are those at the edges of
+    // a region, sharing vertices with the CTA they move to.  Within a colour
+    // tets are reordered by owner, which leaves each colour's tet set - and
+    // so the sweep - unchanged
     std::vector<uint32_t> crs, lbs;
     if (h->cl_feasible) {
         const uint32_t C = (uint32_t)h->cl_size;
@@ -1096,37 +1101,38 @@ plan_again:
             for (uint32_t col = 0; col < g.n_col; ++col) {
                 const uint32_t b = gcol_start[g.col_base + col], e = gcol_start[g.col_base + col + 1];
                 std::vector<std::vector<uint32_t>> by(C);
-                const uint32_t share = (e - b + C - 1) / C;
-                std::vector<uint32_t> load(C, 0), maj(e - b);
-                std::vector<std::array<uint32_t, 4>> cand(e - b);
-                std::vector<uint8_t> ncand(e - b);
+                std::vector<uint32_t> maj(e - b);
+                std::vector<int32_t> lean(e - b);   // vertices in the next slice minus in the previous one
+                std::vector<uint32_t> cnt(C, 0);
                 for (uint32_t k = b; k < e; ++k) {
                     const uint32_t* q = &h->tets[4ull * h->tet_order[k]];
                     uint32_t r[4], best = 0, bestn = 0;
                     for (int i = 0; i < 4; ++i) r[i] = (old_to_new[q[i]] - g.v0) / slice;
-                    uint8_t nc = 0;
                     for (int i = 0; i < 4; ++i) {
                         uint32_t n = 0;
                         for (int j = 0; j < 4; ++j) n += r[j] == r[i];
                         if (n > bestn || (n == bestn && r[i] < best)) { best = r[i]; bestn = n; }
-                        bool seen = false;
-                        for (int j = 0; j < nc; ++j) seen |= cand[k - b][j] == r[i];
-                        if (!seen) cand[k - b][nc++] = r[i];
                     }
+                    int32_t l = 0;
+                    for (int i = 0; i < 4; ++i) l += (r[i] == best + 1) - (r[i] + 1 == best);
                     maj[k - b] = best;
-                    ncand[k - b] = nc;
+                    lean[k - b] = l;
+                    cnt[best]++;
                 }
-                std::vector<uint32_t> owner_of(e - b);
-                for (int pass = 0; pass < 2; ++pass)   // single-candidate tets, then the rest
-                    for (uint32_t i = 0; i < e - b; ++i) {
-                        if ((ncand[i] == 1) != (pass == 0)) continue;
-                        uint32_t o = maj[i];
-                        if (load[o] >= share)
-                            for (int j = 0; j < ncand[i]; ++j)
-                                if (load[cand[i][j]] < load[o]) o = cand[i][j];
-                        owner_of[i] = o;
-                        load[o]++;
-                    }
+                const uint64_t n_col_tets = e - b;
+                const uint32_t maj_max = *std::max_element(cnt.begin(), cnt.end());
+                const uint32_t even_max = (uint32_t)((n_col_tets + C - 1) / C);
+                std::vector<uint32_t> owner_of(maj);
+                if (maj_max > std::max<uint32_t>(256u, (even_max + 31) / 32 * 32)) {
+                    std::vector<uint32_t> idx(e - b);
+                    std::iota(idx.begin(), idx.end(), 0u);
+                    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) {
+                        return maj[x] != maj[y] ? maj[x] < maj[y] : lean[x] < lean[y];
+                    });
+                    for (uint32_t rr = 0; rr < C; ++rr)
+                        for (uint64_t q = n_col_tets * rr / C; q < n_col_tets * (rr + 1) / C; ++q)
+                            owner_of[idx[q]] = rr;
+                }
                 for (uint32_t k = b; k < e; ++k) by[owner_of[k - b]].push_back(h->tet_order[k]);
                 uint32_t k = b;
                 for (uint32_t rr = 0; rr < C; ++rr) {

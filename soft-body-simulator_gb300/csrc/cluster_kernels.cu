@@ -323,9 +323,11 @@ __device__ __forceinline__ double cl_residual(const SceneDev& s, const ClusterDe
 // contact records rec[slice * n_planes] (q.xyz, lambda; q.x = NaN when the
 // vertex has no contact with that plane), their slots in the global contact
 // list gidx[slice * n_planes], and the CTA's contact vertex list clist[slice].
-// JUDGE: the kernel of judged warm-started substeps (kClJudge); the plain
+// MODE: kClModePlain, kClModeJudge (judged warm-started substeps, kClJudge)
+// or kClModeCalib (calibration frames, kClCalibrate); the plain
 // instantiation carries none of the judge's code.
-template <bool JUDGE>
+constexpr int kClModePlain = 0, kClModeJudge = 1, kClModeCalib = 2;
+template <int MODE>
 __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, ClusterDev c, StepParams p,
                                                                      double t0) {
     extern __shared__ float4 sm[];
@@ -381,8 +383,8 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
         // (judged substeps issue it at the start of each chunk of sweeps instead)
         // a judged substep (kClJudge), or a calibration frame (kClCalibrate):
         // plain substeps that record their final residuals as the targets
-        const bool calib = JUDGE && (p.cl_flags & kClCalibrate) != 0;
-        const bool judged = JUDGE && !calib;
+        constexpr bool calib = MODE == kClModeCalib;
+        constexpr bool judged = MODE == kClModeJudge;
         if (c.stage && threadIdx.x == 0 && gd.n_col > 0 && p.substeps > 0 && p.iterations > 0 && !judged)
             stage_issue(s, c, s_cb[0], s_ce[0], stg_base + (ph & 1u) * stg_bytes, mb_base + (ph & 1u) * 8u);
         const bool ext = (p.cl_flags & kClExternal) != 0;
@@ -725,25 +727,26 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
 // to the kernel's static shared memory rather than to this scene's need: a
 // later handle needing less must not make an earlier handle's launch invalid
 // (measured: no change in the frame time).
-template <bool JUDGE>
+template <int MODE>
 static cudaError_t cluster_configure_one(size_t smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_cluster_frame<JUDGE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaError_t e = cudaFuncSetAttribute(k_cluster_frame<MODE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
     int dev = 0, optin = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
     cudaFuncAttributes fa;
-    if ((e = cudaFuncGetAttributes(&fa, k_cluster_frame<JUDGE>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, k_cluster_frame<MODE>)) != cudaSuccess) return e;
     const size_t max_dyn = (size_t)optin > fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
     if (smem > max_dyn) return cudaErrorInvalidValue;
-    return cudaFuncSetAttribute(k_cluster_frame<JUDGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dyn);
+    return cudaFuncSetAttribute(k_cluster_frame<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dyn);
 }
 
 cudaError_t cluster_configure(int block, size_t smem) {
     (void)block;
-    cudaError_t e = cluster_configure_one<false>(smem);
-    if (e != cudaSuccess) return e;
-    return cluster_configure_one<true>(smem);
+    cudaError_t e = cluster_configure_one<kClModePlain>(smem);
+    if (e == cudaSuccess) e = cluster_configure_one<kClModeJudge>(smem);
+    if (e == cudaSuccess) e = cluster_configure_one<kClModeCalib>(smem);
+    return e;
 }
 
 cudaError_t cluster_max_active(int cluster_size, int block, size_t smem, int* n) {
@@ -758,7 +761,7 @@ cudaError_t cluster_max_active(int cluster_size, int block, size_t smem, int* n)
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaOccupancyMaxActiveClusters(n, (void*)k_cluster_frame<false>, &cfg);
+    return cudaOccupancyMaxActiveClusters(n, (void*)k_cluster_frame<kClModePlain>, &cfg);
 }
 
 cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const StepParams& p, double t0,
@@ -776,8 +779,9 @@ cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const S
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     count_launch();
-    if (p.cl_flags & (kClJudge | kClCalibrate)) return cudaLaunchKernelEx(&cfg, k_cluster_frame<true>, s, c, p, t0);
-    return cudaLaunchKernelEx(&cfg, k_cluster_frame<false>, s, c, p, t0);
+    if (p.cl_flags & kClJudge) return cudaLaunchKernelEx(&cfg, k_cluster_frame<kClModeJudge>, s, c, p, t0);
+    if (p.cl_flags & kClCalibrate) return cudaLaunchKernelEx(&cfg, k_cluster_frame<kClModeCalib>, s, c, p, t0);
+    return cudaLaunchKernelEx(&cfg, k_cluster_frame<kClModePlain>, s, c, p, t0);
 }
 
 __global__ void k_store_time(double* t, double v) { *t = v; }

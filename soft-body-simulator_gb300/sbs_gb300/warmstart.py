@@ -15,7 +15,10 @@ solver handle:
 ``TWIST98K`` is the 98,304-tet beam of the benchmark (x=0 face pinned, x=max
 face turned about the beam's axis) with a per-trajectory turning rate
 U(0.5, 1.5) rad/s and jitter seed, no body force: the trajectories a network
-for that scene is trained on.  Trained networks are saved as .npz files
+for that scene is trained on.  Its sweep order is the library's own greedy
+colouring (28 colours): on the grid's lattice colouring (24 colours) the
+solve displacement left after the previous substep's is harder to predict
+per vertex (normalised training loss 0.51 against 0.30).  Trained networks are saved as .npz files
 (parameters and the input/output normalisation, ``save_network``) and loaded
 with ``load_network``.
 """
@@ -63,7 +66,7 @@ def twist98k_trajectory_body(seed: int):
     turning rate and jitter)."""
     rng = np.random.default_rng(seed)
     omega = float(rng.uniform(0.5, 1.5))
-    return scenes.beam_twist(seed=seed + 104729, omega=omega).bodies[0]
+    return scenes.beam_twist(seed=seed + 104729, omega=omega, lattice=False).bodies[0]
 
 
 @dataclass(frozen=True)
