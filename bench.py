@@ -78,6 +78,81 @@ TRAFFIC = {
 WARM_NETWORKS = {"beam98k": ROOT / "soft-body-simulator_gb300" / "sbs_gb300" / "networks" / "twist98k.npz"}
 
 
+def peak_gbs():
+    """(HBM copy bandwidth in GB/s, source): MEASURED_PEAKS.json's hbm_gbs,
+    else the fallback figure of an earlier GB300 measurement."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def other_workload(name, args, device, flush, peak):
+    """One further workload timed like the headline one (default execution
+    mode, 3 warm-up frames, L2 flushed before every timed frame, CUDA events
+    on the solver's stream): ms/frame, tet projections/s and the frame's
+    algorithmic bytes / time against the HBM peak."""
+    import numpy as np
+    import torch
+    from sbs_gb300 import capi
+    sc = workload(name)
+    t0 = time.perf_counter()
+    g = capi.Solver(sc, device=device)
+    for _ in range(3):
+        g.step(1)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    ms = []
+    for _ in range(args.also_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms.append(g.step_timed())
+    st = g.stats()
+    g.close()
+    mean = float(np.mean(ms))
+    fb = frame_bytes(sc, st.n_contacts)
+    ach = fb / (mean * 1e-3) / 1e9
+    return {"workload": sc.name, "tets": sc.n_tets, "vertices": sc.n_verts, "bodies": len(sc.bodies),
+            "substeps": sc.substeps, "iterations": sc.iterations, "material": MATERIALS.get(name, sc.name),
+            "exec_mode": ["auto", "graph", "persistent", "cluster", "wavefront"][st.exec_mode],
+            "colours": st.n_colours, "contacts": st.n_contacts,
+            "frames": len(ms), "ms_per_frame": mean,
+            "value": sc.substeps * sc.iterations * sc.n_tets / (mean * 1e-3), "unit": UNIT,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak[0], "frac": ach / peak[0],
+                         "unit": "GB/s", "bytes_per_frame": fb, "peak_source": peak[1]},
+            "setup_s": setup_s, "frame_ms_samples": ms}
+
+
+def mlp_throughput(args):
+    """Forward pass of the warm-start network on device-resident rows (the
+    vertex count of the 2.6M-tet block by default): the fused tcgen05
+    kernel (path 0) and the per-layer mma.sync GEMMs (path 1), CUDA events on
+    the network's stream after warm-up, median of --steps calls; 70,400 FLOP
+    per row against the measured BF16 peak."""
+    import numpy as np
+    import torch
+    from sbs_gb300 import capi
+    flop_per_row = 2 * (16 * 128 + 2 * 128 * 128 + 128 * 3)
+    m = capi.Mlp(device=0, seed=1)
+    rng = np.random.default_rng(0)
+    x = torch.from_numpy(rng.normal(size=(args.mlp_rows, 16)).astype(np.float32)).cuda()
+    y = torch.empty((args.mlp_rows, 3), dtype=torch.float32, device="cuda")
+    try:
+        peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"])
+    except Exception:
+        peak = 1900.0
+    out = {"metric": "warm-start network forward, rows/s", "rows": args.mlp_rows, "flop_per_row": flop_per_row,
+           "bf16_peak_tflops": peak}
+    for path, name in ((0, "tcgen05_fused"), (1, "mma_sync_layers")):
+        for _ in range(max(3, args.warmup)):
+            m.forward_device(x.data_ptr(), args.mlp_rows, y.data_ptr(), path)
+        ms = sorted(m.forward_device(x.data_ptr(), args.mlp_rows, y.data_ptr(), path) for _ in range(args.steps))
+        med = ms[len(ms) // 2]
+        tf = args.mlp_rows * flop_per_row / (med * 1e-3) / 1e12
+        out[name] = {"ms": med, "rows_per_s": args.mlp_rows / (med * 1e-3), "tflops": tf, "frac": tf / peak}
+    print(json.dumps(out), flush=True)
+
+
 def warm_leg(scene, args, device, flush, plain_ms, exec_mode, net_path):
     """The learned warm start with the plain solver as judge
     (sbs_gpu_set_warm_judge): after 3 plain frames, K frames with the
@@ -347,11 +422,19 @@ def main():
                     help="tet projections in the single-thread CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the judged warm-start leg")
+    ap.add_argument("--also", default="block2m,boxes512",
+                    help="comma list of further workloads timed after the headline one ('' for none)")
+    ap.add_argument("--also-steps", type=int, default=10, help="timed frames of each further workload")
+    ap.add_argument("--mlp", action="store_true",
+                    help="instead: throughput of the warm-start network's forward pass (one JSON line)")
+    ap.add_argument("--mlp-rows", type=int, default=545025)
     ap.add_argument("--warm-check", type=int, default=3, help="sweeps between the judge's residual checks")
     ap.add_argument("--warm-calibrate", type=int, default=5, help="a plain calibration frame every N frames")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mlp:
+        return mlp_throughput(args)
 
     world, rank, local = dist_env()
     import torch
@@ -419,6 +502,10 @@ def main():
     h2d = V * 12 * 2   # x and v, 3 floats per vertex (permuted on the device)
     d2h = V * 12 * 2   # x and v
 
+    others = {}
+    for name in [w for w in args.also.split(",") if w and w != args.workload]:
+        others[name] = other_workload(name, args, device, flush, peak_gbs())
+
     warm = None
     net = WARM_NETWORKS.get(args.workload)
     if net is not None and not args.no_warm:
@@ -432,12 +519,7 @@ def main():
 
     fb = frame_bytes(scene, n_contacts)
     achieved = fb / (ms_per_frame * 1e-3) / 1e9
-    peaks = {}
-    try:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
-    except Exception:
-        peak, peak_src = 6800.0, "fallback"
+    peak, peak_src = peak_gbs()
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -487,6 +569,7 @@ def main():
         "gpu_launches": timed_launches,
         "clocks": clk,
         "warm_start": warm,
+        "other_workloads": others,
     }
     print(json.dumps(line), flush=True)
     solver.close()

@@ -83,6 +83,10 @@ typedef struct sbs_gpu_params {
     int32_t stage_records;        /* cluster mode: 1 (default) copy each colour's tet records
                                      into shared memory one phase ahead (bulk asynchronous
                                      copies); 0 load them from global memory in the phase */
+    int32_t wait_limit_us;        /* bound of every device-side wait of the solver's kernels (grid
+                                     barriers, staging waits) in microseconds, after which the
+                                     kernel stops and the next synchronising call returns
+                                     SBS_ETIMEOUT (0: 2 s) */
 } sbs_gpu_params;
 
 typedef struct sbs_gpu_material {
@@ -237,6 +241,14 @@ sbs_status sbs_gpu_step(sbs_gpu* h, double frame_dt, uint32_t substeps, uint32_t
 /* As sbs_gpu_step, bracketed by CUDA events; waits and stores the frame's
  * device time in stats.last_frame_ms. */
 sbs_status sbs_gpu_step_timed(sbs_gpu* h, double frame_dt, uint32_t substeps, uint32_t iterations);
+/* Test hook for the timeout path, no reference counterpart: the next frame
+ * of the persistent mode starts its grid-barrier arrival count one arrival
+ * short, so its first grid barrier never completes; every CTA gives up after
+ * wait_limit_us, the kernel returns, and the next synchronising call
+ * reports SBS_ETIMEOUT.  That frame is left incomplete; the error is cleared
+ * when reported and later frames run normally.  SBS_ESTATE unless the
+ * handle runs the persistent mode. */
+sbs_status sbs_gpu_withhold_barrier_arrival(sbs_gpu* h);
 
 /* The solver seam alone: resets every multiplier and runs `iterations`
  * sweeps (contacts first, then the elastic colours) on the current predicted

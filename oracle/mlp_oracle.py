@@ -5,7 +5,9 @@ parameters flat as W1[128][16] b1 W2[128][128] b2 W3[128][128] b3 W4[3][128] b4.
 Inputs normalised as (x - mean) / std, outputs multiplied by out_scale.
 Loss: mean over rows of ||z4 - t / out_scale||^2 (z4 = normalised output).
 The GPU kernels' gradients are checked against `loss_grad` here, and
-`loss_grad` itself against central finite differences.
+`loss_grad` itself against central finite differences; `adam` restates the
+optimiser the training kernels apply (Kingma & Ba 2015, bias-corrected
+moments).
 """
 from __future__ import annotations
 
@@ -65,3 +67,19 @@ def loss_grad(p, x, t, mean, std, scale):
         dz = da * s * (1.0 + zs[l - 1] * (1.0 - s))
     flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
     return loss, flat
+
+
+def adam(p, x, t, mean, std, scale, steps: int, lr: float, b1: float = 0.9, b2: float = 0.999,
+         eps: float = 1e-8):
+    """`steps` Adam steps on the full batch (x, t) from parameters p, with
+    moments starting at zero: m = b1 m + (1 - b1) g, v = b2 v + (1 - b2) g^2,
+    p -= lr (m / (1 - b1^k)) / (sqrt(v / (1 - b2^k)) + eps) at step k."""
+    p = np.asarray(p, np.float64).copy()
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    for k in range(1, steps + 1):
+        _, g = loss_grad(p, x, t, mean, std, scale)
+        m = b1 * m + (1 - b1) * g
+        v = b2 * v + (1 - b2) * g * g
+        p -= lr * (m / (1 - b1 ** k)) / (np.sqrt(v / (1 - b2 ** k)) + eps)
+    return p

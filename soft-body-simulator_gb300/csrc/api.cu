@@ -147,6 +147,7 @@ struct sbs_gpu {
     cudaStream_t side = nullptr;      // captures the bodies of the sweep loops
     uint64_t judged_frames = 0;       // judged frames run (calibration ones included)
     bool judge_target_valid = false;
+    bool withhold_arrival = false;    // sbs_gpu_withhold_barrier_arrival: next persistent frame
     double sim_time = 0.0;   // host mirror of the simulation time
     std::vector<uint32_t> seg_split;  // first SNH slot of each colour segment
 
@@ -546,6 +547,7 @@ sbs_status sbs_gpu_params_default(sbs_gpu_params* p) {
     p->candidate_capacity = 0;
     p->check_finite = 1;
     p->stage_records = 1;
+    p->wait_limit_us = 0;
     return SBS_OK;
 }
 
@@ -557,6 +559,7 @@ sbs_status sbs_gpu_create(const sbs_gpu_params* p, sbs_gpu** out) {
     else sbs_gpu_params_default(&prm);
     if (prm.gravity_mode != 0 && prm.gravity_mode != 1) return fail(nullptr, SBS_EINVAL, "gravity_mode");
     if (prm.exec_mode < 0 || prm.exec_mode > 4) return fail(nullptr, SBS_EINVAL, "exec_mode");
+    if (prm.wait_limit_us < 0) return fail(nullptr, SBS_EINVAL, "wait_limit_us");
     if (prm.block_size != 0 && (prm.block_size < 32 || prm.block_size > 512 || prm.block_size % 32))
         return fail(nullptr, SBS_EINVAL, "block_size must be a multiple of 32 in [32, 512]");
     int ndev = 0;
@@ -1287,6 +1290,7 @@ plan_again:
     // 9. device allocations and upload
     SceneDev& d = h->d;
     d.n_verts = V;
+    d.wait_ns = h->prm.wait_limit_us > 0 ? 1000ull * (unsigned long long)h->prm.wait_limit_us : 2000000000ull;
     d.n_tets = T;
     d.n_surf = (uint32_t)h->surf.size();
     d.n_kin = 0;
@@ -1628,7 +1632,13 @@ static sbs_status check_err(sbs_gpu* h) {
     int e = 0;
     CU(h, cudaMemcpyAsync(&e, h->d.err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CU(h, cudaStreamSynchronize(h->st));
-    if (e != 0) return fail(h, (sbs_status)e, "device reported an error (code " + std::to_string(e) + ")");
+    if (e != 0) {
+        // reported once: the flag is cleared so that later frames run (the
+        // frame that set it stopped early and is left incomplete)
+        CU(h, cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+        CU(h, cudaStreamSynchronize(h->st));
+        return fail(h, (sbs_status)e, "device reported an error (code " + std::to_string(e) + ")");
+    }
     return SBS_OK;
 }
 
@@ -1913,11 +1923,16 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
         CU(h, launch_wavefront_frame(h->d, p, 256, h->wave_grid, h->st));
     } else if (h->exec_mode == SBS_EXEC_PERSISTENT) {
         // the frame kernel expects zero live contact counters (it zeroes them
-        // itself at frame end); a standalone detect may have left them set
-        if (h->contacts_live)
-            CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
+        // itself at frame end); a standalone detect or a frame stopped by an
+        // error may have left them set
+        CU(h, cudaMemsetAsync(h->d.counters, 0, (kMaxPlanes + 1) * sizeof(uint32_t), h->st));
         if (h->body_on) CU(h, launch_body_detect(h->d, h->hd, h->st));
         CU(h, cudaMemsetAsync(h->d.bar, 0, 2 * sizeof(unsigned), h->st));   // barrier arrival count
+        if (h->withhold_arrival) {
+            // one arrival short: 0xFFFFFFFF + gridDim arrivals wraps to gridDim - 1
+            CU(h, cudaMemsetAsync(h->d.bar, 0xFF, sizeof(unsigned), h->st));
+            h->withhold_arrival = false;
+        }
         CU(h, launch_persistent_frame(h->d, p, h->pers_block, h->pers_grid, h->st));
     } else {
         const GraphKey key{dt, substeps, iterations, 0};
@@ -2107,6 +2122,15 @@ sbs_status sbs_gpu_step_timed(sbs_gpu* h, double frame_dt, uint32_t substeps, ui
     CU(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
     h->last_frame_ms = ms;
     return check_err(h);
+}
+
+sbs_status sbs_gpu_withhold_barrier_arrival(sbs_gpu* h) {
+    sbs_status s = check_ready(h);
+    if (s) return s;
+    if (h->exec_mode != SBS_EXEC_PERSISTENT || h->mlp)
+        return fail(h, SBS_ESTATE, "withhold_barrier_arrival: the handle does not run persistent frames");
+    h->withhold_arrival = true;
+    return SBS_OK;
 }
 
 sbs_status sbs_gpu_detect_contacts(sbs_gpu* h) {

@@ -111,8 +111,7 @@ __device__ __forceinline__ ClTet cl_load_tet(const SceneDev& s, const ClusterDev
 // (Other arrangements measured slower on the 98k-tet beam: the wait by one
 // thread or a producer warp before the barrier, two phases of lead with three
 // buffers, per-thread cp.async copies.)
-constexpr unsigned long long kStageLimitNs = 2000000000ull;   // 2 s
-constexpr int kErrTimeoutCl = 3;                              // SBS_ETIMEOUT
+constexpr int kErrTimeoutCl = 3;   // SBS_ETIMEOUT
 
 __device__ __forceinline__ unsigned long long cl_ns() {
     unsigned long long t;
@@ -132,8 +131,9 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  ::"r"(dst), "l"(src), "r"(bytes), "r"(mb) : "memory");
 }
-// Bounded wait for phase `parity` of the mbarrier; false after kStageLimitNs.
-__device__ __forceinline__ bool mb_wait(uint32_t mb, uint32_t parity) {
+// Bounded wait for phase `parity` of the mbarrier; false after limit_ns
+// (SceneDev::wait_ns).
+__device__ __forceinline__ bool mb_wait(uint32_t mb, uint32_t parity, unsigned long long limit_ns) {
     unsigned long long t0 = 0;
     for (uint32_t spins = 0;; ++spins) {
         uint32_t done;
@@ -145,7 +145,7 @@ __device__ __forceinline__ bool mb_wait(uint32_t mb, uint32_t parity) {
             : "memory");
         if (done) return true;
         if (spins == 0) t0 = cl_ns();
-        else if ((spins & 15u) == 0 && cl_ns() - t0 > kStageLimitNs) return false;
+        else if ((spins & 15u) == 0 && cl_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
                                         mb_base + (buf ^ 1u) * 8u);
                         }
                         if (b + threadIdx.x < e && !stage_bad) {
-                            if (mb_wait(mb_base + buf * 8u, (ph >> 1) & 1u)) {
+                            if (mb_wait(mb_base + buf * 8u, (ph >> 1) & 1u, s.wait_ns)) {
                                 const float4* B = stg + (size_t)buf * 4 * c.stage;
                                 const uint4* I = reinterpret_cast<const uint4*>(B);
                                 for (uint32_t k = threadIdx.x; k < e - b; k += blockDim.x)

@@ -66,6 +66,7 @@ struct SceneDev {
     uint32_t* nb;
     uint32_t* wave_start;  // [colour * (G + 1) + cta]: first entry of the CTA's tets in wave_idx
     uint32_t* wave_idx;    // tet slots, grouped by (colour, owning CTA)
+    unsigned long long wait_ns;   // bound of every device wait (grid barrier, staging), then SBS_ETIMEOUT
     // reductions
     double* red_out;       // [4]: residual^2 (elastic), energy, residual^2 (contacts), spare
     float* partials;       // per-CTA partial sums for the residual kernel

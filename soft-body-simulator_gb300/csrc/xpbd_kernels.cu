@@ -27,7 +27,6 @@ uint64_t& launch_counter() {
 }
 
 constexpr int kErrTimeout = 3;  // SBS_ETIMEOUT
-constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -59,8 +58,8 @@ __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
 // the CTA barrier before the release add and after the acquire load carries
 // the other threads' writes and reads (release and acquire are cumulative in
 // the PTX memory model); dropping the two __threadfence calls took 18% off a
-// frame of the 98k-tet beam in this mode.  A wait longer than kBarrierLimitNs
-// records SBS_ETIMEOUT.  Returns false when the kernel must stop (timeout
+// frame of the 98k-tet beam in this mode.  A wait longer than `limit_ns`
+// (SceneDev::wait_ns) records SBS_ETIMEOUT.  Returns false when the kernel must stop (timeout
 // here or an error recorded by another CTA).
 __device__ __forceinline__ void grid_arrive(unsigned* bar, unsigned& target) {
     target += gridDim.x;
@@ -68,7 +67,8 @@ __device__ __forceinline__ void grid_arrive(unsigned* bar, unsigned& target) {
     if (threadIdx.x == 0) red_release_add(bar, 1u);
 }
 
-__device__ __forceinline__ bool grid_wait(unsigned* bar, int* err, unsigned target) {
+__device__ __forceinline__ bool grid_wait(unsigned* bar, int* err, unsigned target,
+                                          unsigned long long limit_ns) {
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
         int ok = 1;
@@ -77,7 +77,7 @@ __device__ __forceinline__ bool grid_wait(unsigned* bar, int* err, unsigned targ
         while (ld_acquire(bar) < target) {
             if ((++spins & 63u) == 0) {
                 if (ld_relaxed(err) != 0) { ok = 0; break; }
-                if (global_ns() - t0 > kBarrierLimitNs) {
+                if (global_ns() - t0 > limit_ns) {
                     atomicCAS(err, 0, kErrTimeout);
                     ok = 0;
                     break;
@@ -93,9 +93,10 @@ __device__ __forceinline__ bool grid_wait(unsigned* bar, int* err, unsigned targ
 
 // grid_arrive + grid_wait.  Loads of read-only data issued between the two
 // overlap the wait without holding back the CTA's arrival.
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, unsigned& target) {
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, unsigned& target,
+                                             unsigned long long limit_ns) {
     grid_arrive(bar, target);
-    return grid_wait(bar, err, target);
+    return grid_wait(bar, err, target, limit_ns);
 }
 
 // Work mapping for one phase: 32-item chunks dealt round-robin over CTAs
@@ -471,7 +472,7 @@ __device__ __forceinline__ unsigned ld_relaxed_u(const unsigned* p) {
 // Wavefront wait: warp 0 polls the progress counters of this CTA's
 // neighbours (relaxed loads, all of a lane's in flight at once) until each
 // has finished `need` colour phases, then one acquire fence; bounded by
-// kBarrierLimitNs (then SBS_ETIMEOUT).  The CTA then passes a CTA barrier.
+// s.wait_ns (then SBS_ETIMEOUT).  The CTA then passes a CTA barrier.
 __device__ __forceinline__ bool wave_wait(const SceneDev& s, uint32_t need) {
     __shared__ int s_ok;
     if (threadIdx.x < 32) {
@@ -487,7 +488,7 @@ __device__ __forceinline__ bool wave_wait(const SceneDev& s, uint32_t need) {
                 int stop = 0;
                 if (threadIdx.x == 0) {
                     if (ld_relaxed(s.err) != 0) stop = 1;
-                    else if (global_ns() - t0 > kBarrierLimitNs) {
+                    else if (global_ns() - t0 > s.wait_ns) {
                         atomicCAS(s.err, 0, kErrTimeout);
                         stop = 1;
                     }
@@ -517,7 +518,7 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
             if (k < n) detect_item(s, p, k);
         }
     }
-    if (!grid_barrier(s.bar, s.err, bar_target)) return;
+    if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
     uint32_t cnt[kMaxPlanes];
     for (int pl = 0; pl < kMaxPlanes; ++pl) cnt[pl] = pl < p.n_planes ? min(__ldcg(&s.counters[pl]), s.n_surf) : 0u;
     const uint32_t cnt_body = p.body_contacts ? min(__ldcg(&s.counters[kMaxPlanes]), s.n_surf) : 0u;
@@ -526,7 +527,7 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
     for (int sub = 0; sub < p.substeps; ++sub) {
         const double t_next = t + p.dt_d;
         for_each_vertex(s.n_verts, [&](uint32_t i) { predict_vertex(s, p, i, t_next, has_acc); });
-        if (!grid_barrier(s.bar, s.err, bar_target)) return;
+        if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
         for (int it = 0; it < p.iterations; ++it) {
             const bool first = it == 0;
             uint32_t slot = (!kWave && p.first_tail > 0) ? first_slot(p, 0) : ~0u;
@@ -535,11 +536,11 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
             for (int pl = 0; pl < p.n_planes; ++pl) {
                 if (cnt[pl] == 0) continue;
                 contact_phase(s, (uint32_t)pl * s.n_surf, cnt[pl], p, first);
-                if (!grid_barrier(s.bar, s.err, bar_target)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
             }
             if (cnt_body) {
                 contact_phase(s, (uint32_t)kMaxPlanes * s.n_surf, cnt_body, p, first);
-                if (!grid_barrier(s.bar, s.err, bar_target)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
             }
             if (kWave) {
                 // every colour, each CTA its own slice; wait only for the
@@ -569,32 +570,32 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
                 grid_arrive(s.bar, bar_target);
                 slot = col + 1 < p.first_tail ? first_slot(p, col + 1) : ~0u;
                 if (slot != ~0u) rec = load_tet(s, slot);
-                if (!grid_wait(s.bar, s.err, bar_target)) return;
+                if (!grid_wait(s.bar, s.err, bar_target, s.wait_ns)) return;
             }
             }
             if (!kWave && p.first_tail < p.n_colours) {
                 if (blockIdx.x == 0) tail_phase(s, p, first);
-                if (!grid_barrier(s.bar, s.err, bar_target)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
             }
             if (kWave && (p.n_edge_colours > 0 || (it + 1 < p.iterations && any_contact))) {
                 // distance constraints and the next iteration's contacts touch
                 // vertices of any CTA: a grid barrier before them
-                if (!grid_barrier(s.bar, s.err, bar_target)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
             }
             for (int col = 0; col < p.n_edge_colours; ++col) {
                 for_each_spread(p.edge_start[col], p.edge_start[col + 1],
                                 [&](uint32_t k) { project_edge(s, p, k, first); });
-                if (!grid_barrier(s.bar, s.err, bar_target)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
             }
         }
         if (kWave && !(p.n_edge_colours > 0)) {
             // the velocity update reads every vertex
-            if (!grid_barrier(s.bar, s.err, bar_target)) return;
+            if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
         }
         for_each_vertex(s.n_verts, [&](uint32_t i) { finalize_vertex(s, p, i); });
         t = t_next;
     }
-    if (!grid_barrier(s.bar, s.err, bar_target)) return;
+    if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *s.time = t;
         for (int i = 0; i <= kMaxPlanes; ++i) {

@@ -33,7 +33,7 @@ class Params(C.Structure):
                 ("block_size", C.c_int32), ("ctas_per_sm", C.c_int32),
                 ("tail_threshold", C.c_int32), ("body_contacts", C.c_int32),
                 ("hash_cell", C.c_float), ("candidate_capacity", C.c_uint32),
-                ("check_finite", C.c_int32), ("stage_records", C.c_int32)]
+                ("check_finite", C.c_int32), ("stage_records", C.c_int32), ("wait_limit_us", C.c_int32)]
 
 
 class WarmStats(C.Structure):
@@ -89,6 +89,7 @@ def load(build: bool = True):
         "sbs_gpu_finalize": [P],
         "sbs_gpu_step": [P, C.c_double, C.c_uint32, C.c_uint32],
         "sbs_gpu_step_timed": [P, C.c_double, C.c_uint32, C.c_uint32],
+        "sbs_gpu_withhold_barrier_arrival": [P],
         "sbs_gpu_solve": [P, C.c_double, C.c_uint32],
         "sbs_gpu_predict": [P, C.c_double],
         "sbs_gpu_update_velocities": [P, C.c_double],

@@ -95,6 +95,35 @@ def test_gpu_adam_training_reduces_loss(capi_mod):
 
 
 @pytest.mark.gpu
+def test_gpu_adam_steps_against_fp64_adam(capi_mod):
+    """Three Adam steps on the GPU against the FP64 restatement
+    (mlp_oracle.adam).  The dataset is one row repeated, so every random
+    batch is that row and the GPU's batch gradient is the row's gradient.
+    Adam's first steps move each parameter by about lr in the direction of
+    -sign(gradient), so where the FP64 gradient is clearly nonzero the GPU's
+    BF16 gradients must give the same moves; elsewhere the move stays within
+    the 3 lr the three steps allow."""
+    from oracle import mlp_oracle
+    m = capi_mod.Mlp(seed=9)
+    x1, t1 = (a.astype(np.float32).astype(np.float64) for a in data(1, seed=10))
+    xs, ts = data(4096, seed=11)
+    mean, std, scale = (a.astype(np.float32).astype(np.float64) for a in norm_of(xs, ts))
+    m.set_normalization(mean, std, scale)
+    p0 = m.params().astype(np.float64)
+    m.set_dataset(np.repeat(x1, 4096, axis=0), np.repeat(t1, 4096, axis=0))
+    lr = 1e-3
+    m.train(3, 1024, lr, seed=2)
+    d_gpu = m.params().astype(np.float64) - p0
+    d_ref = mlp_oracle.adam(p0, x1, t1, mean, std, scale, 3, lr) - p0
+    _, g0 = mlp_oracle.loss_grad(p0, x1, t1, mean, std, scale)
+    clear = np.abs(g0) > 1e-2 * np.abs(g0).max()
+    assert clear.sum() > 1000
+    assert np.abs(d_gpu[clear] - d_ref[clear]).max() <= 0.05 * lr
+    assert np.abs(d_gpu).max() <= 3 * lr * (1 + 1e-3)
+    assert np.abs(d_gpu - d_ref).max() <= 6 * lr
+
+
+@pytest.mark.gpu
 def test_gpu_training_is_reproducible(capi_mod):
     """Two trainings from the same seeds end with identical parameters: the
     split-K weight gradients add their K slices in a fixed order."""

@@ -124,3 +124,58 @@ def test_load_scene(capi_mod, tmp_path):
     assert L.sbs_gpu_get_state(h, 0, x.ctypes.data, None) == 0
     assert np.isfinite(x).all() and x.reshape(-1, 3)[:, 1].min() > -0.05
     L.sbs_gpu_destroy(h)
+
+
+# The reference's own data files (data/scenes/scene1.json and the meshes it
+# and the viewer use), copied unchanged under tests/golden/ref_data/.
+REF_DATA = Path(__file__).parent / "golden" / "ref_data"
+
+
+def test_reference_binary_and_ascii_cube_agree(capi_mod):
+    """data/meshes/cube_bin.ply (binary little endian) and cube.ply (ascii)
+    hold the same cube: 8 vertices, 12 triangles."""
+    xa, fa, ta = capi_mod.read_ply(REF_DATA / "meshes" / "cube.ply")
+    xb, fb, tb = capi_mod.read_ply(REF_DATA / "meshes" / "cube_bin.ply")
+    assert xa.shape == (8, 3) and fa.shape == (12, 3) and len(ta) == 0
+    assert np.array_equal(xa, xb) and np.array_equal(fa, fb) and len(tb) == 0
+    assert set(np.unique(xa).tolist()) == {0.0, 1.0}     # the unit cube (colour properties skipped)
+
+
+def test_reference_bar_mesh_parses_as_the_golden_fixture(capi_mod):
+    d = np.load(GOLDEN)
+    x, f, t = capi_mod.read_ply(REF_DATA / "meshes" / "bar_tet.ply")
+    assert np.array_equal(x, d["bar_tet_x0"].astype(np.float32))
+    assert np.array_equal(t, d["bar_tet_tets"]) and len(f) == 0
+
+
+@pytest.mark.gpu
+def test_load_reference_scene1(capi_mod):
+    """data/scenes/scene1.json as the reference ships it: the floor mesh
+    becomes a signed-distance environment, the bar a body rescaled into its
+    box and translated (load_scene.cpp:11-81); it falls onto the floor."""
+    import ctypes as C
+    spec = json.loads((REF_DATA / "scenes" / "scene1.json").read_text())
+    obj = spec["objects"][0]
+    box = tuple(tuple(obj["box"][k][a] for a in "xyz") for k in ("min", "max"))
+    tr = tuple(obj["translation"][a] for a in "xyz")
+    L = capi_mod.load()
+    prm = capi_mod.default_params(exec_mode=1)
+    h = C.c_void_p()
+    assert L.sbs_gpu_create(C.byref(prm), C.byref(h)) == 0
+    mat = capi_mod.Material(0, 1e5, 0.3, 1000.0)
+    first, n = C.c_int32(), C.c_int32()
+    cells = np.array([8, 8, 8], np.uint32)
+    path = str(REF_DATA / "scenes" / "scene1.json").encode()
+    assert L.sbs_gpu_load_scene(h, path, C.byref(mat), cells, 0.5, C.byref(first), C.byref(n)) == 0
+    assert (first.value, n.value) == (0, 1)
+    assert L.sbs_gpu_finalize(h) == 0
+    x0, _, _ = capi_mod.read_ply(REF_DATA / "meshes" / "bar_tet.ply")
+    x = np.zeros(3 * len(x0), np.float32)
+    assert L.sbs_gpu_get_state(h, 0, x.ctypes.data, None) == 0
+    assert np.array_equal(x.reshape(-1, 3), rescale_translate(x0, box, tr))
+    for _ in range(60):
+        assert L.sbs_gpu_step(h, 1.0 / 60.0, 1, 10) == 0
+    assert L.sbs_gpu_get_state(h, 0, x.ctypes.data, None) == 0
+    y = x.reshape(-1, 3)[:, 1]
+    assert np.isfinite(x).all() and y.min() > -0.05 and y.min() < 1.0   # fell, and rests on y = 0
+    L.sbs_gpu_destroy(h)
