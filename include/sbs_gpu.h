@@ -193,17 +193,28 @@ sbs_status sbs_gpu_load_scene(sbs_gpu* h, const char* json_path, const sbs_gpu_m
  * index (k * ny + j) * nx + i at origin + (i, j, k) * spacing, evaluated by
  * trilinear interpolation with the interpolant's gradient.  Surface vertices
  * with sd < 0 get the contact of bvh_model.cpp:72-94 (n = normalised
- * gradient, q = p + |sd| n); outside the grid there is no contact.  Stands in
- * for the Discregrid cubic Lagrange grid of sdf_model_t
- * (src/physics/collision/sdf_model.cpp:66-75).  Up to 2 grids; planes and
- * grids together at most 4, planes first.  Before finalize; not with
- * SBS_EXEC_CLUSTER. */
+ * gradient, q = p + |sd| n); outside the grid there is no contact.  Up to 2
+ * grids (of either kind); planes and grids together at most 4, planes first.
+ * Before finalize; not with SBS_EXEC_CLUSTER. */
 sbs_status sbs_gpu_add_sdf_grid(sbs_gpu* h, const float* values, const uint32_t nodes[3], const double origin[3],
                                 const double spacing[3]);
+/* The cubic Lagrange grid sdf_model_t interpolates
+ * (src/physics/collision/sdf_model.cpp:66-75, a Discregrid
+ * CubicLagrangeDiscreteGrid built at environment_body.cpp:72-73): cells[3]
+ * cells of size `spacing` from `origin`, each the 32-node serendipity
+ * element (Koschier et al. 2017; corners and the points at 1/3 and 2/3 of
+ * every edge), the interpolant's gradient as normal.  values: the (cells+1)
+ * vertices per axis, index (k * ny + j) * nx + i; then 2 values per x-edge
+ * (edge (i, j, k), i < cells[0], index (k * ny + j) * cells[0] + i, the node
+ * at 1/3 first), per y-edge ((k * cells[1] + j) * nx + i) and per z-edge
+ * ((k * ny + j) * nx + i, k < cells[2]), with nx, ny the vertices per axis.
+ * Otherwise as sbs_gpu_add_sdf_grid. */
+sbs_status sbs_gpu_add_sdf_grid_cubic(sbs_gpu* h, const float* values, const uint32_t cells[3], const double origin[3],
+                                      const double spacing[3]);
 /* environment_body_t's constructor (src/physics/environment_body.cpp:12-78) for
  * a triangle mesh (outward winding): the domain grown over the mesh vertices
  * and padded as that constructor does, `cells` cells per axis, node values from
- * sbs_gpu_sdf_from_mesh, added with sbs_gpu_add_sdf_grid. */
+ * sbs_gpu_sdf_cubic_from_mesh, added with sbs_gpu_add_sdf_grid_cubic. */
 sbs_status sbs_gpu_add_environment_mesh(sbs_gpu* h, const double* verts, uint32_t n_verts, const uint32_t* tris,
                                         uint32_t n_tris, const double domain_lo[3], const double domain_hi[3],
                                         const uint32_t cells[3]);
@@ -213,6 +224,11 @@ sbs_status sbs_gpu_add_environment_mesh(sbs_gpu* h, const double* verts, uint32_
  * pseudonormal (Baerentzen & Aanaes 2005); brute force over triangles. */
 sbs_status sbs_gpu_sdf_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris, uint32_t n_tris,
                                  const double lo[3], const double hi[3], const uint32_t cells[3], float* values);
+/* Host only: the values of the cubic grid of sbs_gpu_add_sdf_grid_cubic
+ * (layout there) for a triangle mesh over the box [lo, hi]. */
+sbs_status sbs_gpu_sdf_cubic_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris, uint32_t n_tris,
+                                       const double lo[3], const double hi[3], const uint32_t cells[3],
+                                       float* values);
 
 /* Distance constraints: n rows of ids [4n] = (b1, b2, v1, v2) - body and
  * body-local vertex of each end, the order of distance_constraint_t's

@@ -5,7 +5,7 @@ parameters flat as W1[128][16] b1 W2[128][128] b2 W3[128][128] b3 W4[3][128] b4.
 Inputs normalised as (x - mean) / std, outputs multiplied by out_scale.
 Loss: mean over rows of ||z4 - t / out_scale||^2 (z4 = normalised output).
 The GPU kernels' gradients are checked against `loss_grad` here, and
-`loss_grad` itself against central finite differences; `adam` restates the
+`loss_grad` itself against central finite differences; `adam_update` restates the
 optimiser the training kernels apply (Kingma & Ba 2015, bias-corrected
 moments).
 """
@@ -69,17 +69,11 @@ def loss_grad(p, x, t, mean, std, scale):
     return loss, flat
 
 
-def adam(p, x, t, mean, std, scale, steps: int, lr: float, b1: float = 0.9, b2: float = 0.999,
-         eps: float = 1e-8):
-    """`steps` Adam steps on the full batch (x, t) from parameters p, with
-    moments starting at zero: m = b1 m + (1 - b1) g, v = b2 v + (1 - b2) g^2,
-    p -= lr (m / (1 - b1^k)) / (sqrt(v / (1 - b2^k)) + eps) at step k."""
-    p = np.asarray(p, np.float64).copy()
-    m = np.zeros_like(p)
-    v = np.zeros_like(p)
-    for k in range(1, steps + 1):
-        _, g = loss_grad(p, x, t, mean, std, scale)
-        m = b1 * m + (1 - b1) * g
-        v = b2 * v + (1 - b2) * g * g
-        p -= lr * (m / (1 - b1 ** k)) / (np.sqrt(v / (1 - b2 ** k)) + eps)
-    return p
+def adam_update(p, g, m, v, k: int, lr: float, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8):
+    """Adam step number k (from 1) with gradient g and moments m, v (zero
+    before the first step): m = b1 m + (1 - b1) g, v = b2 v + (1 - b2) g^2,
+    p - lr (m / (1 - b1^k)) / (sqrt(v / (1 - b2^k)) + eps).  Returns
+    (p, m, v)."""
+    m = b1 * m + (1 - b1) * g
+    v = b2 * v + (1 - b2) * g * g
+    return p - lr * (m / (1 - b1 ** k)) / (np.sqrt(v / (1 - b2 ** k)) + eps), m, v

@@ -51,6 +51,9 @@ def lib():
         L.orc_set_external_acceleration.argtypes = [P, I, dp]
         L.orc_add_ground_plane.argtypes = [P, dp, D]
         L.orc_add_sdf_grid.argtypes = [P, C.c_void_p, up, dp, dp]
+        L.orc_add_sdf_grid_cubic.argtypes = [P, C.c_void_p, up, dp, dp]
+        L.orc_grid_eval.restype = I
+        L.orc_grid_eval.argtypes = [P, I, dp, dp]
         L.orc_set_tet_order.restype = I
         L.orc_plan_colours.restype = U32
         L.orc_plan_colours.argtypes = [P, up, up, U32]
@@ -154,11 +157,14 @@ class Oracle:
             n, d = scene.ground
             L.orc_add_ground_plane(self.h, np.asarray(n, np.float64), d)
         self._grids = []
-        for values, nodes, origin, spacing in getattr(scene, "sdf_grids", None) or []:
+        for grid in getattr(scene, "sdf_grids", None) or []:
+            values, dims, origin, spacing = grid[:4]
+            cubic = len(grid) > 4 and grid[4] == "cubic"
             v = np.ascontiguousarray(values, np.float32).ravel()
             self._grids.append(v)
-            L.orc_add_sdf_grid(self.h, v.ctypes.data, np.ascontiguousarray(nodes, np.uint32),
-                               np.asarray(origin, np.float64), np.asarray(spacing, np.float64))
+            add = L.orc_add_sdf_grid_cubic if cubic else L.orc_add_sdf_grid
+            add(self.h, v.ctypes.data, np.ascontiguousarray(dims, np.uint32),
+                np.asarray(origin, np.float64), np.asarray(spacing, np.float64))
         if getattr(scene, "body_contacts", 0):
             cell = scene.hash_cell if scene.hash_cell > 0 else mean_edge_cell(scene)
             self.hash_cell = cell
@@ -279,6 +285,14 @@ class Oracle:
                 "residual_contact": out[3],
                 "projections": int(self.L.orc_projections(self.h)),
                 "contacts": int(self.L.orc_n_contacts(self.h))}
+
+    def grid_eval(self, grid: int, p):
+        """(signed distance, gradient) of environment grid `grid` at p, or
+        None outside it."""
+        out = np.zeros(4)
+        if not self.L.orc_grid_eval(self.h, grid, np.ascontiguousarray(p, np.float64), out):
+            return None
+        return out[0], out[1:]
 
     def time_frames(self, n: int) -> float:
         s = self.scene

@@ -214,13 +214,65 @@ struct kinematic_t {
 
 struct plane_t { vec3 n; double d; };
 
-// Signed-distance grid of an environment body (addition: the reference
-// samples a Discregrid cubic Lagrange grid, sdf_model.cpp:66-75; here node
-// values with trilinear interpolation and the interpolant's gradient).
+// Signed-distance grid of an environment body.  cubic: the reference's
+// Discregrid cubic Lagrange grid (sdf_model.cpp:66-75, environment_body.cpp:
+// 72-73), per cell the 32-node serendipity element (Koschier et al. 2017):
+// corner values and values at 1/3 and 2/3 of every edge (value layout: the
+// (cells+1)^3 vertices, then two per x-, y- and z-edge); otherwise node values
+// with trilinear interpolation.  The gradient is the interpolant's.
 struct grid_t {
     std::vector<double> v;
     uint32_t n[3];
     double o[3], h[3];
+    bool cubic = false;
+
+    // the 32-node cell (c0, c1, c2) at reference coordinates r in [-1, 1]^3:
+    // value and derivatives w.r.t. r
+    void cubic_cell(const uint32_t c[3], const double r[3], double& f, double d[3]) const {
+        const size_t nx = n[0], ny = n[1], nz = n[2];
+        const size_t base[3] = {nx * ny * nz, nx * ny * nz + 2 * (nx - 1) * ny * nz,
+                                nx * ny * nz + 2 * (nx - 1) * ny * nz + 2 * nx * (ny - 1) * nz};
+        f = 0.0;
+        d[0] = d[1] = d[2] = 0.0;
+        const double q = 9.0 * (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) - 19.0;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int e = 0; e < 2; ++e) {
+                    const double s[3] = {a ? 1.0 : -1.0, b ? 1.0 : -1.0, e ? 1.0 : -1.0};
+                    const double val = v[((c[2] + e) * ny + (c[1] + b)) * nx + (c[0] + a)] / 64.0;
+                    const double l[3] = {1 + r[0] * s[0], 1 + r[1] * s[1], 1 + r[2] * s[2]};
+                    f += val * l[0] * l[1] * l[2] * q;
+                    for (int k = 0; k < 3; ++k) {
+                        const double lk = l[(k + 1) % 3] * l[(k + 2) % 3];
+                        d[k] += val * (s[k] * lk * q + l[0] * l[1] * l[2] * 18.0 * r[k]);
+                    }
+                }
+        for (int ax = 0; ax < 3; ++ax) {
+            const int o1 = (ax + 1) % 3, o2 = (ax + 2) % 3;
+            for (int b1 = 0; b1 < 2; ++b1)
+                for (int b2 = 0; b2 < 2; ++b2) {
+                    uint32_t g[3] = {c[0], c[1], c[2]};
+                    g[o1] += b1;
+                    g[o2] += b2;
+                    size_t idx;
+                    if (ax == 0) idx = base[0] + 2 * ((g[2] * ny + g[1]) * (nx - 1) + g[0]);
+                    else if (ax == 1) idx = base[1] + 2 * ((g[2] * (ny - 1) + g[1]) * nx + g[0]);
+                    else idx = base[2] + 2 * ((g[2] * ny + g[1]) * nx + g[0]);
+                    const double s1 = b1 ? 1.0 : -1.0, s2 = b2 ? 1.0 : -1.0;
+                    const double p1 = 1 + r[o1] * s1, p2 = 1 + r[o2] * s2, u = r[ax];
+                    for (int t = 0; t < 2; ++t) {
+                        const double tt = t ? 1.0 / 3.0 : -1.0 / 3.0;
+                        const double val = v[idx + t] * 9.0 / 64.0;
+                        const double pu = (1 - u * u) * (1 + 9 * u * tt);
+                        f += val * pu * p1 * p2;
+                        d[ax] += val * (-2 * u * (1 + 9 * u * tt) + (1 - u * u) * 9 * tt) * p1 * p2;
+                        d[o1] += val * pu * s1 * p2;
+                        d[o2] += val * pu * p1 * s2;
+                    }
+                }
+        }
+    }
+
     // false outside the grid (no contact there)
     bool eval(vec3 p, double& sd, vec3& g) const {
         const double u[3] = {(p.x - o[0]) / h[0], (p.y - o[1]) / h[1], (p.z - o[2]) / h[2]};
@@ -230,6 +282,13 @@ struct grid_t {
             if (!(u[k] >= 0.0 && u[k] <= (double)(n[k] - 1))) return false;
             c[k] = std::min((uint32_t)u[k], n[k] - 2);
             f[k] = u[k] - c[k];
+        }
+        if (cubic) {
+            const double r[3] = {2 * f[0] - 1, 2 * f[1] - 1, 2 * f[2] - 1};
+            double d[3];
+            cubic_cell(c, r, sd, d);
+            g = {d[0] * 2 / h[0], d[1] * 2 / h[1], d[2] * 2 / h[2]};
+            return true;
         }
         auto at = [&](uint32_t i, uint32_t j, uint32_t k) {
             return v[((size_t)(c[2] + k) * n[1] + (c[1] + j)) * n[0] + (c[0] + i)];
@@ -975,6 +1034,37 @@ void orc_add_sdf_grid(void* h, const float* values, const uint32_t* nodes, const
     }
     g.v.assign(values, values + n);
     s.grids.push_back(std::move(g));
+}
+
+// A cubic grid (layout of grid_t) of cells[3] cells.
+void orc_add_sdf_grid_cubic(void* h, const float* values, const uint32_t* cells, const double* origin,
+                            const double* spacing) {
+    sim_t& s = *(sim_t*)h;
+    grid_t g;
+    g.cubic = true;
+    for (int k = 0; k < 3; ++k) {
+        g.n[k] = cells[k] + 1;
+        g.o[k] = origin[k];
+        g.h[k] = spacing[k];
+    }
+    const size_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    const size_t n = nx * ny * nz + 2 * ((nx - 1) * ny * nz + nx * (ny - 1) * nz + nx * ny * (nz - 1));
+    g.v.assign(values, values + n);
+    s.grids.push_back(std::move(g));
+}
+
+// The cubic cell interpolant alone (for its tests): value and gradient of
+// grid `gi` at p; returns 0 outside the grid.
+int orc_grid_eval(void* h, int gi, const double* p, double* out4) {
+    const grid_t& g = ((sim_t*)h)->grids[gi];
+    double sd;
+    vec3 gr;
+    if (!g.eval(vec3{p[0], p[1], p[2]}, sd, gr)) return 0;
+    out4[0] = sd;
+    out4[1] = gr.x;
+    out4[2] = gr.y;
+    out4[3] = gr.z;
+    return 1;
 }
 
 void orc_add_ground_plane(void* h, const double* n, double d) {

@@ -78,6 +78,7 @@ struct sbs_gpu {
     // signed-distance grids of environment bodies (after the planes)
     struct GridHost {
         std::vector<float> v;
+        int cubic = 0;
         uint32_t n[3];
         double o[3], h[3];
     };
@@ -780,33 +781,47 @@ sbs_status sbs_gpu_set_body_velocity(sbs_gpu* h, int32_t body, const double v[3]
     return SBS_OK;
 }
 
-sbs_status sbs_gpu_add_sdf_grid(sbs_gpu* h, const float* values, const uint32_t nodes[3], const double origin[3],
-                                const double spacing[3]) {
+static sbs_status add_grid(sbs_gpu* h, const float* values, const uint32_t nodes[3], const double origin[3],
+                           const double spacing[3], int cubic) {
     if (!h || !values || !nodes || !origin || !spacing) return fail(h, SBS_EINVAL, "sdf grid: null");
     if (h->finalized) return fail(h, SBS_ESTATE, "sdf grid after finalize");
     if (h->grids.size() >= (size_t)kMaxGrids) return fail(h, SBS_EINVAL, "too many sdf grids");
     if (h->planes.size() + h->grids.size() >= (size_t)kMaxPlanes)
         return fail(h, SBS_EINVAL, "too many environment bodies (planes + grids)");
     sbs_gpu::GridHost g;
-    size_t n = 1;
     for (int k = 0; k < 3; ++k) {
-        if (nodes[k] < 2 || nodes[k] > 4096) return fail(h, SBS_EINVAL, "sdf grid: 2..4096 nodes per axis");
+        if (nodes[k] < 2 || nodes[k] > 4096) return fail(h, SBS_EINVAL, "sdf grid: 1..4095 cells per axis");
         if (!(spacing[k] > 0) || !std::isfinite(origin[k])) return fail(h, SBS_EINVAL, "sdf grid: spacing/origin");
         g.n[k] = nodes[k];
         g.o[k] = origin[k];
         g.h[k] = spacing[k];
-        n *= nodes[k];
     }
+    const size_t n = cubic ? sdf_cubic_count(nodes[0], nodes[1], nodes[2]) : (size_t)nodes[0] * nodes[1] * nodes[2];
     g.v.assign(values, values + n);
+    g.cubic = cubic;
     for (float f : g.v)
         if (!std::isfinite(f)) return fail(h, SBS_EINVAL, "sdf grid: non-finite value");
     h->grids.push_back(std::move(g));
     return SBS_OK;
 }
 
-extern "C" sbs_status sbs_gpu_sdf_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris,
-                                            uint32_t n_tris, const double lo[3], const double hi[3],
-                                            const uint32_t cells[3], float* values);
+sbs_status sbs_gpu_add_sdf_grid(sbs_gpu* h, const float* values, const uint32_t nodes[3], const double origin[3],
+                                const double spacing[3]) {
+    return add_grid(h, values, nodes, origin, spacing, 0);
+}
+
+sbs_status sbs_gpu_add_sdf_grid_cubic(sbs_gpu* h, const float* values, const uint32_t cells[3], const double origin[3],
+                                      const double spacing[3]) {
+    if (!cells) return fail(h, SBS_EINVAL, "sdf grid: null");
+    for (int k = 0; k < 3; ++k)
+        if (cells[k] == 0 || cells[k] > 4095) return fail(h, SBS_EINVAL, "sdf grid: 1..4095 cells per axis");
+    const uint32_t nodes[3] = {cells[0] + 1, cells[1] + 1, cells[2] + 1};
+    return add_grid(h, values, nodes, origin, spacing, 1);
+}
+
+extern "C" sbs_status sbs_gpu_sdf_cubic_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris,
+                                                  uint32_t n_tris, const double lo[3], const double hi[3],
+                                                  const uint32_t cells[3], float* values);
 
 sbs_status sbs_gpu_add_environment_mesh(sbs_gpu* h, const double* verts, uint32_t n_verts, const uint32_t* tris,
                                         uint32_t n_tris, const double domain_lo[3], const double domain_hi[3],
@@ -831,12 +846,12 @@ sbs_status sbs_gpu_add_environment_mesh(sbs_gpu* h, const double* verts, uint32_
     }
     for (int k = 0; k < 3; ++k)
         if (cells[k] == 0 || cells[k] > 4095) return fail(h, SBS_EINVAL, "environment: 1..4095 cells per axis");
-    std::vector<float> v((size_t)(cells[0] + 1) * (cells[1] + 1) * (cells[2] + 1));
-    const sbs_status s = sbs_gpu_sdf_from_mesh(verts, n_verts, tris, n_tris, lo, hi, cells, v.data());
+    // the cubic Lagrange grid of environment_body.cpp:72-73
+    std::vector<float> v(sdf_cubic_count(cells[0] + 1, cells[1] + 1, cells[2] + 1));
+    const sbs_status s = sbs_gpu_sdf_cubic_from_mesh(verts, n_verts, tris, n_tris, lo, hi, cells, v.data());
     if (s) return fail(h, s, "environment: bad mesh or domain");
-    const uint32_t nodes[3] = {cells[0] + 1, cells[1] + 1, cells[2] + 1};
     const double sp[3] = {(hi[0] - lo[0]) / cells[0], (hi[1] - lo[1]) / cells[1], (hi[2] - lo[2]) / cells[2]};
-    return sbs_gpu_add_sdf_grid(h, v.data(), nodes, lo, sp);
+    return sbs_gpu_add_sdf_grid_cubic(h, v.data(), cells, lo, sp);
 }
 
 static sbs_status upload(sbs_gpu* h, void* dst, const void* src, size_t bytes) {
@@ -1537,6 +1552,7 @@ plan_again:
         dg.nx = gh.n[0]; dg.ny = gh.n[1]; dg.nz = gh.n[2];
         dg.ox = (float)gh.o[0]; dg.oy = (float)gh.o[1]; dg.oz = (float)gh.o[2];
         dg.hx = (float)gh.h[0]; dg.hy = (float)gh.h[1]; dg.hz = (float)gh.h[2];
+        dg.cubic = gh.cubic;
     }
     p.n_kin_groups = (int)h->groups.size();
     p.has_acc = h->has_acc ? 1 : 0;

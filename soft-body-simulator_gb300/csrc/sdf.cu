@@ -70,58 +70,113 @@ inline uint64_t edge_key(uint32_t a, uint32_t b) {
 
 }  // namespace
 
-extern "C" sbs_status sbs_gpu_sdf_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris,
-                                            uint32_t n_tris, const double lo[3], const double hi[3],
-                                            const uint32_t cells[3], float* values) {
+namespace {
+
+// Signed distance of a triangle mesh (pseudonormals precomputed), brute force
+// over the triangles.
+struct MeshSdf {
+    std::vector<V3> x, fn, vn;
+    std::unordered_map<uint64_t, V3> en;
+    const uint32_t* tris;
+    uint32_t n_tris;
+
+    MeshSdf(const double* verts, uint32_t n_verts, const uint32_t* t, uint32_t nt) : tris(t), n_tris(nt) {
+        x.resize(n_verts);
+        for (uint32_t i = 0; i < n_verts; ++i) x[i] = {verts[3ull * i], verts[3ull * i + 1], verts[3ull * i + 2]};
+        fn.resize(n_tris);
+        vn.assign(n_verts, V3{0, 0, 0});
+        for (uint32_t f = 0; f < n_tris; ++f) {
+            const uint32_t* q = tris + 3ull * f;
+            fn[f] = unit(cross(x[q[1]] - x[q[0]], x[q[2]] - x[q[0]]));
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t v = q[k], v1 = q[(k + 1) % 3], v2 = q[(k + 2) % 3];
+                const V3 e1 = unit(x[v1] - x[v]), e2 = unit(x[v2] - x[v]);
+                const double ang = std::acos(std::max(-1.0, std::min(1.0, dot(e1, e2))));
+                vn[v] = vn[v] + fn[f] * ang;
+                auto it = en.find(edge_key(v, v1));
+                if (it == en.end()) en.emplace(edge_key(v, v1), fn[f]);
+                else it->second = it->second + fn[f];
+            }
+        }
+    }
+
+    double at(V3 p) {
+        Hit best{1e300, {0, 0, 0}, 0};
+        uint32_t bt = 0;
+        for (uint32_t t = 0; t < n_tris; ++t) {
+            const uint32_t* q = tris + 3ull * t;
+            const Hit h = closest_on_triangle(p, x[q[0]], x[q[1]], x[q[2]]);
+            if (h.d2 < best.d2) {
+                best = h;
+                bt = t;
+            }
+        }
+        const uint32_t* q = tris + 3ull * bt;
+        V3 n;
+        if (best.feature == 0) n = fn[bt];
+        else if (best.feature <= 3) n = vn[q[best.feature - 1]];
+        else {
+            const int e = best.feature - 4;
+            n = en[edge_key(q[e], q[(e + 1) % 3])];
+        }
+        const double d = std::sqrt(best.d2);
+        return dot(p - best.c, n) < 0 ? -d : d;
+    }
+};
+
+sbs_status check_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris, uint32_t n_tris, const double lo[3],
+                      const double hi[3], const uint32_t cells[3], const float* values) {
     if (!verts || !tris || !lo || !hi || !cells || !values || n_verts == 0 || n_tris == 0) return SBS_EINVAL;
     for (int k = 0; k < 3; ++k)
         if (cells[k] == 0 || !(hi[k] > lo[k])) return SBS_EINVAL;
     for (uint64_t t = 0; t < 3ull * n_tris; ++t)
         if (tris[t] >= n_verts) return SBS_EINVAL;
-    std::vector<V3> x(n_verts);
-    for (uint32_t i = 0; i < n_verts; ++i) x[i] = {verts[3ull * i], verts[3ull * i + 1], verts[3ull * i + 2]};
-    // pseudonormals
-    std::vector<V3> fn(n_tris), vn(n_verts, V3{0, 0, 0});
-    std::unordered_map<uint64_t, V3> en;
-    for (uint32_t t = 0; t < n_tris; ++t) {
-        const uint32_t* q = tris + 3ull * t;
-        fn[t] = unit(cross(x[q[1]] - x[q[0]], x[q[2]] - x[q[0]]));
-        for (int k = 0; k < 3; ++k) {
-            const uint32_t v = q[k], v1 = q[(k + 1) % 3], v2 = q[(k + 2) % 3];
-            const V3 e1 = unit(x[v1] - x[v]), e2 = unit(x[v2] - x[v]);
-            const double ang = std::acos(std::max(-1.0, std::min(1.0, dot(e1, e2))));
-            vn[v] = vn[v] + fn[t] * ang;
-            auto it = en.find(edge_key(v, v1));
-            if (it == en.end()) en.emplace(edge_key(v, v1), fn[t]);
-            else it->second = it->second + fn[t];
-        }
-    }
+    return SBS_OK;
+}
+
+}  // namespace
+
+extern "C" sbs_status sbs_gpu_sdf_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris,
+                                            uint32_t n_tris, const double lo[3], const double hi[3],
+                                            const uint32_t cells[3], float* values) {
+    const sbs_status st = check_mesh(verts, n_verts, tris, n_tris, lo, hi, cells, values);
+    if (st) return st;
+    MeshSdf m(verts, n_verts, tris, n_tris);
     const uint32_t nx = cells[0] + 1, ny = cells[1] + 1, nz = cells[2] + 1;
     const double hx = (hi[0] - lo[0]) / cells[0], hy = (hi[1] - lo[1]) / cells[1], hz = (hi[2] - lo[2]) / cells[2];
     for (uint32_t k = 0; k < nz; ++k)
         for (uint32_t j = 0; j < ny; ++j)
-            for (uint32_t i = 0; i < nx; ++i) {
-                const V3 p{lo[0] + i * hx, lo[1] + j * hy, lo[2] + k * hz};
-                Hit best{1e300, {0, 0, 0}, 0};
-                uint32_t bt = 0;
-                for (uint32_t t = 0; t < n_tris; ++t) {
-                    const uint32_t* q = tris + 3ull * t;
-                    const Hit h = closest_on_triangle(p, x[q[0]], x[q[1]], x[q[2]]);
-                    if (h.d2 < best.d2) {
-                        best = h;
-                        bt = t;
-                    }
-                }
-                const uint32_t* q = tris + 3ull * bt;
-                V3 n;
-                if (best.feature == 0) n = fn[bt];
-                else if (best.feature <= 3) n = vn[q[best.feature - 1]];
-                else {
-                    const int e = best.feature - 4;
-                    n = en[edge_key(q[e], q[(e + 1) % 3])];
-                }
-                const double d = std::sqrt(best.d2);
-                values[((size_t)k * ny + j) * nx + i] = (float)(dot(p - best.c, n) < 0 ? -d : d);
-            }
+            for (uint32_t i = 0; i < nx; ++i)
+                values[((size_t)k * ny + j) * nx + i] = (float)m.at(V3{lo[0] + i * hx, lo[1] + j * hy, lo[2] + k * hz});
+    return SBS_OK;
+}
+
+// The values of a cubic grid (layout of csrc/sdf_eval.cuh): the grid
+// vertices, then the two nodes at 1/3 and 2/3 along every x-, y- and z-edge.
+extern "C" sbs_status sbs_gpu_sdf_cubic_from_mesh(const double* verts, uint32_t n_verts, const uint32_t* tris,
+                                                  uint32_t n_tris, const double lo[3], const double hi[3],
+                                                  const uint32_t cells[3], float* values) {
+    const sbs_status st = check_mesh(verts, n_verts, tris, n_tris, lo, hi, cells, values);
+    if (st) return st;
+    MeshSdf m(verts, n_verts, tris, n_tris);
+    const uint64_t nx = cells[0] + 1, ny = cells[1] + 1, nz = cells[2] + 1;
+    const double h[3] = {(hi[0] - lo[0]) / cells[0], (hi[1] - lo[1]) / cells[1], (hi[2] - lo[2]) / cells[2]};
+    auto at = [&](double i, double j, double k) { return (float)m.at(V3{lo[0] + i * h[0], lo[1] + j * h[1], lo[2] + k * h[2]}); };
+    size_t o = 0;
+    for (uint64_t k = 0; k < nz; ++k)
+        for (uint64_t j = 0; j < ny; ++j)
+            for (uint64_t i = 0; i < nx; ++i) values[o++] = at(i, j, k);
+    for (uint64_t k = 0; k < nz; ++k)
+        for (uint64_t j = 0; j < ny; ++j)
+            for (uint64_t i = 0; i + 1 < nx; ++i)
+                for (int s = 0; s < 2; ++s) values[o++] = at(i + (s + 1) / 3.0, j, k);
+    for (uint64_t k = 0; k < nz; ++k)
+        for (uint64_t j = 0; j + 1 < ny; ++j)
+            for (uint64_t i = 0; i < nx; ++i)
+                for (int s = 0; s < 2; ++s) values[o++] = at(i, j + (s + 1) / 3.0, k);
+    for (uint64_t k = 0; k + 1 < nz; ++k)
+        for (uint64_t j = 0; j < ny; ++j)
+            for (uint64_t i = 0; i < nx; ++i)
+                for (int s = 0; s < 2; ++s) values[o++] = at(i, j, k + (s + 1) / 3.0);
     return SBS_OK;
 }

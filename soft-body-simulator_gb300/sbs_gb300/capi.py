@@ -110,6 +110,8 @@ def load(build: bool = True):
         "sbs_gpu_load_scene": [P, C.c_char_p, C.POINTER(Material), u32, C.c_double, C.POINTER(C.c_int32),
                                C.POINTER(C.c_int32)],
         "sbs_gpu_add_sdf_grid": [P, C.c_void_p, u32, f64, f64],
+        "sbs_gpu_add_sdf_grid_cubic": [P, C.c_void_p, u32, f64, f64],
+        "sbs_gpu_sdf_cubic_from_mesh": [f64, C.c_uint32, u32, C.c_uint32, f64, f64, u32, C.c_void_p],
         "sbs_gpu_add_environment_mesh": [P, f64, C.c_uint32, u32, C.c_uint32, f64, f64, u32],
         "sbs_gpu_sdf_from_mesh": [f64, C.c_uint32, u32, C.c_uint32, f64, f64, u32, C.c_void_p],
         "sbs_gpu_add_distance_constraints": [P, C.c_void_p, C.c_uint32, C.c_double, C.c_double],
@@ -212,6 +214,23 @@ def sdf_from_mesh(verts, tris, lo, hi, cells) -> np.ndarray:
     return out.reshape(int(c[2]) + 1, int(c[1]) + 1, int(c[0]) + 1)
 
 
+def sdf_cubic_from_mesh(verts, tris, lo, hi, cells) -> np.ndarray:
+    """Host-only values of the cubic Lagrange grid (layout of
+    sbs_gpu_add_sdf_grid_cubic) of a triangle mesh over the box [lo, hi]."""
+    L = load()
+    v = np.ascontiguousarray(verts, np.float64).ravel()
+    t = np.ascontiguousarray(tris, np.uint32).ravel()
+    c = np.ascontiguousarray(cells, np.uint32)
+    nx, ny, nz = (int(k) + 1 for k in c)
+    n = nx * ny * nz + 2 * ((nx - 1) * ny * nz + nx * (ny - 1) * nz + nx * ny * (nz - 1))
+    out = np.zeros(n, np.float32)
+    st = L.sbs_gpu_sdf_cubic_from_mesh(v, len(v) // 3, t, len(t) // 3, np.asarray(lo, np.float64),
+                                       np.asarray(hi, np.float64), c, out.ctypes.data)
+    if st != SBS_OK:
+        raise SbsError(st, "sbs_gpu_sdf_cubic_from_mesh failed")
+    return out
+
+
 def plan_sweep(scene):
     """Sweep order of a scene computed by the library's host code (no GPU):
     (order, offsets) with bodies concatenated in add order; the bodies'
@@ -287,10 +306,12 @@ class Solver:
         if scene.ground is not None:
             n, d = scene.ground
             self._check(L.sbs_gpu_add_ground_plane(h, np.asarray(n, np.float64), d))
-        for values, nodes, origin, spacing in getattr(scene, "sdf_grids", None) or []:
+        for grid in getattr(scene, "sdf_grids", None) or []:
+            values, dims, origin, spacing = grid[:4]
+            add = L.sbs_gpu_add_sdf_grid_cubic if len(grid) > 4 and grid[4] == "cubic" else L.sbs_gpu_add_sdf_grid
             v = np.ascontiguousarray(values, np.float32).ravel()
-            self._check(L.sbs_gpu_add_sdf_grid(h, v.ctypes.data, np.ascontiguousarray(nodes, np.uint32),
-                                               np.asarray(origin, np.float64), np.asarray(spacing, np.float64)))
+            self._check(add(h, v.ctypes.data, np.ascontiguousarray(dims, np.uint32),
+                            np.asarray(origin, np.float64), np.asarray(spacing, np.float64)))
         self._check(L.sbs_gpu_finalize(h))
         if any(b.v_init is not None for b in scene.bodies):
             for i, b in enumerate(scene.bodies):

@@ -96,31 +96,34 @@ def test_gpu_adam_training_reduces_loss(capi_mod):
 
 @pytest.mark.gpu
 def test_gpu_adam_steps_against_fp64_adam(capi_mod):
-    """Three Adam steps on the GPU against the FP64 restatement
-    (mlp_oracle.adam).  The dataset is one row repeated, so every random
-    batch is that row and the GPU's batch gradient is the row's gradient.
-    Adam's first steps move each parameter by about lr in the direction of
-    -sign(gradient), so where the FP64 gradient is clearly nonzero the GPU's
-    BF16 gradients must give the same moves; elsewhere the move stays within
-    the 3 lr the three steps allow."""
+    """Three Adam steps of the GPU's training against the FP64 restatement
+    of Adam (mlp_oracle.adam_update) driven by the same gradients.  The
+    dataset is one row repeated, so every random batch is that row and a
+    training step's gradient is that row's gradient, which sbs_mlp_loss_grad
+    returns from the same kernels (the gradients themselves are checked
+    against FP64 above).  Moves of parameters whose gradient is below 1e-6
+    depend on Adam's epsilon and on rounding; they stay within lr per step."""
     from oracle import mlp_oracle
     m = capi_mod.Mlp(seed=9)
-    x1, t1 = (a.astype(np.float32).astype(np.float64) for a in data(1, seed=10))
+    x1, t1 = data(1, seed=10)
     xs, ts = data(4096, seed=11)
-    mean, std, scale = (a.astype(np.float32).astype(np.float64) for a in norm_of(xs, ts))
-    m.set_normalization(mean, std, scale)
-    p0 = m.params().astype(np.float64)
+    m.set_normalization(*norm_of(xs, ts))
     m.set_dataset(np.repeat(x1, 4096, axis=0), np.repeat(t1, 4096, axis=0))
     lr = 1e-3
-    m.train(3, 1024, lr, seed=2)
-    d_gpu = m.params().astype(np.float64) - p0
-    d_ref = mlp_oracle.adam(p0, x1, t1, mean, std, scale, 3, lr) - p0
-    _, g0 = mlp_oracle.loss_grad(p0, x1, t1, mean, std, scale)
-    clear = np.abs(g0) > 1e-2 * np.abs(g0).max()
-    assert clear.sum() > 1000
-    assert np.abs(d_gpu[clear] - d_ref[clear]).max() <= 0.05 * lr
-    assert np.abs(d_gpu).max() <= 3 * lr * (1 + 1e-3)
-    assert np.abs(d_gpu - d_ref).max() <= 6 * lr
+    p = m.params().astype(np.float64)
+    mom1 = np.zeros_like(p)
+    mom2 = np.zeros_like(p)
+    for k in range(1, 4):
+        _, g = m.loss_grad(x1, t1)
+        g = g.astype(np.float64)
+        m.train(1, 1024, lr, seed=k)
+        ref, mom1, mom2 = mlp_oracle.adam_update(p, g, mom1, mom2, k, lr)
+        got = m.params().astype(np.float64)
+        big = np.abs(g) > 1e-6
+        assert big.sum() > 10000
+        assert np.abs((got - p)[big] - (ref - p)[big]).max() <= 2e-3 * lr
+        assert np.abs(got - p).max() <= lr * (1 + 1e-3)
+        p = got
 
 
 @pytest.mark.gpu

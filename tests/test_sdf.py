@@ -168,3 +168,174 @@ def test_gpu_grid_rejects_cluster_and_bad_grids(capi_mod):
     sc.sdf_grids = [(vals, nodes, lo, sp)]
     with pytest.raises(capi_mod.SbsError):
         capi_mod.Solver(sc)
+
+
+# ---- the cubic Lagrange grid (Discregrid's CubicLagrangeDiscreteGrid,
+# environment_body.cpp:72-73): 32-node serendipity cells
+
+def cubic_layout_points(lo, sp, cells):
+    """Positions of the cubic grid's values in their layout: vertices, then
+    the nodes at 1/3 and 2/3 of every x-, y- and z-edge."""
+    nx, ny, nz = (c + 1 for c in cells)
+    lo, sp = np.asarray(lo, float), np.asarray(sp, float)
+    pts = []
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                pts.append((i, j, k))
+    for ax, (mx, my, mz) in enumerate(((nx - 1, ny, nz), (nx, ny - 1, nz), (nx, ny, nz - 1))):
+        for k in range(mz):
+            for j in range(my):
+                for i in range(mx):
+                    for s in (1 / 3, 2 / 3):
+                        q = [i, j, k]
+                        q[ax] += s
+                        pts.append(tuple(q))
+    return lo + np.asarray(pts, float) * sp
+
+
+def serendipity(values, lo, sp, cells, p):
+    """Independent numpy restatement of the 32-node cell interpolant: value
+    and gradient at p (p inside the grid)."""
+    nx, ny, nz = (c + 1 for c in cells)
+    u = (np.asarray(p, float) - lo) / sp
+    c = np.minimum(np.floor(u).astype(int), np.asarray(cells) - 1)
+    r = 2 * (u - c) - 1
+    V = values
+    bases = [nx * ny * nz]
+    bases.append(bases[0] + 2 * (nx - 1) * ny * nz)
+    bases.append(bases[1] + 2 * nx * (ny - 1) * nz)
+    f, g = 0.0, np.zeros(3)
+    for a in (0, 1):
+        for b in (0, 1):
+            for e in (0, 1):
+                s = np.array([2 * a - 1, 2 * b - 1, 2 * e - 1], float)
+                val = V[((c[2] + e) * ny + c[1] + b) * nx + c[0] + a]
+                lin = 1 + r * s
+                q = 9 * (r @ r) - 19
+                f += val * lin.prod() * q / 64
+                for k in range(3):
+                    g[k] += val * (s[k] * np.prod(np.delete(lin, k)) * q + lin.prod() * 18 * r[k]) / 64
+    for ax in range(3):
+        o = [k for k in range(3) if k != ax]
+        for b1 in (0, 1):
+            for b2 in (0, 1):
+                idx3 = list(c)
+                idx3[o[0]] += b1
+                idx3[o[1]] += b2
+                i, j, k = idx3
+                if ax == 0:
+                    base = bases[0] + 2 * ((k * ny + j) * (nx - 1) + i)
+                elif ax == 1:
+                    base = bases[1] + 2 * ((k * (ny - 1) + j) * nx + i)
+                else:
+                    base = bases[2] + 2 * ((k * ny + j) * nx + i)
+                s1, s2 = 2 * b1 - 1, 2 * b2 - 1
+                for t, tt in ((0, -1 / 3), (1, 1 / 3)):
+                    val = V[base + t] * 9 / 64
+                    u_ = r[ax]
+                    pu = (1 - u_ * u_) * (1 + 9 * u_ * tt)
+                    p1, p2 = 1 + r[o[0]] * s1, 1 + r[o[1]] * s2
+                    f += val * pu * p1 * p2
+                    g[ax] += val * (-2 * u_ * (1 + 9 * u_ * tt) + (1 - u_ * u_) * 9 * tt) * p1 * p2
+                    g[o[0]] += val * pu * s1 * p2
+                    g[o[1]] += val * pu * p1 * s2
+    return f, g * 2 / sp
+
+
+def _cubic_scene(values, cells, lo, sp):
+    sc = scenes.beam_c1()
+    sc.ground = None
+    sc.sdf_grids = [(values, cells, lo, sp, "cubic")]
+    return sc
+
+
+def test_oracle_cubic_grid_matches_numpy_restatement(oracle_mod):
+    rng = np.random.default_rng(3)
+    cells, lo, sp = (3, 4, 2), np.array([-0.3, -0.5, 0.1]), np.array([0.2, 0.15, 0.3])
+    pts = cubic_layout_points(lo, sp, cells)
+    vals = rng.normal(size=len(pts)).astype(np.float32)
+    o = oracle_mod.Oracle(_cubic_scene(vals, cells, lo, sp))
+    hi = lo + sp * np.asarray(cells)
+    for p in rng.uniform(lo, hi, size=(200, 3)):
+        sd, g = o.grid_eval(0, p)
+        f, gr = serendipity(vals.astype(np.float64), lo, sp, cells, p)
+        assert abs(sd - f) < 1e-12 and np.abs(g - gr).max() < 1e-10
+    assert o.grid_eval(0, hi + 0.01) is None
+
+
+def test_cubic_grid_reproduces_cubic_polynomials(oracle_mod):
+    """The 32-node element interpolates every cubic polynomial exactly
+    (value and gradient), the property of the cubic Lagrange grid."""
+    rng = np.random.default_rng(4)
+    mons = [(a, b, c) for a in range(4) for b in range(4) for c in range(4) if a + b + c <= 3]
+    coef = rng.normal(size=len(mons))
+
+    def f(p):
+        return sum(k * p[..., 0] ** a * p[..., 1] ** b * p[..., 2] ** c for k, (a, b, c) in zip(coef, mons))
+
+    def grad(p, h=1e-6):
+        return np.array([(f(p + h * e) - f(p - h * e)) / (2 * h) for e in np.eye(3)])
+    cells, lo, sp = (2, 3, 2), np.array([-0.4, -0.3, -0.2]), np.array([0.4, 0.2, 0.2])
+    vals = f(cubic_layout_points(lo, sp, cells))
+    hi = lo + sp * np.asarray(cells)
+    for p in rng.uniform(lo, hi, size=(100, 3)):
+        fp, gp = serendipity(vals, lo, sp, cells, p)
+        assert abs(fp - f(p)) < 1e-12
+        assert np.abs(gp - grad(p)).max() < 1e-6
+
+
+def test_cubic_grid_of_sphere_and_box(capi_mod, oracle_mod):
+    """Analytic signed distances through the cubic grid: a radius-1 sphere
+    sampled at the nodes of 0.25 m cells interpolates to within 5e-4 of its
+    distance in the shell 0.6 < r < 1.4, a fifth of the trilinear grid's
+    error on the same vertices or less; a box mesh's cubic node values are
+    its exact distance."""
+    cells, lo = (12, 12, 12), np.array([-1.5, -1.5, -1.5])
+    sp = np.full(3, 3.0 / 12)
+    pts = cubic_layout_points(lo, sp, cells)
+    sph = (np.linalg.norm(pts, axis=1) - 1.0).astype(np.float32)
+    o = oracle_mod.Oracle(_cubic_scene(sph, cells, lo, sp))
+    n = 13 ** 3
+    lin = scenes.beam_c1()
+    lin.ground = None
+    lin.sdf_grids = [(sph[:n].reshape(13, 13, 13), (13, 13, 13), lo, sp)]
+    o_lin = oracle_mod.Oracle(lin)
+    rng = np.random.default_rng(5)
+    q = rng.normal(size=(300, 3))
+    q = q / np.linalg.norm(q, axis=1)[:, None] * rng.uniform(0.6, 1.4, size=(300, 1))
+    exact = np.linalg.norm(q, axis=1) - 1.0
+    err = max(abs(o.grid_eval(0, p)[0] - e) for p, e in zip(q, exact))
+    err_lin = max(abs(o_lin.grid_eval(0, p)[0] - e) for p, e in zip(q, exact))
+    assert err < 5e-4 and err < 0.2 * err_lin
+    blo, bhi = (-0.3, -0.2, -0.25), (0.4, 0.1, 0.35)
+    v, t = box_mesh(blo, bhi)
+    glo, ghi, gcells = np.array([-1.0, -0.8, -0.9]), np.array([1.1, 0.9, 1.0]), (7, 6, 5)
+    vals = capi_mod.sdf_cubic_from_mesh(v, t, glo, ghi, gcells)
+    exact = box_sdf(cubic_layout_points(glo, (ghi - glo) / np.asarray(gcells), gcells), blo, bhi)
+    assert np.abs(vals - exact).max() < 1e-6
+
+
+@pytest.mark.gpu
+def test_gpu_cubic_grid_contacts_match_oracle(capi_mod, oracle_mod):
+    """Contacts of the beam against a cubic grid of a box the beam's
+    underside sinks into: same vertices as the oracle, contact points (p +
+    |sd| n, from the interpolant and its gradient) within 1e-5 m."""
+    from conftest import make_pair
+    blo, bhi = (-0.2, -1.0, -0.2), (1.2, 0.06, 0.5)
+    v, t = box_mesh(blo, bhi)
+    lo, hi, cells = np.array([-0.4, -1.2, -0.4]), np.array([1.4, 0.4, 0.7]), (18, 16, 11)
+    vals = capi_mod.sdf_cubic_from_mesh(v, t, lo, hi, cells)
+    sc = _cubic_scene(vals, cells, lo, (hi - lo) / np.asarray(cells))
+    for mode in (1, 2):
+        g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=mode)
+        g.detect_contacts()
+        vg, qg = g.contacts()
+        vo, qo = o.detect_contacts()
+        assert len(vo) > 0
+        assert np.array_equal(vg, vo)
+        assert np.abs(qg - qo).max() < 1e-5
+        g.step(1)
+        o.step(1)
+        assert np.isfinite(g.positions()).all()
+        g.close()
