@@ -102,7 +102,8 @@ def test_gpu_adam_steps_against_fp64_adam(capi_mod):
     training step's gradient is that row's gradient, which sbs_mlp_loss_grad
     returns from the same kernels (the gradients themselves are checked
     against FP64 above).  Moves of parameters whose gradient is below 1e-6
-    depend on Adam's epsilon and on rounding; they stay within lr per step."""
+    depend on Adam's epsilon and on rounding; they stay within Adam's bound
+    on a step, lr (1 - b1) / sqrt(1 - b2)."""
     from oracle import mlp_oracle
     m = capi_mod.Mlp(seed=9)
     x1, t1 = data(1, seed=10)
@@ -122,7 +123,7 @@ def test_gpu_adam_steps_against_fp64_adam(capi_mod):
         big = np.abs(g) > 1e-6
         assert big.sum() > 10000
         assert np.abs((got - p)[big] - (ref - p)[big]).max() <= 2e-3 * lr
-        assert np.abs(got - p).max() <= lr * (1 + 1e-3)
+        assert np.abs(got - p).max() <= 3.2 * lr    # Adam's step bound, lr (1 - b1) / sqrt(1 - b2)
         p = got
 
 
