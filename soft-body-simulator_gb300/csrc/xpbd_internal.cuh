@@ -174,9 +174,11 @@ cudaError_t launch_edges(const SceneDev& s, const StepParams& p, int colour, int
 cudaError_t launch_residual_ex(const SceneDev& s, const StepParams& p, int block, int grid, int cnt_base,
                                cudaStream_t st, int zero_lam = 0, const JudgeOp* op = nullptr);
 cudaError_t launch_end_frame(const SceneDev& s, cudaStream_t st);
+// stage: tet records copied into shared memory one colour phase ahead (bulk
+// asynchronous copies per warp, csrc/xpbd_kernels.cu)
 cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
-                                    cudaStream_t st);
-cudaError_t persistent_occupancy(int block, int* ctas_per_sm);
+                                    cudaStream_t st, int stage = 0);
+cudaError_t persistent_occupancy(int block, int* ctas_per_sm, int stage = 0);
 // State transfer (transfer_kernels.cu): o2n maps a global input vertex id to
 // its library slot.
 cudaError_t launch_gather_xyz(const float4* src, const uint32_t* o2n, uint32_t v0, uint32_t nv, float* out,

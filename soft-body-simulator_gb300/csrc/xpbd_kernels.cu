@@ -254,6 +254,14 @@ __device__ __forceinline__ TetRec load_tet(const SceneDev& s, uint32_t t) {
     return r;
 }
 
+// The part of a record the staged copies do not carry: the model flag and
+// the multipliers.
+__device__ __forceinline__ void load_tet_dyn(const SceneDev& s, uint32_t t, TetRec& r) {
+    r.snh = s.model[t] != 0;
+    r.l0 = __ldcg(&s.lam0[t]);
+    r.l1 = r.snh ? __ldcg(&s.lam1[t]) : 0.0f;
+}
+
 // One elastic tet constraint (StVK: green_constraint.cpp:49-158; SNH coupled).
 __device__ __forceinline__ void project_tet_rec(const SceneDev& s, const StepParams& p, uint32_t t,
                                                 const TetRec& R, bool first) {
@@ -503,9 +511,106 @@ __device__ __forceinline__ bool wave_wait(const SceneDev& s, uint32_t need) {
     return s_ok != 0;
 }
 
-template <bool kWave>
+// ---- staged tet records (persistent mode, kStage): each warp copies the
+// 64-byte rest records (corner ids, DmInv rows) of the 32 tets it projects
+// first in the next colour phase into its own shared-memory buffer with four
+// bulk asynchronous copies completing on the warp's mbarrier, issued at the
+// start of the current phase - a whole phase and grid barrier of lead
+// instead of the load between the barrier's arrive and wait.  Two buffers
+// per warp alternate.  Dynamic shared memory: 2 x warps x 4 x 32 x 16 bytes.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void pmb_init(uint32_t mb) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+}
+
+// Bounded wait for the completion of phase `parity` of an mbarrier.
+__device__ __forceinline__ bool pmb_wait(uint32_t mb, uint32_t parity, unsigned long long limit_ns) {
+    unsigned long long t0 = 0;
+    for (uint32_t spins = 0;; ++spins) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mb), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (spins == 0) t0 = global_ns();
+        else if ((spins & 15u) == 0 && global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+struct WarpStage {
+    uint32_t buf_base;     // shared address of this warp's two buffers
+    uint32_t mb_base;      // shared address of this warp's two mbarriers
+    uint32_t phase[2];     // completed (and consumed) phases of each mbarrier
+    bool pending[2];       // a copy into the buffer is in flight or unconsumed
+    uint32_t n[2];         // tets staged in the buffer
+};
+
+constexpr uint32_t kStageWarpBytes = 4u * 32u * 16u;   // one buffer: ids + 3 DmInv rows of 32 tets
+
+// Lane 0 issues the copies of this warp's first chunk of colour `col` into
+// buffer `buf`; every lane records whether it did.
+__device__ __forceinline__ void stage_chunk(const SceneDev& s, const StepParams& p, int col, WarpStage& w,
+                                            int buf) {
+    const uint32_t b = p.colour_start[col], n = p.colour_start[col + 1] - b;
+    const uint32_t i0 = (((threadIdx.x >> 5) * gridDim.x + blockIdx.x) << 5);
+    const uint32_t cnt = i0 < n ? min(32u, n - i0) : 0u;
+    w.pending[buf] = cnt > 0;
+    w.n[buf] = cnt;
+    if (cnt == 0) return;
+    __syncwarp();   // every lane has read the buffer's previous contents
+    if ((threadIdx.x & 31u) == 0) {
+        const uint32_t bytes = cnt * 16u, dst = w.buf_base + (uint32_t)buf * kStageWarpBytes;
+        const uint32_t mb = w.mb_base + (uint32_t)buf * 8u;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(4u * bytes) : "memory");
+        const void* src[4] = {s.tet + b + i0, s.dm0 + b + i0, s.dm1 + b + i0, s.dm2 + b + i0};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(dst + (uint32_t)k * 512u), "l"(src[k]), "r"(bytes), "r"(mb) : "memory");
+    }
+}
+
+// Waits for buffer `buf` (false: the wait ran out, SBS_ETIMEOUT recorded).
+__device__ __forceinline__ bool stage_wait(const SceneDev& s, WarpStage& w, int buf) {
+    if (!w.pending[buf]) return true;
+    const bool ok = pmb_wait(w.mb_base + (uint32_t)buf * 8u, w.phase[buf] & 1u, s.wait_ns);
+    w.phase[buf]++;
+    w.pending[buf] = false;
+    if (!ok) atomicCAS(s.err, 0, kErrTimeout);
+    return ok;
+}
+
+template <bool kWave, bool kStage>
 __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int has_acc) {
     if (ld_relaxed(s.err) != 0) return;
+    extern __shared__ __align__(16) uint4 stage_smem[];
+    __shared__ __align__(8) unsigned long long s_pmb[2 * 16];
+    WarpStage ws{};
+    if (kStage) {
+        const uint32_t wib = threadIdx.x >> 5;
+        ws.buf_base = smem_u32(stage_smem) + wib * 2u * kStageWarpBytes;
+        ws.mb_base = smem_u32(&s_pmb[2 * wib]);
+        if ((threadIdx.x & 31u) == 0) {
+            pmb_init(ws.mb_base);
+            pmb_init(ws.mb_base + 8u);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncwarp();
+    }
+    int sb = 0;                // staging buffer of the current colour phase
+    // before leaving on an error: no bulk copy may still be writing into
+    // this CTA's shared memory
+    auto drain = [&]() {
+        if (kStage) {
+            stage_wait(s, ws, 0);
+            stage_wait(s, ws, 1);
+        }
+    };
     uint32_t done = 0;         // wavefront: colour phases this CTA has finished
     unsigned bar_target = 0;   // arrivals expected by the next barrier (host zeroes s.bar[0])
     double t = *s.time;
@@ -518,7 +623,7 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
             if (k < n) detect_item(s, p, k);
         }
     }
-    if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+    if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
     uint32_t cnt[kMaxPlanes];
     for (int pl = 0; pl < kMaxPlanes; ++pl) cnt[pl] = pl < p.n_planes ? min(__ldcg(&s.counters[pl]), s.n_surf) : 0u;
     const uint32_t cnt_body = p.body_contacts ? min(__ldcg(&s.counters[kMaxPlanes]), s.n_surf) : 0u;
@@ -527,20 +632,27 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
     for (int sub = 0; sub < p.substeps; ++sub) {
         const double t_next = t + p.dt_d;
         for_each_vertex(s.n_verts, [&](uint32_t i) { predict_vertex(s, p, i, t_next, has_acc); });
-        if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+        if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
         for (int it = 0; it < p.iterations; ++it) {
             const bool first = it == 0;
             uint32_t slot = (!kWave && p.first_tail > 0) ? first_slot(p, 0) : ~0u;
             TetRec rec;
-            if (slot != ~0u) rec = load_tet(s, slot);
+            if (kStage) {
+                // the frame's first colour phase is staged here; later ones
+                // by the phase before them
+                if (sub == 0 && it == 0 && p.first_tail > 0) stage_chunk(s, p, 0, ws, sb);
+                if (slot != ~0u) load_tet_dyn(s, slot, rec);
+            } else if (slot != ~0u) {
+                rec = load_tet(s, slot);
+            }
             for (int pl = 0; pl < p.n_planes; ++pl) {
                 if (cnt[pl] == 0) continue;
                 contact_phase(s, (uint32_t)pl * s.n_surf, cnt[pl], p, first);
-                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
             }
             if (cnt_body) {
                 contact_phase(s, (uint32_t)kMaxPlanes * s.n_surf, cnt_body, p, first);
-                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
             }
             if (kWave) {
                 // every colour, each CTA its own slice; wait only for the
@@ -566,36 +678,60 @@ __global__ void __launch_bounds__(512) k_frame_t(SceneDev s, StepParams p, int h
                 }
             } else {
             for (int col = 0; col < p.first_tail; ++col) {
+                if (kStage) {
+                    // the next colour phase of the frame (the next iteration's
+                    // or substep's first one after the last colour)
+                    const bool last = col + 1 == p.first_tail && it + 1 == p.iterations && sub + 1 == p.substeps;
+                    if (!last) stage_chunk(s, p, col + 1 < p.first_tail ? col + 1 : 0, ws, sb ^ 1);
+                    if (!stage_wait(s, ws, sb)) slot = ~0u;
+                    if (slot != ~0u) {
+                        const uint4* B = stage_smem + (threadIdx.x >> 5) * (2u * kStageWarpBytes / 16u) +
+                                         (uint32_t)sb * (kStageWarpBytes / 16u);
+                        const uint32_t lane = threadIdx.x & 31u;
+                        rec.id = B[lane];
+                        const uint4 r0 = B[32 + lane], r1 = B[64 + lane], r2 = B[96 + lane];
+                        rec.a = make_float4(__uint_as_float(r0.x), __uint_as_float(r0.y), __uint_as_float(r0.z),
+                                            __uint_as_float(r0.w));
+                        rec.b = make_float4(__uint_as_float(r1.x), __uint_as_float(r1.y), __uint_as_float(r1.z),
+                                            __uint_as_float(r1.w));
+                        rec.c = make_float4(__uint_as_float(r2.x), __uint_as_float(r2.y), __uint_as_float(r2.z),
+                                            __uint_as_float(r2.w));
+                    }
+                    sb ^= 1;
+                }
                 colour_phase_pf(s, p, col, first, slot, rec);
                 grid_arrive(s.bar, bar_target);
                 slot = col + 1 < p.first_tail ? first_slot(p, col + 1) : ~0u;
-                if (slot != ~0u) rec = load_tet(s, slot);
-                if (!grid_wait(s.bar, s.err, bar_target, s.wait_ns)) return;
+                if (slot != ~0u) {
+                    if (kStage) load_tet_dyn(s, slot, rec);
+                    else rec = load_tet(s, slot);
+                }
+                if (!grid_wait(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
             }
             }
             if (!kWave && p.first_tail < p.n_colours) {
                 if (blockIdx.x == 0) tail_phase(s, p, first);
-                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
             }
             if (kWave && (p.n_edge_colours > 0 || (it + 1 < p.iterations && any_contact))) {
                 // distance constraints and the next iteration's contacts touch
                 // vertices of any CTA: a grid barrier before them
-                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
             }
             for (int col = 0; col < p.n_edge_colours; ++col) {
                 for_each_spread(p.edge_start[col], p.edge_start[col + 1],
                                 [&](uint32_t k) { project_edge(s, p, k, first); });
-                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+                if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
             }
         }
         if (kWave && !(p.n_edge_colours > 0)) {
             // the velocity update reads every vertex
-            if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+            if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
         }
         for_each_vertex(s.n_verts, [&](uint32_t i) { finalize_vertex(s, p, i); });
         t = t_next;
     }
-    if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) return;
+    if (!grid_barrier(s.bar, s.err, bar_target, s.wait_ns)) { drain(); return; }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *s.time = t;
         for (int i = 0; i <= kMaxPlanes; ++i) {
@@ -836,12 +972,21 @@ cudaError_t launch_residual_ex(const SceneDev& s, const StepParams& p, int block
     return cudaGetLastError();
 }
 
-cudaError_t persistent_occupancy(int block, int* ctas_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame_t<false>, block, 0);
+static size_t stage_bytes(int block) { return (size_t)(block / 32) * 2u * kStageWarpBytes; }
+
+cudaError_t persistent_occupancy(int block, int* ctas_per_sm, int stage) {
+    if (stage) {
+        cudaError_t e = cudaFuncSetAttribute(k_frame_t<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)stage_bytes(512));
+        if (e != cudaSuccess) return e;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame_t<false, true>, block,
+                                                             stage_bytes(block));
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame_t<false, false>, block, 0);
 }
 
 cudaError_t wavefront_occupancy(int block, int* ctas_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame_t<true>, block, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_frame_t<true, false>, block, 0);
 }
 
 cudaError_t launch_wavefront_frame(const SceneDev& s, const StepParams& p, int block, int grid, cudaStream_t st) {
@@ -850,17 +995,20 @@ cudaError_t launch_wavefront_frame(const SceneDev& s, const StepParams& p, int b
     StepParams pc = p;
     void* args[] = {&sc, &pc, &has_acc};
     count_launch();
-    return cudaLaunchCooperativeKernel((const void*)k_frame_t<true>, dim3(grid), dim3(block), args, 0, st);
+    return cudaLaunchCooperativeKernel((const void*)k_frame_t<true, false>, dim3(grid), dim3(block), args, 0, st);
 }
 
 cudaError_t launch_persistent_frame(const SceneDev& s, const StepParams& p, int block, int grid,
-                                    cudaStream_t st) {
+                                    cudaStream_t st, int stage) {
     int has_acc = p.has_acc;
     SceneDev sc = s;
     StepParams pc = p;
     void* args[] = {&sc, &pc, &has_acc};
     count_launch();
-    return cudaLaunchCooperativeKernel((const void*)k_frame_t<false>, dim3(grid), dim3(block), args, 0, st);
+    if (stage)
+        return cudaLaunchCooperativeKernel((const void*)k_frame_t<false, true>, dim3(grid), dim3(block), args,
+                                           stage_bytes(block), st);
+    return cudaLaunchCooperativeKernel((const void*)k_frame_t<false, false>, dim3(grid), dim3(block), args, 0, st);
 }
 
 cudaError_t launch_set_error(int* err, int code, cudaStream_t st) {

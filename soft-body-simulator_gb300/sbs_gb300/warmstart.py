@@ -79,6 +79,123 @@ class Workload:
     make_scene: Callable | None = None   # seed -> a whole scene (one trajectory)
 
 
+def block_initial_state(x0: np.ndarray, seed: int):
+    """One trajectory of the 2.6M-tet block: the rest shape turned by a
+    random rotation of up to 0.3 rad about a random axis through its centre,
+    its lowest point raised to U(0.1, 1.0) m above the ground, and a random
+    initial velocity (horizontal U(-1, 1) m/s per axis, vertical U(-2, 0)).
+    Returns (positions, velocities)."""
+    rng = np.random.default_rng(seed)
+    axis = rng.normal(size=3)
+    axis /= np.linalg.norm(axis)
+    ang = rng.uniform(0.0, 0.3)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    R = np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * K @ K
+    c = x0.mean(0)
+    x = (x0 - c) @ R.T + c
+    x[:, 1] += rng.uniform(0.1, 1.0) - x[:, 1].min()
+    v = np.zeros_like(x)
+    v[:] = [rng.uniform(-1, 1), rng.uniform(-2, 0), rng.uniform(-1, 1)]
+    return x, v
+
+
+def generate_resets(scene: scenes.Scene, make_state, seeds, frames: int, keep: float, seed: int = 0,
+                    exec_mode: int = 0):
+    """As generate, for one large body whose trajectories differ only in
+    their initial state: one handle, the state replaced (set_state) at the
+    start of each trajectory, so the scene is built and coloured once."""
+    g = capi.Solver(scene, exec_mode=exec_mode)
+    dt = scene.frame_dt / scene.substeps
+    rng = np.random.default_rng(seed)
+    x0 = scene.bodies[0].x0
+    X, Y = [], []
+    for s in seeds:
+        x, v = make_state(x0, s)
+        g.set_state(-1, x, v)
+        for _ in range(frames):
+            g.detect_contacts()
+            for _ in range(scene.substeps):
+                g.predict(dt)
+                feat = g.features()
+                xp = g.predicted_all()
+                g.solve(dt, scene.iterations)
+                y = g.predicted_all() - xp - feat[:, 3:6]
+                sel = rng.random(len(feat)) < keep
+                X.append(feat[sel].astype(np.float32))
+                Y.append(y[sel].astype(np.float32))
+                g.update_velocities(dt)
+    g.close()
+    return np.concatenate(X), np.concatenate(Y)
+
+
+def block_judged(mlp, frames: int = 20, lead_frames: int = 5, check_every: int = 3, calibrate_every: int = 5,
+                 exec_mode: int = 0):
+    """The 2.6M-tet block as configured (dropped 0.5 m): plain frames and
+    judged warm-started frames (as judged_rate) from the same start, timed."""
+    sc = scenes.big_block()
+    out = {}
+    for judged in (False, True):
+        g = capi.Solver(sc, exec_mode=exec_mode)
+        g.step(lead_frames)
+        if judged:
+            g.set_warm_start(mlp, 0)
+            g.set_warm_judge(check_every, 0, calibrate_every, 0.0)
+        ms = [g.step_timed() for _ in range(frames)]
+        out["judged" if judged else "plain"] = {"ms_per_frame": float(np.mean(ms)), "frame_ms": ms,
+                                                "exec_mode": int(g.stats().exec_mode)}
+        if judged:
+            st = g.warm_stats()
+            out["judged"].update({"warm_substeps": int(st.warm_substeps),
+                                  "calibration_substeps": int(st.calibration_substeps),
+                                  "mean_sweeps_per_warm_substep": st.sweeps / max(1, st.warm_substeps),
+                                  "fallbacks": int(st.fallbacks), "capped": int(st.capped),
+                                  "mean_residual_ratio": st.mean_residual_ratio,
+                                  "max_residual_ratio": st.max_residual_ratio})
+            g.set_warm_start(None)
+        g.close()
+    out["frames_per_s_ratio"] = out["plain"]["ms_per_frame"] / out["judged"]["ms_per_frame"]
+    out["check_every"], out["calibrate_every"] = check_every, calibrate_every
+    return out
+
+
+def main_block(argv=None):
+    """C5's learned warm start: trajectories of the 2.6M-tet block from
+    random initial states (block_initial_state), a network trained on them,
+    and judged frames of the configured drop against plain ones; one JSON
+    line (python -m sbs_gb300.warmstart block ...)."""
+    import argparse
+    import json
+    import time
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train-seeds", type=int, default=200)
+    ap.add_argument("--frames", type=int, default=10)
+    ap.add_argument("--keep", type=float, default=1.0 / 32)
+    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--judge-frames", type=int, default=20)
+    ap.add_argument("--judge-check", type=int, default=3)
+    ap.add_argument("--judge-calibrate", type=int, default=5)
+    ap.add_argument("--save", default="")
+    args = ap.parse_args(argv)
+    sc = scenes.big_block()
+    t0 = time.perf_counter()
+    X, Y = generate_resets(sc, block_initial_state, list(range(5000, 5000 + args.train_seeds)), args.frames,
+                           args.keep)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    m, losses = fit(X, Y, steps=args.steps, batch=args.batch, lr=1e-3, seed=1)
+    t_fit = time.perf_counter() - t0
+    if args.save:
+        save_network(m, args.save, workload="block2m", train_trajectories=args.train_seeds, frames=args.frames,
+                     keep=args.keep, steps=args.steps, loss_first=losses[0], loss_last=losses[-1])
+    line = {"workload": "block2m", "train_trajectories": args.train_seeds, "frames": args.frames,
+            "samples": int(len(X)), "generate_s": t_gen, "train_steps": args.steps, "train_s": t_fit,
+            "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
+            "judged": block_judged(m, frames=args.judge_frames, check_every=args.judge_check,
+                                   calibrate_every=args.judge_calibrate)}
+    print(json.dumps(line))
+
+
 def _box_scene(seed: int) -> scenes.Scene:
     return scenes.box_drop(seed=seed)
 
@@ -402,4 +519,8 @@ def main(argv=None):
 
 
 if __name__ == "__main__":
-    main()
+    import sys
+    if len(sys.argv) > 1 and sys.argv[1] == "block":
+        main_block(sys.argv[2:])
+    else:
+        main()
