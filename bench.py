@@ -416,7 +416,7 @@ def main():
     ap.add_argument("--workload", default="beam98k")
     ap.add_argument("--exec-mode", type=int, default=0)
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: the library's choice)")
-    ap.add_argument("--stage-records", type=int, default=1, choices=[0, 1],
+    ap.add_argument("--stage-records", type=int, default=1, choices=[0, 1, 2],
                     help="cluster mode: stage each colour's tet records in shared memory one phase ahead")
     ap.add_argument("--cpu-budget", type=int, default=25_000_000,
                     help="tet projections in the single-thread CPU baseline sample")

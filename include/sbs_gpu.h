@@ -80,9 +80,11 @@ typedef struct sbs_gpu_params {
     uint32_t candidate_capacity;  /* >0: record up to this many broad-phase candidate pairs
                                      per detection for sbs_gpu_get_candidates */
     int32_t check_finite;         /* 1: sbs_gpu_get_* report SBS_ENAN on non-finite x */
-    int32_t stage_records;        /* cluster and persistent modes: 1 (default) copy each colour's
-                                     tet records into shared memory one phase ahead (bulk
-                                     asynchronous copies); 0 load them from global memory */
+    int32_t stage_records;        /* copy each colour's tet records into shared memory one phase
+                                     ahead (bulk asynchronous copies) instead of loading them from
+                                     global memory in the phase: 1 (default) in the cluster mode,
+                                     2 also in the persistent mode (measured slower there: 24.5
+                                     against 20.3 ms per frame of the 2.6M-tet block), 0 never */
     int32_t wait_limit_us;        /* bound of every device-side wait of the solver's kernels (grid
                                      barriers, staging waits) in microseconds, after which the
                                      kernel stops and the next synchronising call returns

@@ -561,6 +561,7 @@ sbs_status sbs_gpu_create(const sbs_gpu_params* p, sbs_gpu** out) {
     if (prm.gravity_mode != 0 && prm.gravity_mode != 1) return fail(nullptr, SBS_EINVAL, "gravity_mode");
     if (prm.exec_mode < 0 || prm.exec_mode > 4) return fail(nullptr, SBS_EINVAL, "exec_mode");
     if (prm.wait_limit_us < 0) return fail(nullptr, SBS_EINVAL, "wait_limit_us");
+    if (prm.stage_records < 0 || prm.stage_records > 2) return fail(nullptr, SBS_EINVAL, "stage_records");
     if (prm.block_size != 0 && (prm.block_size < 32 || prm.block_size > 512 || prm.block_size % 32))
         return fail(nullptr, SBS_EINVAL, "block_size must be a multiple of 32 in [32, 512]");
     int ndev = 0;
@@ -1570,7 +1571,7 @@ plan_again:
     }
     // 11. execution mode
     int occ = 0;
-    CU(h, persistent_occupancy(h->block, &occ, h->prm.stage_records));
+    CU(h, persistent_occupancy(h->block, &occ, h->prm.stage_records >= 2));
     uint32_t maxc = 0;
     for (uint32_t c = 0; c + 1 < h->colour_offsets.size(); ++c)
         maxc = std::max(maxc, h->colour_offsets[c + 1] - h->colour_offsets[c]);
@@ -1949,7 +1950,7 @@ static sbs_status run_frame(sbs_gpu* h, double dt, uint32_t substeps, uint32_t i
             CU(h, cudaMemsetAsync(h->d.bar, 0xFF, sizeof(unsigned), h->st));
             h->withhold_arrival = false;
         }
-        CU(h, launch_persistent_frame(h->d, p, h->pers_block, h->pers_grid, h->st, h->prm.stage_records));
+        CU(h, launch_persistent_frame(h->d, p, h->pers_block, h->pers_grid, h->st, h->prm.stage_records >= 2));
     } else {
         const GraphKey key{dt, substeps, iterations, 0};
         sbs_status s = run_graph(h, key, [&]() { return enqueue_frame_kernels(h, p); });
@@ -2012,7 +2013,7 @@ static sbs_status autotune_modes(sbs_gpu* h, double dt, uint32_t substeps, uint3
     for (int blk : {128, 256}) {
         if (!h->global_modes) break;
         int occ = 0;
-        if (persistent_occupancy(blk, &occ, h->prm.stage_records) != cudaSuccess || occ < 1) continue;
+        if (persistent_occupancy(blk, &occ, h->prm.stage_records >= 2) != cudaSuccess || occ < 1) continue;
         for (int g : {h->n_sm / 2, h->n_sm, 2 * h->n_sm, occ * h->n_sm}) {
             int gg = std::max(1, std::min({g, occ * h->n_sm, need}));
             bool dup = false;
