@@ -132,10 +132,11 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                  ::"r"(dst), "l"(src), "r"(bytes), "r"(mb) : "memory");
 }
 // Bounded wait for phase `parity` of the mbarrier; false after limit_ns
-// (SceneDev::wait_ns).
-__device__ __forceinline__ bool mb_wait(uint32_t mb, uint32_t parity, unsigned long long limit_ns) {
-    unsigned long long t0 = 0;
-    for (uint32_t spins = 0;; ++spins) {
+// (SceneDev::wait_ns).  One probe inline; the timed loop out of line, so the
+// colour-phase loop carries only the probe.
+__device__ __noinline__ bool mb_wait_slow(uint32_t mb, uint32_t parity, unsigned long long limit_ns) {
+    const unsigned long long t0 = cl_ns();
+    for (uint32_t spins = 1;; ++spins) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -144,9 +145,19 @@ __device__ __forceinline__ bool mb_wait(uint32_t mb, uint32_t parity, unsigned l
             : "r"(mb), "r"(parity)
             : "memory");
         if (done) return true;
-        if (spins == 0) t0 = cl_ns();
-        else if ((spins & 15u) == 0 && cl_ns() - t0 > limit_ns) return false;
+        if ((spins & 15u) == 0 && cl_ns() - t0 > limit_ns) return false;
     }
+}
+
+__device__ __forceinline__ bool mb_wait(uint32_t mb, uint32_t parity, unsigned long long limit_ns) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(mb), "r"(parity)
+        : "memory");
+    return done ? true : mb_wait_slow(mb, parity, limit_ns);
 }
 
 // Stage the records of tets [b, e) (at most c.stage) into buffer `buf`:
@@ -323,9 +334,325 @@ __device__ __forceinline__ double cl_residual(const SceneDev& s, const ClusterDe
 // contact records rec[slice * n_planes] (q.xyz, lambda; q.x = NaN when the
 // vertex has no contact with that plane), their slots in the global contact
 // list gidx[slice * n_planes], and the CTA's contact vertex list clist[slice].
-// MODE: kClModePlain, kClModeJudge (judged warm-started substeps, kClJudge)
-// or kClModeCalib (calibration frames, kClCalibrate); the plain
-// instantiation carries none of the judge's code.
+// The plain frame: the whole frame of a group per launch (prediction,
+// sweeps, velocity update), or one warm-started substep with the
+// kClExternal / kClCarry / kClContinue flags.  Kept apart from the judge's
+// kernel below so that the hot loop of plain frames carries none of its code
+// (measured: sharing one templated body made the 98k-tet beam's frame 4-5%
+// slower).
+__global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame_plain(SceneDev s, ClusterDev c, StepParams p,
+                                                                           double t0) {
+    extern __shared__ float4 sm[];
+    const uint32_t rank = cl_rank();
+    const uint32_t C = c.cluster_size;
+    const uint32_t slice = c.slice;
+    const float4* stg = sm;                        // 2 staging buffers of 4 * c.stage float4
+    float4* xi = sm + 8 * (size_t)c.stage;
+    float4* xn = xi + slice;
+    float4* vv = xi + 2 * slice;
+    const int S = p.n_planes + (c.body ? 1 : 0);   // contact slots per vertex: planes, then body
+    float4* rec = xi + 3 * slice;
+    float4* bn = rec + (size_t)slice * S;          // body contact normals (when c.body)
+    uint32_t* gidx = reinterpret_cast<uint32_t*>(bn + (c.body ? slice : 0));
+    uint32_t* clist = gidx + (size_t)slice * S;
+    float* lam_s = reinterpret_cast<float*>(clist + slice);   // [2 * lcap] multipliers of this CTA's tets
+    __shared__ uint32_t s_ncont;
+    __shared__ uint32_t s_any_contact;
+    // this CTA's tet range and multiplier base per colour of the current
+    // group, kept on chip: they head every colour phase's dependency chain
+    __shared__ uint32_t s_cb[kMaxColours], s_ce[kMaxColours], s_lb[kMaxColours];
+    __shared__ __align__(8) unsigned long long s_mb[2];   // one mbarrier per staging buffer
+    const uint32_t xi_base = smem_addr(xi);
+    const uint32_t stg_base = smem_addr(stg), stg_bytes = c.stage * 64u, mb_base = smem_addr(s_mb);
+    // colour phases run so far (all groups): staging buffer ph & 1, whose
+    // mbarrier is then in its (ph >> 1)-th phase
+    uint32_t ph = 0;
+    bool stage_bad = false;   // a staging wait expired: this thread projects nothing more
+    if (c.stage && threadIdx.x == 0) {
+        mb_init(mb_base);
+        mb_init(mb_base + 8);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    for (uint32_t g = cl_id(); g < c.n_groups; g += cl_count()) {
+        const GroupDesc gd = c.groups[g];
+        const uint32_t own0 = gd.v0 + rank * slice;
+        const uint32_t own1 = min(gd.v0 + (rank + 1) * slice, gd.v0 + gd.nv);
+        const uint32_t nown = own1 > own0 ? own1 - own0 : 0;
+        if (threadIdx.x == 0) s_ncont = 0;
+        for (uint32_t col = threadIdx.x; col < gd.n_col; col += blockDim.x) {
+            const uint32_t k = gd.col_base + col * C + rank;
+            s_cb[col] = c.col_start[k];
+            s_ce[col] = c.col_start[k + 1];
+            s_lb[col] = c.lam_base[gd.lb_base + col * C + rank];
+        }
+        __syncthreads();
+        // the group's first colour phase: its records arrive while the slice loads
+        if (c.stage && threadIdx.x == 0 && gd.n_col > 0 && p.substeps > 0 && p.iterations > 0)
+            stage_issue(s, c, s_cb[0], s_ce[0], stg_base + (ph & 1u) * stg_bytes, mb_base + (ph & 1u) * 8u);
+        const bool ext = (p.cl_flags & kClExternal) != 0;
+        // load own slice; ground contacts of own surface vertices from the
+        // frame-start positions (bvh_model.cpp:72-94 with the plane SDF)
+        for (uint32_t i = threadIdx.x; i < nown && ext; i += blockDim.x) {
+            // one warm-started substep: positions as predicted and moved by
+            // the warm start; contacts from the frame's list (below)
+            const uint32_t gv = own0 + i;
+            xi[i] = s.xi[gv];
+            xn[i] = s.xn[gv];
+            vv[i] = s.v[gv];
+            for (int pl = 0; pl < p.n_planes; ++pl)
+                rec[(size_t)i * S + pl] = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+            if (c.body) {
+                const float4 bq = c.bc_q[gv];
+                float4 r = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+                if (bq.w != 0.0f) {
+                    const float4 nn = c.bc_n[gv];
+                    r = make_float4(bq.x, bq.y, bq.z, 0.0f);
+                    bn[i] = nn;
+                    gidx[(size_t)i * S + p.n_planes] = __float_as_uint(nn.w);
+                }
+                rec[(size_t)i * S + p.n_planes] = r;
+            }
+        }
+        if (ext) {
+            __syncthreads();
+            for (int pl = 0; pl < p.n_planes; ++pl) {
+                const uint32_t cnt = min(__ldcg(&s.counters[pl]), s.n_surf);
+                for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                    const Contact ct = s.contacts[(size_t)pl * s.n_surf + k];
+                    const uint32_t gv = __float_as_uint(ct.q.w);
+                    if (gv < own0 || gv >= own1) continue;
+                    const uint32_t i = gv - own0;
+                    rec[(size_t)i * S + pl] = make_float4(ct.q.x, ct.q.y, ct.q.z, 0.0f);
+                    gidx[(size_t)i * S + pl] = k;
+                }
+            }
+            __syncthreads();
+            for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+                bool any = false;
+                for (int sl = 0; sl < S; ++sl) any |= !isnan(rec[(size_t)i * S + sl].x);
+                if (any) clist[atomicAdd(&s_ncont, 1u)] = i;
+            }
+            if (p.cl_flags & kClCarry) {
+                // the multipliers the warm start left (carried or fitted)
+                for (uint32_t col = 0; col < gd.n_col; ++col) {
+                    const uint32_t b = s_cb[col], e = s_ce[col];
+                    float* lb = lam_s + s_lb[col] - b;
+                    for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x) {
+                        lb[tt] = s.lam0[tt];
+                        lb[tt + c.lcap] = s.lam1[tt];
+                    }
+                }
+            }
+        }
+        for (uint32_t i = threadIdx.x; i < nown && !ext; i += blockDim.x) {
+            const uint32_t gv = own0 + i;
+            const float4 x = s.xn[gv];
+            xn[i] = x;
+            xi[i] = x;
+            vv[i] = s.v[gv];
+            bool any = false;
+            const bool surf = (c.vflags[gv] & 1u) != 0;
+            for (int pl = 0; pl < p.n_planes; ++pl) {
+                const Plane P = p.planes[pl];
+                const float sd = P.nx * x.x + P.ny * x.y + P.nz * x.z + P.d;
+                float4 r = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+                if (surf && sd < 0.0f) {
+                    const float ad = fabsf(sd);
+                    r = make_float4(x.x + P.nx * ad, x.y + P.ny * ad, x.z + P.nz * ad, 0.0f);
+                    any = true;
+                    // publish in the frame's global contact list (introspection, residual)
+                    const uint32_t slot = atomicAdd(&s.counters[pl], 1u);
+                    gidx[(size_t)i * S + pl] = slot;
+                    if (slot < s.n_surf) {
+                        Contact ct;
+                        ct.q = make_float4(r.x, r.y, r.z, __uint_as_float(gv));
+                        ct.n = make_float4(P.nx, P.ny, P.nz, 0.0f);
+                        s.contacts[(size_t)pl * s.n_surf + slot] = ct;
+                    }
+                }
+                rec[(size_t)i * S + pl] = r;
+            }
+            if (c.body) {
+                // body-body contact found by the spatial hash for this vertex
+                const float4 bq = c.bc_q[gv];
+                float4 r = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+                if (bq.w != 0.0f) {
+                    const float4 nn = c.bc_n[gv];
+                    r = make_float4(bq.x, bq.y, bq.z, 0.0f);
+                    bn[i] = nn;
+                    gidx[(size_t)i * S + p.n_planes] = __float_as_uint(nn.w);
+                    any = true;
+                }
+                rec[(size_t)i * S + p.n_planes] = r;
+            }
+            if (any) clist[atomicAdd(&s_ncont, 1u)] = i;
+        }
+        cluster_sync();
+        const uint32_t ncont = s_ncont;
+        // does any CTA of the cluster hold a contact this frame?  (the same
+        // answer everywhere, so the contact phase and its barrier are skipped
+        // cluster-wide when none does)
+        if (threadIdx.x == 0) {
+            uint32_t any = 0;
+            for (uint32_t r = 0; r < C; ++r) any |= ld_dsmem_u32(map_rank(smem_addr(&s_ncont), r));
+            s_any_contact = any;
+        }
+        __syncthreads();
+        const bool group_contacts = s_any_contact != 0;
+        double t = t0;
+        for (int sub = 0; sub < p.substeps; ++sub) {
+            const double t_next = t + p.dt_d;
+            // prediction of own vertices (timestep.cpp:35-43) + prescribed motion
+            for (uint32_t i = threadIdx.x; i < nown && !ext; i += blockDim.x) {
+                float4 v = vv[i];
+                const float4 x = xn[i];
+                if (v.w != 0.0f) {
+                    const KinGroup k = p.kin[(int)v.w - 1];
+                    const float4 rel = s.acc[own0 + i];
+                    float sn, cs;
+                    sincosf((float)(k.omega * t_next), &sn, &cs);
+                    const f3 ax = mk(k.ax, k.ay, k.az), r = mk(rel.x, rel.y, rel.z);
+                    const f3 rr = r * cs + cross(ax, r) * sn + ax * (dot(ax, r) * (1.0f - cs));
+                    xi[i] = make_float4(k.cx + rr.x, k.cy + rr.y, k.cz + rr.z, x.w);
+                    continue;
+                }
+                const float w = x.w;
+                float ax = 0.f, ay = 0.f, az = 0.f;
+                if (w > 0.0f) {
+                    if (p.gravity_mode == 1) { ax = p.gx * w; ay = p.gy * w; az = p.gz * w; }
+                    else { ax = p.gx; ay = p.gy; az = p.gz; }
+                    if (p.has_acc) {
+                        const float4 e = s.acc[own0 + i];
+                        ax += e.x; ay += e.y; az += e.z;
+                    }
+                }
+                v.x += ax * p.dt;
+                v.y += ay * p.dt;
+                v.z += az * p.dt;
+                vv[i] = v;
+                xi[i] = make_float4(x.x + v.x * p.dt, x.y + v.y * p.dt, x.z + v.z * p.dt, w);
+            }
+            cluster_sync();
+            for (int it = 0; it < p.iterations; ++it) {
+                const bool first = it == 0;                                 // contacts start from 0
+                const bool first_lam = first && !(p.cl_flags & kClCarry);  // elastic multipliers
+                // contacts: own vertices only (collision_constraint.cpp:21-41)
+                for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
+                    const uint32_t i = clist[k];
+                    float4 x = xi[i];
+                    for (int sl = 0; sl < S; ++sl) {
+                        float4 r = rec[(size_t)i * S + sl];
+                        if (isnan(r.x)) continue;
+                        if (first) r.w = 0.0f;
+                        float nx, ny, nz;
+                        if (sl < p.n_planes) {
+                            nx = p.planes[sl].nx; ny = p.planes[sl].ny; nz = p.planes[sl].nz;
+                        } else {
+                            const float4 nn = bn[i];
+                            nx = nn.x; ny = nn.y; nz = nn.z;
+                        }
+                        const float C_ = (x.x - r.x) * nx + (x.y - r.y) * ny + (x.z - r.z) * nz;
+                        if (C_ < 0.0f) {
+                            const float w = x.w;
+                            const float dl = -(C_ + p.contact_alpha_tilde * r.w) / (w + p.contact_alpha_tilde);
+                            r.w += dl;
+                            x.x += w * nx * dl;
+                            x.y += w * ny * dl;
+                            x.z += w * nz * dl;
+                        }
+                        rec[(size_t)i * S + sl] = r;
+                    }
+                    xi[i] = x;
+                }
+                if (S > 0 && group_contacts) cluster_sync();  // cluster-uniform condition
+                for (uint32_t col = 0; col < gd.n_col; ++col) {
+                    // this CTA's tets of the colour: those owning most of their vertices here
+                    const uint32_t b = s_cb[col], e = s_ce[col];
+                    float* lb = lam_s + s_lb[col] - b;
+                    if (c.stage) {
+                        const uint32_t buf = ph & 1u;
+                        if (threadIdx.x == 0 &&
+                            !(sub + 1 == p.substeps && it + 1 == p.iterations && col + 1 == gd.n_col)) {
+                            // next phase's records into the other buffer, whose
+                            // readers all passed the cluster barrier behind us
+                            const uint32_t nc = col + 1 == gd.n_col ? 0u : col + 1;
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            stage_issue(s, c, s_cb[nc], s_ce[nc], stg_base + (buf ^ 1u) * stg_bytes,
+                                        mb_base + (buf ^ 1u) * 8u);
+                        }
+                        if (b + threadIdx.x < e && !stage_bad) {
+                            if (mb_wait(mb_base + buf * 8u, (ph >> 1) & 1u, s.wait_ns)) {
+                                const float4* B = stg + (size_t)buf * 4 * c.stage;
+                                const uint4* I = reinterpret_cast<const uint4*>(B);
+                                for (uint32_t k = threadIdx.x; k < e - b; k += blockDim.x)
+                                    project_tet_dsmem(c, p,
+                                                      cl_make_tet(I[k], B[c.stage + k], B[2 * c.stage + k],
+                                                                  B[3 * c.stage + k], xi_base),
+                                                      first_lam, lb + b + k, c.lcap);
+                            } else {
+                                stage_bad = true;
+                                atomicCAS(s.err, 0, kErrTimeoutCl);
+                            }
+                        }
+                        ++ph;
+                    } else {
+                        for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
+                            project_tet_dsmem(c, p, cl_load_tet(s, c, tt, xi_base), first_lam, lb + tt, c.lcap);
+                    }
+                    cluster_sync();
+                }
+            }
+            // velocity update of own vertices (timestep.cpp:48-57)
+            for (uint32_t i = threadIdx.x; i < nown && !ext; i += blockDim.x) {
+                const float4 a = xi[i];
+                const float4 b = xn[i];
+                float4 v = vv[i];
+                v.x = (a.x - b.x) * p.inv_dt;
+                v.y = (a.y - b.y) * p.inv_dt;
+                v.z = (a.z - b.z) * p.inv_dt;
+                vv[i] = v;
+                xn[i] = a;
+            }
+            t = t_next;
+            __syncthreads();
+        }
+        // write back the slice and the multipliers of the last substep
+        for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) {
+            const uint32_t gv = own0 + i;
+            s.xi[gv] = xi[i];
+            s.xn[gv] = xn[i];
+            s.v[gv] = vv[i];
+        }
+        for (uint32_t col = 0; col < gd.n_col; ++col) {
+            const uint32_t k = gd.col_base + col * C + rank;
+            const uint32_t b = c.col_start[k], e = c.col_start[k + 1];
+            const float* lb = lam_s + c.lam_base[gd.lb_base + col * C + rank] - b;
+            for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x) {
+                s.lam0[tt] = lb[tt];
+                s.lam1[tt] = lb[tt + c.lcap];
+            }
+        }
+        for (uint32_t k = threadIdx.x; k < ncont; k += blockDim.x) {
+            const uint32_t i = clist[k];
+            for (int sl = 0; sl < S; ++sl) {
+                const float4 r = rec[(size_t)i * S + sl];
+                const uint32_t slot = gidx[(size_t)i * S + sl];
+                const size_t seg = sl < p.n_planes ? (size_t)sl : (size_t)kMaxPlanes;
+                if (!isnan(r.x) && slot < s.n_surf) s.contact_lam[seg * s.n_surf + slot] = r.w;
+            }
+        }
+        __syncthreads();
+    }
+    // no CTA may leave while a peer could still read its shared memory
+    cluster_sync();
+}
+
+// MODE: kClModeJudge (judged warm-started substeps, kClJudge),
+// kClModeCalib (calibration frames, kClCalibrate) or kClModePlain (further
+// chunks of a judged substep's sweeps in the global judge loop,
+// kClContinue).
 constexpr int kClModePlain = 0, kClModeJudge = 1, kClModeCalib = 2;
 template <int MODE>
 __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, ClusterDev c, StepParams p,
@@ -727,25 +1054,26 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame(SceneDev s, 
 // to the kernel's static shared memory rather than to this scene's need: a
 // later handle needing less must not make an earlier handle's launch invalid
 // (measured: no change in the frame time).
-template <int MODE>
-static cudaError_t cluster_configure_one(size_t smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_cluster_frame<MODE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+template <typename K>
+static cudaError_t cluster_configure_one(K kernel, size_t smem) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
     int dev = 0, optin = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
     cudaFuncAttributes fa;
-    if ((e = cudaFuncGetAttributes(&fa, k_cluster_frame<MODE>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess) return e;
     const size_t max_dyn = (size_t)optin > fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
     if (smem > max_dyn) return cudaErrorInvalidValue;
-    return cudaFuncSetAttribute(k_cluster_frame<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dyn);
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dyn);
 }
 
 cudaError_t cluster_configure(int block, size_t smem) {
     (void)block;
-    cudaError_t e = cluster_configure_one<kClModePlain>(smem);
-    if (e == cudaSuccess) e = cluster_configure_one<kClModeJudge>(smem);
-    if (e == cudaSuccess) e = cluster_configure_one<kClModeCalib>(smem);
+    cudaError_t e = cluster_configure_one(k_cluster_frame_plain, smem);
+    if (e == cudaSuccess) e = cluster_configure_one(k_cluster_frame<kClModePlain>, smem);
+    if (e == cudaSuccess) e = cluster_configure_one(k_cluster_frame<kClModeJudge>, smem);
+    if (e == cudaSuccess) e = cluster_configure_one(k_cluster_frame<kClModeCalib>, smem);
     return e;
 }
 
@@ -761,7 +1089,7 @@ cudaError_t cluster_max_active(int cluster_size, int block, size_t smem, int* n)
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaOccupancyMaxActiveClusters(n, (void*)k_cluster_frame<kClModePlain>, &cfg);
+    return cudaOccupancyMaxActiveClusters(n, (void*)k_cluster_frame_plain, &cfg);
 }
 
 cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const StepParams& p, double t0,
@@ -781,7 +1109,11 @@ cudaError_t launch_cluster_frame(const SceneDev& s, const ClusterDev& c, const S
     count_launch();
     if (p.cl_flags & kClJudge) return cudaLaunchKernelEx(&cfg, k_cluster_frame<kClModeJudge>, s, c, p, t0);
     if (p.cl_flags & kClCalibrate) return cudaLaunchKernelEx(&cfg, k_cluster_frame<kClModeCalib>, s, c, p, t0);
-    return cudaLaunchKernelEx(&cfg, k_cluster_frame<kClModePlain>, s, c, p, t0);
+    // a further chunk of a substep's sweeps (contact multipliers carried
+    // over, kClContinue) runs the general body, every other plain launch the
+    // lean one
+    if (p.cl_flags & kClContinue) return cudaLaunchKernelEx(&cfg, k_cluster_frame<kClModePlain>, s, c, p, t0);
+    return cudaLaunchKernelEx(&cfg, k_cluster_frame_plain, s, c, p, t0);
 }
 
 __global__ void k_store_time(double* t, double v) { *t = v; }

@@ -45,6 +45,7 @@ constexpr uint32_t kSmemBytes = kGroupBase + kGroups * kGroupBytes;  // 221,184
 
 struct TcArgs {
     const float* x;            // [n][16] raw features
+    int x_aligned;             // x is 16-byte aligned: rows load as float4
     int n;
     const float* mean;         // [16]
     const float* inv_std;      // [16]
@@ -225,10 +226,22 @@ __global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_infer_tc(TcArgs a) {
         // layer-1 A operand: normalised features
         {
             __align__(16) __nv_bfloat16 h[16];
+            float xv[kIn];
+            if (valid && a.x_aligned) {
+                // the row's 64 bytes as four 16-byte loads
+                const float4* xr = reinterpret_cast<const float4*>(a.x + (size_t)row * kIn);
+#pragma unroll
+                for (int q = 0; q < kIn / 4; ++q) {
+                    const float4 f = __ldg(xr + q);
+                    xv[4 * q] = f.x; xv[4 * q + 1] = f.y; xv[4 * q + 2] = f.z; xv[4 * q + 3] = f.w;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < kIn; ++k) xv[k] = valid ? __ldg(&a.x[(size_t)row * kIn + k]) : 0.0f;
+            }
 #pragma unroll
             for (int k = 0; k < kIn; ++k) {
-                const float f = valid ? (__ldg(&a.x[(size_t)row * kIn + k]) - __ldg(&a.mean[k])) * __ldg(&a.inv_std[k])
-                                      : 0.0f;
+                const float f = valid ? (xv[k] - __ldg(&a.mean[k])) * __ldg(&a.inv_std[k]) : 0.0f;
                 h[k] = __float2bfloat16(f);
             }
             *reinterpret_cast<uint4*>(gsm + kA1 + canon(r, 0, kIn)) = *reinterpret_cast<const uint4*>(&h[0]);
@@ -295,6 +308,7 @@ cudaError_t mlp_infer_tc(const MlpDev& d, const float* x, int n, float* y, int* 
     if (cs == cudaStreamCaptureStatusNone && (e = mlp_tc_configure()) != cudaSuccess) return e;
     TcArgs a;
     a.x = x;
+    a.x_aligned = ((uintptr_t)x & 15u) == 0;
     a.n = n;
     a.mean = d.mean;
     a.inv_std = d.inv_std;
