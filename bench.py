@@ -124,11 +124,15 @@ def other_workload(name, args, device, flush, peak):
 
 
 def mlp_throughput(args):
-    """Forward pass of the warm-start network on device-resident rows (the
-    vertex count of the 2.6M-tet block by default): the fused tcgen05
-    kernel (path 0) and the per-layer mma.sync GEMMs (path 1), CUDA events on
+    """The warm-start network on device-resident rows (the vertex count of
+    the 2.6M-tet block by default).  Forward: the fused tcgen05 kernel
+    (path 0) and the per-layer GEMMs (path 1) of both engines, CUDA events on
     the network's stream after warm-up, median of --steps calls; 70,400 FLOP
-    per row against the measured BF16 peak."""
+    per row against the measured BF16 peak.  Training: Adam steps at batch
+    65,536 on each engine, host wall time of 20 steps after 5 warm-up steps
+    (sbs_mlp_train returns when its stream is done); forward plus backward is
+    about 3 x 70,400 FLOP per row."""
+    import time
     import numpy as np
     import torch
     from sbs_gb300 import capi
@@ -143,13 +147,28 @@ def mlp_throughput(args):
         peak = 1900.0
     out = {"metric": "warm-start network forward, rows/s", "rows": args.mlp_rows, "flop_per_row": flop_per_row,
            "bf16_peak_tflops": peak}
-    for path, name in ((0, "tcgen05_fused"), (1, "mma_sync_layers")):
+    for path, engine, name in ((0, 0, "tcgen05_fused"), (1, 0, "tcgen05_layers"), (1, 1, "mma_sync_layers")):
+        m.set_gemm(engine)
         for _ in range(max(3, args.warmup)):
             m.forward_device(x.data_ptr(), args.mlp_rows, y.data_ptr(), path)
         ms = sorted(m.forward_device(x.data_ptr(), args.mlp_rows, y.data_ptr(), path) for _ in range(args.steps))
         med = ms[len(ms) // 2]
         tf = args.mlp_rows * flop_per_row / (med * 1e-3) / 1e12
         out[name] = {"ms": med, "rows_per_s": args.mlp_rows / (med * 1e-3), "tflops": tf, "frac": tf / peak}
+    batch = 65536
+    xs = rng.normal(size=(4 * batch, 16)).astype(np.float32)
+    ts = (0.01 * np.tanh(xs[:, :3])).astype(np.float32)
+    m.set_normalization(xs.mean(0), xs.std(0) + 1e-6, np.abs(ts).std(0) + 1e-9)
+    m.set_dataset(xs, ts)
+    for engine, name in ((0, "train_tcgen05"), (1, "train_mma_sync")):
+        m.set_gemm(engine)
+        m.train(5, batch, 1e-4, seed=1)
+        t0 = time.perf_counter()
+        m.train(20, batch, 1e-4, seed=2)
+        step_ms = (time.perf_counter() - t0) / 20 * 1e3
+        tf = batch * 3 * flop_per_row / (step_ms * 1e-3) / 1e12
+        out[name] = {"batch": batch, "ms_per_step": step_ms, "tflops": tf, "frac": tf / peak}
+    m.close()
     print(json.dumps(out), flush=True)
 
 

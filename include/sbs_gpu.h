@@ -410,7 +410,8 @@ sbs_status sbs_mlp_set_normalization(sbs_mlp* m, const float* in_mean, const flo
 sbs_status sbs_mlp_forward(sbs_mlp* m, const float* x, uint32_t n, float* y);
 /* As sbs_mlp_forward with the implementation chosen: 0 the fused tcgen05
  * kernel (the default; weights resident in shared memory, accumulators in
- * tensor memory), 1 the per-layer mma.sync GEMMs that training uses. */
+ * tensor memory), 1 the per-layer GEMMs that training uses (engine chosen by
+ * sbs_mlp_set_gemm). */
 sbs_status sbs_mlp_forward_path(sbs_mlp* m, const float* x, uint32_t n, float* y, int32_t path);
 /* The same on device buffers of the network's device (x [n*16], y [n*3]);
  * with ms != NULL the kernels' device time in milliseconds (CUDA events on
@@ -423,6 +424,12 @@ sbs_status sbs_mlp_loss_grad(sbs_mlp* m, const float* x, const float* t, uint32_
  * on random batches of `batch` rows; *loss = loss of the last batch. */
 sbs_status sbs_mlp_set_dataset(sbs_mlp* m, const float* x, const float* t, uint32_t n);
 sbs_status sbs_mlp_train(sbs_mlp* m, uint32_t steps, uint32_t batch, float lr, uint64_t seed, float* loss);
+/* Engine of the per-layer GEMMs (training, loss_grad, forward path 1): 0 the
+ * tcgen05 kernels (default; TMEM accumulators, split-K weight gradients summed
+ * in a fixed order), 1 the warp-level mma.sync kernels.  Each engine gives the
+ * same result bit for bit on every run; the two differ in summation order.
+ * loss_grad and train return SBS_ETIMEOUT when a tensor-core wait expired. */
+sbs_status sbs_mlp_set_gemm(sbs_mlp* m, int32_t engine);
 
 /* Attaches (m != NULL) or detaches the warm-start network.  While attached,
  * every substep of sbs_gpu_step runs predict -> features -> MLP ->

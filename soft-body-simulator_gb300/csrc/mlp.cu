@@ -24,30 +24,11 @@
 namespace sbs {
 
 // --------------------------------------------------------------------------
-// Generic BF16 GEMM on tensor cores:
-//   C[m, n] (f32) = beta * C[m, n] + sum_k A(m, k) * B(k, n) (+ bias[n])
-// with A(m, k) = A[m * sam + k * sak] and B(k, n) = B[k * sbk + n * sbn]
-// (BF16, arbitrary strides, so transposes are free).  Epilogue: optional
-// bias, optional SiLU into a BF16 copy, optional BF16 copy of C.
-// CTA tile 64 x 64, k-step 32, 4 warps of 32 x 32.
+// Generic BF16 GEMM on the warp-level tensor-core path (mma.sync m16n8k16),
+// the comparison engine for the tcgen05 GEMM of mlp_gemm_tc.cu; both take the
+// same GemmArgs (mlp_internal.cuh).  CTA tile 64 x 64, k-step 32, 4 warps of
+// 32 x 32.
 constexpr int GM = 64, GN = 64, GK = 32, GPAD = 8;
-
-struct GemmArgs {
-    const __nv_bfloat16* A;
-    long long sam, sak;
-    const __nv_bfloat16* B;
-    long long sbk, sbn;
-    float* C;             // [M x N] row-major, ldc
-    long long ldc;
-    float beta;
-    const float* bias;    // [N] or null
-    __nv_bfloat16* Cb;    // optional BF16 copy of C (pre-activation), ld = ldc
-    __nv_bfloat16* Act;   // optional BF16 SiLU(C), ld = ldc
-    int M, N, K;
-    int splitk;           // > 1: blockIdx.z takes a K slice and writes its partial product
-                          // to ws[z][M x N]; k_splitk_sum then adds the slices in order
-    float* ws;
-};
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
     asm volatile(
@@ -57,14 +38,12 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
-
 __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
     __shared__ __align__(16) __nv_bfloat16 As[GM][GK + GPAD];
     __shared__ __align__(16) __nv_bfloat16 Bs[GN][GK + GPAD];  // n-major, k contiguous
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int gid = lane >> 2, tig = lane & 3;
-    const int m0 = blockIdx.y * GM, n0 = blockIdx.x * GN;
+    const int m0 = blockIdx.x * GM, n0 = blockIdx.y * GN;
     const int kper = g.splitk > 1 ? ((g.K + g.splitk * GK - 1) / (g.splitk * GK)) * GK : g.K;
     const int kbeg = g.splitk > 1 ? blockIdx.z * kper : 0;
     const int kend = g.splitk > 1 ? min(g.K, kbeg + kper) : g.K;
@@ -123,52 +102,81 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
                 const int n = n0 + wn + j * 8 + tig * 2 + (r & 1);
                 if (m >= g.M || n >= g.N) continue;
                 float v = acc[i][j][r];
-                float* cp = g.C + m * g.ldc + n;
+                float* cp = g.C + (long long)m * g.ldc + n;
                 if (g.splitk > 1) {
                     g.ws[(size_t)blockIdx.z * g.M * g.N + (size_t)m * g.N + n] = v;
                     continue;
                 }
                 if (g.beta != 0.0f) v += g.beta * *cp;
                 if (g.bias) v += g.bias[n];
-                *cp = v;
-                if (g.Cb) g.Cb[m * g.ldc + n] = __float2bfloat16(v);
-                if (g.Act) g.Act[m * g.ldc + n] = __float2bfloat16(silu(v));
+                if (g.dsilu) v *= silu_grad(g.dsilu[(long long)m * g.ldc + n]);
+                if (g.C) *cp = v;
+                if (g.Cb) g.Cb[(long long)m * g.ldc + n] = __float2bfloat16(v);
+                if (g.Act) g.Act[(long long)m * g.ldc + n] = __float2bfloat16(silu(v));
+                if (g.T) g.T[(long long)n * g.ldt + m] = __float2bfloat16(g.Act ? silu(v) : v);
             }
 }
 
-// C[i] = sum over the K slices z = 0, 1, ... of ws[z][i], always in that
-// order: split-K products come out the same bit for bit on every run (an
-// atomic accumulation would add the slices in whatever order they finish).
+// C[i] = sum over the K slices z = 0, 1, ... of ws[z][i] in a fixed order:
+// four threads per element take consecutive quarters of the slices (each
+// added in slice order), and the quarters are added in order.  Split-K
+// products come out the same bit for bit on every run (an atomic
+// accumulation would add the slices in whatever order they finish).
 __global__ void k_splitk_sum(const float* __restrict__ ws, float* __restrict__ C, int mn, int splitk) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < mn; i += gridDim.x * blockDim.x) {
-        float s = 0.0f;
-        for (int z = 0; z < splitk; ++z) s += ws[(size_t)z * mn + i];
-        C[i] = s;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t >> 2), p = (int)(t & 3);
+    const int per = (splitk + 3) / 4, z0 = p * per, z1 = min(splitk, z0 + per);
+    float s = 0.0f;
+    if (i < mn) {
+#pragma unroll 8
+        for (int z = z0; z < z1; ++z) s += ws[(size_t)z * mn + i];
     }
+    // the four quarters, in order (lanes 4q .. 4q + 3 of a warp hold one element)
+    const float s1 = __shfl_down_sync(0xffffffffu, s, 1), s2 = __shfl_down_sync(0xffffffffu, s, 2),
+                s3 = __shfl_down_sync(0xffffffffu, s, 3);
+    if (p == 0 && i < mn) C[i] = ((s + s1) + s2) + s3;
 }
 
-static cudaError_t gemm(const GemmArgs& g, cudaStream_t st) {
-    dim3 grid((g.N + GN - 1) / GN, (g.M + GM - 1) / GM, g.splitk > 1 ? g.splitk : 1);
-    k_gemm<<<grid, 128, 0, st>>>(g);
+cudaError_t splitk_sum(const float* ws, float* C, int mn, int splitk, cudaStream_t st) {
+    k_splitk_sum<<<(int)(((long long)mn * 4 + 255) / 256), 256, 0, st>>>(ws, C, mn, splitk);
     count_launch();
-    if (g.splitk > 1) {
-        // the slices' sum into C (ldc == N for the split-K products)
-        const int mn = g.M * g.N;
-        k_splitk_sum<<<(mn + 255) / 256, 256, 0, st>>>(g.ws, g.C, mn, g.splitk);
-        count_launch();
-    }
     return cudaGetLastError();
 }
+
+cudaError_t gemm_mma_sync(const GemmArgs& g, cudaStream_t st) {
+    if (g.M <= 0 || g.N <= 0) return cudaSuccess;
+    dim3 grid((g.M + GM - 1) / GM, (g.N + GN - 1) / GN, g.splitk > 1 ? g.splitk : 1);
+    k_gemm<<<grid, 128, 0, st>>>(g);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // the slices' sum into C (ldc == N for the split-K products)
+    if (g.splitk > 1) return splitk_sum(g.ws, g.C, g.M * g.N, g.splitk, st);
+    return cudaSuccess;
+}
+
+// the handle's engine; the tcgen05 kernel reports a timed-out wait in tc_err
+static cudaError_t gemm(const MlpDev& d, GemmArgs g, cudaStream_t st) {
+    g.err = d.tc_err;
+    g.err_code = 3;
+    return d.engine == kGemmMmaSync ? gemm_mma_sync(g, st) : gemm_tc(g, st);
+}
+
+// split-K slices of a weight-gradient product over n rows (512 rows or more a slice)
+static int splitk_for(int n) { return std::max(1, std::min(kMaxSplitK, n / 512)); }
 
 // --------------------------------------------------------------------------
 // Elementwise kernels
 
-// xn = bf16((x - mean) / std), x [n][16]
-__global__ void k_norm_in(const float* x, const float* mean, const float* inv_std, __nv_bfloat16* xn, int n) {
+// xn = bf16((x - mean) / std), x [n][16]; xnT [16][n] its transpose (optional)
+__global__ void k_norm_in(const float* x, const float* mean, const float* inv_std, __nv_bfloat16* xn,
+                          __nv_bfloat16* xnT, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n * kIn) return;
     const int f = i % kIn;
-    xn[i] = __float2bfloat16((x[i] - mean[f]) * inv_std[f]);
+    const __nv_bfloat16 v = __float2bfloat16((x[i] - mean[f]) * inv_std[f]);
+    xn[i] = v;
+    if (xnT) xnT[(long long)f * n + i / kIn] = v;
 }
 
 // y = z4 * out_scale (raw output), z4 [n][3]
@@ -178,36 +186,51 @@ __global__ void k_scale_out(const float* z4, const float* scale, float* y, int n
     y[i] = z4[i] * scale[i % kOut];
 }
 
-// loss = mean_i sum_o (z4 - t / scale)^2 ; dz4 = 2 (z4 - t/scale) / n  (bf16 and f32)
-__global__ void k_loss(const float* z4, const float* t, const float* scale, float* dz4, __nv_bfloat16* dz4b,
-                       float* loss_acc, int n) {
+// loss = mean_i sum_o (z4 - t / scale)^2 ; dz4 = 2 (z4 - t/scale) / n  (bf16 and
+// the transposed bf16 copy dz4T [3][n])
+__global__ void k_loss(const float* z4, const float* t, const float* scale, __nv_bfloat16* dz4b,
+                       __nv_bfloat16* dz4T, float* loss_acc, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float e2 = 0.0f;
     if (i < n * kOut) {
         const float d = z4[i] - t[i] / scale[i % kOut];
-        dz4[i] = 2.0f * d / (float)n;
-        dz4b[i] = __float2bfloat16(2.0f * d / (float)n);
+        const __nv_bfloat16 b = __float2bfloat16(2.0f * d / (float)n);
+        dz4b[i] = b;
+        dz4T[(long long)(i % kOut) * n + i / kOut] = b;
         e2 = d * d;
     }
     for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(loss_acc, e2 / (float)n);
+    __shared__ float warp_sum[8];
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = e2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float b = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += warp_sum[w];
+        atomicAdd(loss_acc, b / (float)n);   // the reported loss only; gradients take no atomics
+    }
 }
 
-// dz = da * silu'(z), z kept in f32: silu'(z) = s (1 + z (1 - s)), s = sigmoid(z)
-__global__ void k_silu_back(const float* da, const float* z, __nv_bfloat16* dzb, float* dz, int count) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const float s = 1.0f / (1.0f + __expf(-z[i]));
-    const float v = da[i] * s * (1.0f + z[i] * (1.0f - s));
-    dz[i] = v;
-    dzb[i] = __float2bfloat16(v);
-}
-
-// db[j] = sum_rows dz[r][j]
-__global__ void k_colsum(const float* dz, float* db, int n, int cols) {
-    const int j = blockIdx.x;
+// db[o] = sum_r dzT[o][r] (the bias gradient from the transposed BF16 output
+// gradient): one block per row, 16-byte loads where aligned, a fixed-order
+// tree over the threads' partial sums.
+__global__ void k_rowsum_bf16(const __nv_bfloat16* __restrict__ X, long long ld, int n, float* __restrict__ out) {
+    const __nv_bfloat16* row = X + (long long)blockIdx.x * ld;
     float s = 0.0f;
-    for (int r = threadIdx.x; r < n; r += blockDim.x) s += dz[(long long)r * cols + j];
+    if ((ld & 7) == 0 && ((uintptr_t)X & 15) == 0) {
+        const int n8 = n / 8;
+        for (int q = threadIdx.x; q < n8; q += blockDim.x) {
+            const uint4 u = __ldg(reinterpret_cast<const uint4*>(row) + q);
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const float2 f = __bfloat1622float2(h[e]);
+                s += f.x + f.y;
+            }
+        }
+        for (int r = n8 * 8 + threadIdx.x; r < n; r += blockDim.x) s += __bfloat162float(row[r]);
+    } else {
+        for (int r = threadIdx.x; r < n; r += blockDim.x) s += __bfloat162float(row[r]);
+    }
     __shared__ float sh[256];
     sh[threadIdx.x] = s;
     __syncthreads();
@@ -215,12 +238,28 @@ __global__ void k_colsum(const float* dz, float* db, int n, int cols) {
         if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) db[j] = sh[0];
+    if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
 }
 
-// Adam on the FP32 masters, then refresh the BF16 copies.
-__global__ void k_adam(float* w, const float* gr, float* m1, float* m2, __nv_bfloat16* wb, int count, float lr,
-                       float b1, float b2, float eps, float c1, float c2) {
+// Where parameter i's BF16 copy goes in the transposed weight copies: weight
+// (o, c) of layer l (row-major [out][in] at woff[l]) to woff[l] + c * out + o;
+// biases keep their place.
+struct LayerMap {
+    int woff[4], fin[4], fout[4];
+};
+
+__device__ __forceinline__ int transposed_index(const LayerMap& L, int i) {
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        const int q = i - L.woff[l];
+        if (q >= 0 && q < L.fin[l] * L.fout[l]) return L.woff[l] + (q % L.fin[l]) * L.fout[l] + q / L.fin[l];
+    }
+    return i;
+}
+
+// Adam on the FP32 masters, then refresh the BF16 copies (plain and transposed).
+__global__ void k_adam(float* w, const float* gr, float* m1, float* m2, __nv_bfloat16* wb, __nv_bfloat16* wbT,
+                       LayerMap L, int count, float lr, float b1, float b2, float eps, float c1, float c2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
     const float g = gr[i];
@@ -231,11 +270,25 @@ __global__ void k_adam(float* w, const float* gr, float* m1, float* m2, __nv_bfl
     const float v = w[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
     w[i] = v;
     wb[i] = __float2bfloat16(v);
+    wbT[transposed_index(L, i)] = __float2bfloat16(v);
 }
 
-__global__ void k_to_bf16(const float* w, __nv_bfloat16* wb, int count) {
+__global__ void k_to_bf16(const float* w, __nv_bfloat16* wb, __nv_bfloat16* wbT, LayerMap L, int count) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) wb[i] = __float2bfloat16(w[i]);
+    if (i >= count) return;
+    wb[i] = __float2bfloat16(w[i]);
+    wbT[transposed_index(L, i)] = __float2bfloat16(w[i]);
+}
+
+static LayerMap layer_map(const MlpDev& d) {
+    LayerMap L;
+    const int fin[4] = {kIn, kHid, kHid, kHid}, fout[4] = {kHid, kHid, kHid, kOut};
+    for (int l = 0; l < 4; ++l) {
+        L.woff[l] = d.woff[l];
+        L.fin[l] = fin[l];
+        L.fout[l] = fout[l];
+    }
+    return L;
 }
 
 // gather rows idx[0..n) of (x, t) into contiguous batch buffers
@@ -263,10 +316,11 @@ static inline int nb(long long n, int b = 256) { return (int)((n + b - 1) / b); 
 // --------------------------------------------------------------------------
 // Network passes on device buffers (MlpDev holds weights and workspace).
 
-cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cudaStream_t st) {
+cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cudaStream_t st, bool keep_t) {
     cudaError_t e;
     if ((e = mlp_reserve(d, n)) != cudaSuccess) return e;
-    k_norm_in<<<nb((long long)n * kIn), 256, 0, st>>>(x, d.mean, d.inv_std, d.xn, n);
+    if (keep_t && (e = mlp_reserve_train(d, n)) != cudaSuccess) return e;
+    k_norm_in<<<nb((long long)n * kIn), 256, 0, st>>>(x, d.mean, d.inv_std, d.xn, keep_t ? d.xnT : nullptr, n);
     count_launch();
     const __nv_bfloat16* in = d.xn;
     int kin = kIn;
@@ -276,8 +330,12 @@ cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cuda
         g.B = d.wb[l]; g.sbk = 1; g.sbn = kin;        // B(k, n) = W[n][k]
         g.C = d.z[l]; g.ldc = kHid; g.beta = 0.0f; g.bias = d.b[l];
         g.Act = d.a[l];
+        if (keep_t) {
+            g.T = d.aT[l];
+            g.ldt = n;
+        }
         g.M = n; g.N = kHid; g.K = kin;
-        if ((e = gemm(g, st)) != cudaSuccess) return e;
+        if ((e = gemm(d, g, st)) != cudaSuccess) return e;
         in = d.a[l];
         kin = kHid;
     }
@@ -286,7 +344,7 @@ cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cuda
     g.B = d.wb[3]; g.sbk = 1; g.sbn = kHid;
     g.C = d.z[3]; g.ldc = kOut; g.beta = 0.0f; g.bias = d.b[3];
     g.M = n; g.N = kOut; g.K = kHid;
-    if ((e = gemm(g, st)) != cudaSuccess) return e;
+    if ((e = gemm(d, g, st)) != cudaSuccess) return e;
     if (y_raw) {
         k_scale_out<<<nb((long long)n * kOut), 256, 0, st>>>(d.z[3], d.out_scale, y_raw, n);
         count_launch();
@@ -294,38 +352,45 @@ cudaError_t mlp_forward_dev(MlpDev& d, const float* x, int n, float* y_raw, cuda
     return cudaGetLastError();
 }
 
-// Loss and gradient w.r.t. all parameters (into d.grad) for n rows.
+// Loss and gradient w.r.t. all parameters (into d.grad) for n rows.  Every
+// product reads its operands K-contiguous: the weight gradients
+// dW_l = dz_l^T act_{l-1} from the transposed copies dzT_l [out][n] and
+// actT_{l-1} [in][n] that the epilogues before them wrote, the input
+// gradients dz_l W_l from W_l^T; the SiLU backward is the input-gradient
+// product's epilogue.
 cudaError_t mlp_backward_dev(MlpDev& d, const float* x, const float* t, int n, cudaStream_t st) {
     cudaError_t e;
-    if ((e = mlp_forward_dev(d, x, n, nullptr, st)) != cudaSuccess) return e;
+    if ((e = mlp_forward_dev(d, x, n, nullptr, st, true)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(d.loss, 0, sizeof(float), st)) != cudaSuccess) return e;
-    k_loss<<<nb((long long)n * kOut), 256, 0, st>>>(d.z[3], t, d.out_scale, d.dz[3], d.dzb[3], d.loss, n);
+    k_loss<<<nb((long long)n * kOut), 256, 0, st>>>(d.z[3], t, d.out_scale, d.dzb[3], d.dzT[3], d.loss, n);
     count_launch();
     const int fin[4] = {kIn, kHid, kHid, kHid};
     const int fout[4] = {kHid, kHid, kHid, kOut};
     for (int l = 3; l >= 0; --l) {
         // dW_l[o][i] = sum_r dz_l[r][o] * act_{l-1}[r][i]
-        const __nv_bfloat16* act = l == 0 ? d.xn : d.a[l - 1];
         GemmArgs g{};
-        g.A = d.dzb[l]; g.sam = 1; g.sak = fout[l];    // A(m=o, k=r) = dz[r][o]
-        g.B = act; g.sbk = fin[l]; g.sbn = 1;           // B(k=r, n=i) = act[r][i]
+        g.A = d.dzT[l]; g.sam = n; g.sak = 1;           // A(m=o, k=r) = dzT[o][r]
+        g.B = l == 0 ? d.xnT : d.aT[l - 1];
+        g.sbk = 1; g.sbn = n;                           // B(k=r, n=i) = actT[i][r]
         g.C = d.grad + d.woff[l]; g.ldc = fin[l]; g.beta = 0.0f;
         g.M = fout[l]; g.N = fin[l]; g.K = n;
-        g.splitk = std::max(1, std::min(kMaxSplitK, n / 1024));
+        g.splitk = splitk_for(n);
         g.ws = d.splitk_ws;
-        if ((e = gemm(g, st)) != cudaSuccess) return e;
-        k_colsum<<<fout[l], 256, 0, st>>>(d.dz[l], d.grad + d.boff[l], n, fout[l]);
+        if ((e = gemm(d, g, st)) != cudaSuccess) return e;
+        // db_l[o] = sum_r dz_l[r][o]
+        k_rowsum_bf16<<<fout[l], 256, 0, st>>>(d.dzT[l], n, n, d.grad + d.boff[l]);
         count_launch();
         if (l == 0) break;
-        // da_{l-1}[r][i] = sum_o dz_l[r][o] * W_l[o][i]
+        // dz_{l-1}[r][i] = SiLU'(z_{l-1}[r][i]) sum_o dz_l[r][o] * W_l[o][i]
         GemmArgs h{};
         h.A = d.dzb[l]; h.sam = fout[l]; h.sak = 1;
-        h.B = d.wb[l]; h.sbk = fin[l]; h.sbn = 1;       // B(k=o, n=i) = W[o][i]
-        h.C = d.da; h.ldc = fin[l]; h.beta = 0.0f;
+        h.B = d.wbT[l]; h.sbk = 1; h.sbn = fout[l];     // B(k=o, n=i) = W^T[i][o]
+        h.C = nullptr; h.ldc = kHid; h.beta = 0.0f;
+        h.dsilu = d.z[l - 1];
+        h.Cb = d.dzb[l - 1];
+        h.T = d.dzT[l - 1]; h.ldt = n;
         h.M = n; h.N = fin[l]; h.K = fout[l];
-        if ((e = gemm(h, st)) != cudaSuccess) return e;
-        k_silu_back<<<nb((long long)n * kHid), 256, 0, st>>>(d.da, d.z[l - 1], d.dzb[l - 1], d.dz[l - 1], n * kHid);
-        count_launch();
+        if ((e = gemm(d, h, st)) != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
@@ -334,13 +399,14 @@ cudaError_t mlp_adam_dev(MlpDev& d, float lr, cudaStream_t st) {
     d.step += 1;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     const float c1 = 1.0f - powf(b1, (float)d.step), c2 = 1.0f - powf(b2, (float)d.step);
-    k_adam<<<nb(kParams), 256, 0, st>>>(d.w, d.grad, d.m1, d.m2, d.wball, kParams, lr, b1, b2, eps, c1, c2);
+    k_adam<<<nb(kParams), 256, 0, st>>>(d.w, d.grad, d.m1, d.m2, d.wball, d.wballT, layer_map(d), kParams, lr, b1, b2,
+                                        eps, c1, c2);
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t mlp_sync_bf16(MlpDev& d, cudaStream_t st) {
-    k_to_bf16<<<nb(kParams), 256, 0, st>>>(d.w, d.wball, kParams);
+    k_to_bf16<<<nb(kParams), 256, 0, st>>>(d.w, d.wball, d.wballT, layer_map(d), kParams);
     count_launch();
     return cudaGetLastError();
 }

@@ -19,8 +19,8 @@ static cudaError_t alloc_ws(void** p, size_t bytes) { return cudaMalloc(p, bytes
 
 cudaError_t mlp_reserve(MlpDev& d, int n) {
     if (n <= d.cap) return cudaSuccess;
-    void* ptrs[] = {d.xn, d.z[0], d.z[1], d.z[2], d.z[3], d.a[0], d.a[1], d.a[2], d.dz[0], d.dz[1], d.dz[2],
-                    d.dz[3], d.dzb[0], d.dzb[1], d.dzb[2], d.dzb[3], d.da, d.idx, d.bx, d.bt};
+    void* ptrs[] = {d.xn, d.z[0], d.z[1], d.z[2], d.z[3], d.a[0], d.a[1], d.a[2], d.dzb[0], d.dzb[1], d.dzb[2],
+                    d.dzb[3], d.idx, d.bx, d.bt};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     const size_t N = (size_t)n;
@@ -31,18 +31,35 @@ cudaError_t mlp_reserve(MlpDev& d, int n) {
     for (int l = 0; l < 3; ++l) {
         WS(d.z[l], N * kHid * sizeof(float));
         WS(d.a[l], N * kHid * sizeof(__nv_bfloat16));
-        WS(d.dz[l], N * kHid * sizeof(float));
         WS(d.dzb[l], N * kHid * sizeof(__nv_bfloat16));
     }
     WS(d.z[3], N * kOut * sizeof(float));
-    WS(d.dz[3], N * kOut * sizeof(float));
     WS(d.dzb[3], N * kOut * sizeof(__nv_bfloat16));
-    WS(d.da, N * kHid * sizeof(float));
     WS(d.idx, N * sizeof(uint32_t));
     WS(d.bx, N * kIn * sizeof(float));
     WS(d.bt, N * kOut * sizeof(float));
 #undef WS
     d.cap = e == cudaSuccess ? n : 0;
+    return e;
+}
+
+cudaError_t mlp_reserve_train(MlpDev& d, int n) {
+    if (n <= d.cap_t) return cudaSuccess;
+    void* ptrs[] = {d.xnT, d.aT[0], d.aT[1], d.aT[2], d.dzT[0], d.dzT[1], d.dzT[2], d.dzT[3]};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    const size_t N = (size_t)n;
+    cudaError_t e = cudaSuccess;
+#define WS(ptr, bytes) \
+    if (e == cudaSuccess) e = alloc_ws((void**)&(ptr), (bytes))
+    WS(d.xnT, N * kIn * sizeof(__nv_bfloat16));
+    for (int l = 0; l < 3; ++l) {
+        WS(d.aT[l], N * kHid * sizeof(__nv_bfloat16));
+        WS(d.dzT[l], N * kHid * sizeof(__nv_bfloat16));
+    }
+    WS(d.dzT[3], N * kOut * sizeof(__nv_bfloat16));
+#undef WS
+    d.cap_t = e == cudaSuccess ? n : 0;
     return e;
 }
 
@@ -61,11 +78,22 @@ static sbs_status mfail(sbs_mlp* m, sbs_status s, const std::string& msg) {
 
 static void free_all(sbs_mlp* m) {
     MlpDev& d = m->d;
-    void* ptrs[] = {d.xn, d.z[0], d.z[1], d.z[2], d.z[3], d.a[0], d.a[1], d.a[2], d.dz[0], d.dz[1], d.dz[2],
-                    d.dz[3], d.dzb[0], d.dzb[1], d.dzb[2], d.dzb[3], d.da, d.idx, d.bx, d.bt, d.data_x, d.data_t};
+    void* ptrs[] = {d.xn, d.z[0], d.z[1], d.z[2], d.z[3], d.a[0], d.a[1], d.a[2], d.dzb[0], d.dzb[1], d.dzb[2],
+                    d.dzb[3], d.idx, d.bx, d.bt, d.data_x, d.data_t,
+                    d.xnT, d.aT[0], d.aT[1], d.aT[2], d.dzT[0], d.dzT[1], d.dzT[2], d.dzT[3]};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (void* p : m->allocs) cudaFree(p);
+}
+
+// A tensor-core wait that timed out since the last check (the error flag is cleared).
+static sbs_status check_tc(sbs_mlp* m) {
+    int flag = 0;
+    MCU(m, cudaMemcpyAsync(&flag, m->d.tc_err, sizeof(int), cudaMemcpyDeviceToHost, m->st));
+    MCU(m, cudaStreamSynchronize(m->st));
+    if (!flag) return SBS_OK;
+    MCU(m, cudaMemsetAsync(m->d.tc_err, 0, sizeof(int), m->st));
+    return mfail(m, SBS_ETIMEOUT, "tensor-core product: a wait timed out");
 }
 
 extern "C" {
@@ -117,6 +145,7 @@ sbs_status sbs_mlp_create(int32_t device, uint64_t seed, sbs_mlp** out) {
     A((void**)&d.m1, kParams * sizeof(float));
     A((void**)&d.m2, kParams * sizeof(float));
     A((void**)&d.wball, kParams * sizeof(__nv_bfloat16));
+    A((void**)&d.wballT, kParams * sizeof(__nv_bfloat16));
     A((void**)&d.mean, kIn * sizeof(float));
     A((void**)&d.inv_std, kIn * sizeof(float));
     A((void**)&d.out_scale, kOut * sizeof(float));
@@ -140,6 +169,7 @@ sbs_status sbs_mlp_create(int32_t device, uint64_t seed, sbs_mlp** out) {
     }
     for (int l = 0; l < 4; ++l) {
         d.wb[l] = d.wball + d.woff[l];
+        d.wbT[l] = d.wballT + d.woff[l];
         d.b[l] = d.w + d.boff[l];
     }
     *out = m;
@@ -266,7 +296,7 @@ sbs_status sbs_mlp_loss_grad(sbs_mlp* m, const float* x, const float* t, uint32_
     cudaFree(dx);
     if (dt) cudaFree(dt);
     if (e != cudaSuccess) return mfail(m, SBS_ECUDA, cudaGetErrorString(e));
-    return SBS_OK;
+    return check_tc(m);
 }
 
 sbs_status sbs_mlp_set_dataset(sbs_mlp* m, const float* x, const float* t, uint32_t n) {
@@ -294,6 +324,12 @@ sbs_status sbs_mlp_train(sbs_mlp* m, uint32_t steps, uint32_t batch, float lr, u
     MCU(m, mlp_train_steps(m->d, (int)steps, (int)batch, lr, seed, m->st));
     if (loss) MCU(m, cudaMemcpyAsync(loss, m->d.loss, sizeof(float), cudaMemcpyDeviceToHost, m->st));
     MCU(m, cudaStreamSynchronize(m->st));
+    return check_tc(m);
+}
+
+sbs_status sbs_mlp_set_gemm(sbs_mlp* m, int32_t engine) {
+    if (!m || (engine != kGemmTc && engine != kGemmMmaSync)) return SBS_EINVAL;
+    m->d.engine = engine;
     return SBS_OK;
 }
 

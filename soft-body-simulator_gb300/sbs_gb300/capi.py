@@ -150,6 +150,7 @@ def load(build: bool = True):
         "sbs_mlp_loss_grad": [P, f32p, f32p, C.c_uint32, C.POINTER(C.c_float), C.c_void_p],
         "sbs_mlp_set_dataset": [P, f32p, f32p, C.c_uint32],
         "sbs_mlp_train": [P, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64, C.POINTER(C.c_float)],
+        "sbs_mlp_set_gemm": [P, C.c_int32],
     }
     for name, args in msig.items():
         fn = getattr(L, name)
@@ -604,3 +605,9 @@ class Mlp:
         loss = C.c_float()
         self._check(self.L.sbs_mlp_train(self.h, steps, batch, lr, seed, C.byref(loss)))
         return loss.value
+
+    GEMM_TC, GEMM_MMA_SYNC = 0, 1
+
+    def set_gemm(self, engine: int):
+        """Engine of the per-layer GEMMs: GEMM_TC (tcgen05, default) or GEMM_MMA_SYNC."""
+        self._check(self.L.sbs_mlp_set_gemm(self.h, engine))

@@ -287,12 +287,14 @@ def random_rotation(rng: np.random.Generator) -> np.ndarray:
 def box_drop(n_bodies: int = 512, seed: int = 3, cell: float = 0.05,
              min_cells: int = 4, max_cells: int = 24, arena: float = 20.0,
              frames: int = 600, substeps: int = 2, iterations: int = 20,
-             model: int = MODEL_STVK, body_contacts: bool = True) -> Scene:
+             model: int = MODEL_STVK, body_contacts: bool = True,
+             young: tuple = (1e4, 1e6)) -> Scene:
     """Batch of box bodies dropped onto the ground.
 
     Cells per axis are floor(log-uniform[min_cells, max_cells]), 5 tets per
-    cube; E log-uniform [1e4, 1e6], nu U(0.3, 0.49); drop height U(1, 10) m;
-    uniform random rotation; centres on a jittered grid over the arena.
+    cube; E log-uniform [young[0], young[1]] (1e4..1e6 Pa by default), nu
+    U(0.3, 0.49); drop height U(1, 10) m; uniform random rotation; centres on
+    a jittered grid over the arena.
     """
     rng = np.random.default_rng(seed)
     bodies = []
@@ -304,7 +306,7 @@ def box_drop(n_bodies: int = 512, seed: int = 3, cell: float = 0.05,
                                                   math.log(max_cells)))))
              for _ in range(3)]
         n = [min(max(v, min_cells), max_cells) for v in n]
-        young = math.exp(rng.uniform(math.log(1e4), math.log(1e6)))
+        young_b = math.exp(rng.uniform(math.log(young[0]), math.log(young[1])))
         nu = rng.uniform(0.3, 0.49)
         height = rng.uniform(1.0, 10.0)
         rot = random_rotation(rng)
@@ -314,7 +316,7 @@ def box_drop(n_bodies: int = 512, seed: int = 3, cell: float = 0.05,
         x0, tets = bar_5tet(n[0] + 1, n[1] + 1, n[2] + 1, cell)
         x0 = x0 - x0.mean(0)
         x0 = x0 @ rot.T + np.array([cx, height, cz])
-        bodies.append(Body(x0=x0, tets=tets, model=model, young=young,
+        bodies.append(Body(x0=x0, tets=tets, model=model, young=young_b,
                            poisson=nu, density=1000.0, x_init=x0.copy()))
         edge_sum += cell * (n[0] * 1.0)
         edge_n += n[0]

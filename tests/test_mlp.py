@@ -45,9 +45,15 @@ def blocks():
 
 
 @pytest.mark.gpu
-def test_gpu_forward_and_gradients_match_fp64(capi_mod):
+@pytest.mark.parametrize("engine", [0, 1], ids=["tcgen05", "mma_sync"])
+@pytest.mark.parametrize("n", [4096, 1003, 77])
+def test_gpu_forward_and_gradients_match_fp64(capi_mod, engine, n):
+    """Both GEMM engines; 4096 rows take the 16-byte operand loads and split
+    K, 1003 and 77 rows (not a multiple of 8) the element-wise loads and
+    ragged tiles."""
     m = capi_mod.Mlp(seed=3)
-    x, t = data(4096, seed=2)
+    m.set_gemm(engine)
+    x, t = data(n, seed=2)
     mean, std, scale = norm_of(x, t)
     m.set_normalization(mean, std, scale)
     p = m.params().astype(np.float64)
@@ -62,6 +68,24 @@ def test_gpu_forward_and_gradients_match_fp64(capi_mod):
 
 
 @pytest.mark.gpu
+def test_gpu_gemm_engines_agree(capi_mod):
+    """The tcgen05 and mma.sync engines read the same BF16 operands and
+    accumulate in FP32 in different orders: gradients agree to 5e-3 per
+    parameter block (a BF16 activation may round the other way)."""
+    x, t = data(20000, seed=12)
+    mean, std, scale = norm_of(x, t)
+    grads = []
+    for engine in (0, 1):
+        m = capi_mod.Mlp(seed=13)
+        m.set_gemm(engine)
+        m.set_normalization(mean, std, scale)
+        grads.append(m.loss_grad(x, t)[1].astype(np.float64))
+        m.close()
+    for sl in blocks():
+        assert np.linalg.norm(grads[0][sl] - grads[1][sl]) <= 5e-3 * np.linalg.norm(grads[1][sl]) + 1e-12
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("n", [1, 127, 128, 129, 4096, 300001])
 def test_tcgen05_inference_matches_fp64_and_gemm_path(capi_mod, n):
     """The fused tcgen05 kernel (path 0) against the FP64 network and the
@@ -73,12 +97,15 @@ def test_tcgen05_inference_matches_fp64_and_gemm_path(capi_mod, n):
     m.set_normalization(mean, std, scale)
     p = m.params().astype(np.float64)
     y_tc = m.forward(x, path=0)
+    y_layers = m.forward(x, path=1)       # per-layer tcgen05 GEMMs
+    m.set_gemm(m.GEMM_MMA_SYNC)
     y_mm = m.forward(x, path=1)
     assert np.isfinite(y_tc).all()
     k = min(n, 4096)
     y_ref = mlp_oracle.forward(p, x[:k], mean, std, scale)
     assert np.linalg.norm(y_tc[:k] - y_ref) <= 3e-2 * np.linalg.norm(y_ref) + 1e-6
     assert np.abs(y_tc - y_mm).max() <= 2e-2 * np.abs(y_mm).max() + 1e-6
+    assert np.abs(y_layers - y_mm).max() <= 2e-2 * np.abs(y_mm).max() + 1e-6
 
 
 @pytest.mark.gpu
@@ -128,7 +155,8 @@ def test_gpu_adam_steps_against_fp64_adam(capi_mod):
 
 
 @pytest.mark.gpu
-def test_gpu_training_is_reproducible(capi_mod):
+@pytest.mark.parametrize("engine", [0, 1], ids=["tcgen05", "mma_sync"])
+def test_gpu_training_is_reproducible(capi_mod, engine):
     """Two trainings from the same seeds end with identical parameters: the
     split-K weight gradients add their K slices in a fixed order."""
     x, t = data(40000, seed=6)
@@ -136,6 +164,7 @@ def test_gpu_training_is_reproducible(capi_mod):
     out = []
     for _ in range(2):
         m = capi_mod.Mlp(seed=7)
+        m.set_gemm(engine)
         m.set_normalization(mean, std, scale)
         m.set_dataset(x, t)
         m.train(50, 32768, 1e-3, seed=3)    # batches large enough to split K
