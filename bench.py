@@ -69,8 +69,8 @@ MATERIALS = {
 # frame for these kernels), from one ncu capture of the same workload and
 # execution mode
 TRAFFIC = {
-    ("beam-98304-snh-twist", "k_cluster_frame"): 7.01e6,
-    ("block-2621440-snh", "k_frame_t<false>"): 22.876e9 + 2.582e9,
+    ("beam-98304-snh-twist", "k_cluster_frame_plain"): 7.01e6,
+    ("block-2621440-snh", "k_frame_t<0, 0>"): 22.94e9 + 2.57e9,
 }
 
 
@@ -550,8 +550,8 @@ def main():
     st = solver.stats()
     footprint = scene_bytes(scene)
     resident = footprint < 100 * 1024 * 1024
-    kernel = {capi.EXEC_PERSISTENT: "k_frame_t<false>", capi.EXEC_CLUSTER: "k_cluster_frame",
-              capi.EXEC_WAVEFRONT: "k_frame_t<true>"}.get(st.exec_mode, "k_colour")
+    kernel = {capi.EXEC_PERSISTENT: "k_frame_t<0, 0>", capi.EXEC_CLUSTER: "k_cluster_frame_plain",
+              capi.EXEC_WAVEFRONT: "k_frame_t<1, 0>"}.get(st.exec_mode, "k_colour")
     # DRAM bytes (read + write) per launch of the dominant kernel from one ncu
     # capture of the same workload and mode
     traffic = TRAFFIC.get((scene.name, kernel))
