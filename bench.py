@@ -263,7 +263,7 @@ def bounded_sample(scene, budget: int):
     import dataclasses
     per_frame = scene.substeps * scene.iterations * scene.n_tets
     if per_frame <= budget:
-        frames = max(1, min(4, budget // per_frame))
+        frames = max(1, min(16, budget // per_frame))
         return scene, frames, f"{frames} frame(s) of {scene.name}"
     its = max(1, min(scene.iterations, budget // scene.n_tets))
     sub = dataclasses.replace(scene, substeps=1, iterations=its)
@@ -437,8 +437,8 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0: the library's choice)")
     ap.add_argument("--stage-records", type=int, default=1, choices=[0, 1, 2],
                     help="cluster mode: stage each colour's tet records in shared memory one phase ahead")
-    ap.add_argument("--cpu-budget", type=int, default=25_000_000,
-                    help="tet projections in the single-thread CPU baseline sample")
+    ap.add_argument("--cpu-budget", type=int, default=160_000_000,
+                    help="tet projections in the single-thread CPU baseline sample (about 10 s on one core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the judged warm-start leg")
     ap.add_argument("--also", default="block2m,boxes512",
