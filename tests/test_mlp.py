@@ -68,6 +68,24 @@ def test_gpu_forward_and_gradients_match_fp64(capi_mod, engine, n):
 
 
 @pytest.mark.gpu
+def test_gpu_gradients_with_empty_split_k_slices(capi_mod):
+    """70,001 rows: 136 split-K slices of 576 rows, the last 14 of them
+    empty (they contribute zero partial products), and a row count that is
+    not a multiple of 8, so every transposed operand takes the element-wise
+    loads.  Gradients against the FP64 network."""
+    m = capi_mod.Mlp(seed=21)
+    x, t = data(70001, seed=22)
+    mean, std, scale = norm_of(x, t)
+    m.set_normalization(mean, std, scale)
+    p = m.params().astype(np.float64)
+    loss, g = m.loss_grad(x, t)
+    loss_ref, g_ref = mlp_oracle.loss_grad(p, x, t, mean, std, scale)
+    assert loss == pytest.approx(loss_ref, rel=3e-2)
+    for sl in blocks():
+        assert np.linalg.norm(g[sl] - g_ref[sl]) <= 3e-2 * np.linalg.norm(g_ref[sl]) + 1e-12
+
+
+@pytest.mark.gpu
 def test_gpu_gemm_engines_agree(capi_mod):
     """The tcgen05 and mma.sync engines read the same BF16 operands and
     accumulate in FP32 in different orders: gradients agree to 5e-3 per
