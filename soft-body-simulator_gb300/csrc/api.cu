@@ -2010,7 +2010,7 @@ static sbs_status autotune_modes(sbs_gpu* h, double dt, uint32_t substeps, uint3
     const int need = std::max(1, (int)((maxc + 31) / 32));
     if (h->cl_feasible)
         for (int blk : {256, 320, 384, 512}) cands.push_back({SBS_EXEC_CLUSTER, blk, 0});
-    for (int blk : {128, 256}) {
+    for (int blk : {128, 256, 512}) {
         if (!h->global_modes) break;
         int occ = 0;
         if (persistent_occupancy(blk, &occ, h->prm.stage_records >= 2) != cudaSuccess || occ < 1) continue;
