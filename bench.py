@@ -70,7 +70,7 @@ MATERIALS = {
 # execution mode
 TRAFFIC = {
     ("beam-98304-snh-twist", "k_cluster_frame_plain"): 7.01e6,
-    ("block-2621440-snh", "k_frame_t<0, 0>"): 22.94e9 + 2.57e9,
+    ("block-2621440-snh", "k_frame_t<0, 0>"): 22.95e9 + 2.57e9,
 }
 
 
