@@ -159,7 +159,7 @@ def block_judged(mlp, frames: int = 20, lead_frames: int = 5, check_every: int =
 
 
 def main_block(argv=None):
-    """C5's learned warm start: trajectories of the 2.6M-tet block from
+    """The 2.6M-tet block's learned warm start: trajectories of the block from
     random initial states (block_initial_state), a network trained on them,
     and judged frames of the configured drop against plain ones; one JSON
     line (python -m sbs_gb300.warmstart block ...)."""
