@@ -89,6 +89,11 @@ typedef struct sbs_gpu_params {
                                      barriers, staging waits) in microseconds, after which the
                                      kernel stops and the next synchronising call returns
                                      SBS_ETIMEOUT (0: 2 s) */
+    int32_t colour_size_cap;      /* scenes that run in the global modes only: colours are
+                                     rebalanced (more of them if needed) so that none holds more
+                                     than this many tets - one tet per resident thread of the
+                                     persistent kernel and phase.  0 (default): the device's
+                                     resident threads (512 per SM); -1: no cap */
 } sbs_gpu_params;
 
 typedef struct sbs_gpu_material {

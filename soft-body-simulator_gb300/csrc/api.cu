@@ -222,7 +222,7 @@ static void invert3(const double m[3][3], double r[3][3], double* det) {
 // cap of ~T/K per colour to balance colour sizes.  Returns the colour count
 // or -1 if more than kMaxColours are needed.
 static int colour_tets(const std::vector<uint32_t>& tets, uint32_t n_verts, const std::vector<uint32_t>& order,
-                       std::vector<int32_t>& colour) {
+                       std::vector<int32_t>& colour, uint32_t size_cap = 0) {
     const size_t T = order.size();
     colour.assign(tets.size() / 4, -1);
     std::vector<std::array<uint64_t, 2>> vm(n_verts, {0ull, 0ull});
@@ -356,10 +356,15 @@ static int colour_tets(const std::vector<uint32_t>& tets, uint32_t n_verts, cons
         }
     }
     // balance the classes: move tets of oversized classes into the smallest
-    // class they fit (no shared vertex); the colour count does not change
+    // class they fit (no shared vertex).  The colour count does not change,
+    // unless a size cap asks for more classes than there are: then empty
+    // classes are added for the moves to fill
+    if (size_cap > 0 && (uint64_t)K * size_cap < T)
+        K = std::min(kMaxColours, (int)((T + size_cap - 1) / size_cap));
     std::vector<uint32_t> size(K, 0);
     for (uint32_t t : order) size[colour[t]]++;
-    const uint32_t cap = (uint32_t)std::ceil((double)T / K * 1.02) + 1;
+    uint32_t cap = (uint32_t)std::ceil((double)T / K * 1.02) + 1;
+    if (size_cap > 0) cap = std::max((uint32_t)((T + K - 1) / K), std::min(cap, size_cap));
     for (auto& m : vm) m = {0ull, 0ull};
     for (uint32_t t : order) mark(t, colour[t]);
     for (uint32_t t : order) {
@@ -431,7 +436,7 @@ static int hint_colouring(const uint32_t* tets, uint32_t T, uint32_t V, const in
 
 static int plan_sweep(const double* x0, uint32_t V, const uint32_t* tets, uint32_t T, const int32_t* model,
                       std::vector<uint32_t>& order, std::vector<uint32_t>& offsets, std::vector<uint32_t>& split,
-                      const int32_t* hint = nullptr, bool* bad_hint = nullptr) {
+                      const int32_t* hint = nullptr, bool* bad_hint = nullptr, uint32_t size_cap = 0) {
     auto mdl = [&](uint32_t t) { return model ? model[t] : (int32_t)SBS_MODEL_STVK; };
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (uint32_t i = 0; i < V; ++i)
@@ -451,7 +456,7 @@ static int plan_sweep(const double* x0, uint32_t V, const uint32_t* tets, uint32
     std::stable_sort(morder.begin(), morder.end(), [&](uint32_t a, uint32_t b) { return tm[a] < tm[b]; });
     std::vector<uint32_t> tv(tets, tets + 4ull * T);
     std::vector<int32_t> colour, hinted;
-    int K = colour_tets(tv, V, morder, colour);
+    int K = colour_tets(tv, V, morder, colour, size_cap);
     const int Kh = hint_colouring(tets, T, V, hint, hinted);
     if (bad_hint) *bad_hint = Kh == -2;
     if (Kh > 0 && (K < 0 || Kh <= K)) {
@@ -549,6 +554,7 @@ sbs_status sbs_gpu_params_default(sbs_gpu_params* p) {
     p->check_finite = 1;
     p->stage_records = 1;
     p->wait_limit_us = 0;
+    p->colour_size_cap = 0;
     return SBS_OK;
 }
 
@@ -561,6 +567,7 @@ sbs_status sbs_gpu_create(const sbs_gpu_params* p, sbs_gpu** out) {
     if (prm.gravity_mode != 0 && prm.gravity_mode != 1) return fail(nullptr, SBS_EINVAL, "gravity_mode");
     if (prm.exec_mode < 0 || prm.exec_mode > 4) return fail(nullptr, SBS_EINVAL, "exec_mode");
     if (prm.wait_limit_us < 0) return fail(nullptr, SBS_EINVAL, "wait_limit_us");
+    if (prm.colour_size_cap < -1) return fail(nullptr, SBS_EINVAL, "colour_size_cap");
     if (prm.stage_records < 0 || prm.stage_records > 2) return fail(nullptr, SBS_EINVAL, "stage_records");
     if (prm.block_size != 0 && (prm.block_size < 32 || prm.block_size > 512 || prm.block_size % 32))
         return fail(nullptr, SBS_EINVAL, "block_size must be a multiple of 32 in [32, 512]");
@@ -1068,8 +1075,13 @@ plan_again:
         h->n_colours = (uint32_t)(h->colour_offsets.size() - 1);
     } else {
         bool bad = false;
+        // without the cluster mode, colours of at most one tet per resident
+        // thread of the persistent kernel (512 per SM at its 128 registers)
+        const uint32_t size_cap = h->cl_feasible || h->prm.colour_size_cap < 0 ? 0u
+                                  : h->prm.colour_size_cap > 0           ? (uint32_t)h->prm.colour_size_cap
+                                                                         : (uint32_t)h->n_sm * 512u;
         K = plan_sweep(h->x0.data(), V, h->tets.data(), T, h->tet_model.data(), h->tet_order, h->colour_offsets,
-                       split, h->tet_hint.data(), &bad);
+                       split, h->tet_hint.data(), &bad, size_cap);
         if (bad) return fail(h, SBS_EINVAL, "two tets of one given colour share a vertex");
         if (K < 0) return fail(h, SBS_ECOLOUR, "constraint graph needs more than 128 colours");
         h->n_colours = (uint32_t)K;

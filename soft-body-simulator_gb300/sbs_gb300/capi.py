@@ -33,7 +33,8 @@ class Params(C.Structure):
                 ("block_size", C.c_int32), ("ctas_per_sm", C.c_int32),
                 ("tail_threshold", C.c_int32), ("body_contacts", C.c_int32),
                 ("hash_cell", C.c_float), ("candidate_capacity", C.c_uint32),
-                ("check_finite", C.c_int32), ("stage_records", C.c_int32), ("wait_limit_us", C.c_int32)]
+                ("check_finite", C.c_int32), ("stage_records", C.c_int32), ("wait_limit_us", C.c_int32),
+                ("colour_size_cap", C.c_int32)]
 
 
 class WarmStats(C.Structure):

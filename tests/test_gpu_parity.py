@@ -433,3 +433,33 @@ def test_snh_kernel_against_closed_form_stress(capi_mod, kind):
     extrapolated = 2 * scaled[1] - scaled[0]
     assert np.abs(scaled[1] - f).max() < 0.05 * np.abs(f).max()      # first order already close
     assert np.abs(extrapolated - f).max() < 3e-3 * np.abs(f).max()
+
+
+def test_colour_size_cap(capi_mod, oracle_mod):
+    """Scenes that run in the global modes only: colours are rebalanced into
+    more classes so that none holds more tets than the cap (one per resident
+    thread of the persistent kernel by default).  With a small cap: every
+    class within it, vertex-disjoint, at least ceil(T / cap) classes, and one
+    frame against the oracle replaying that sweep within twice its FP32 noise
+    floor."""
+    sc = _batch(24, seed=11)
+    g0 = capi_mod.Solver(sc, exec_mode=capi_mod.EXEC_PERSISTENT, colour_size_cap=-1)
+    _, off0 = g0.tet_order()
+    g0.close()
+    T = sc.n_tets
+    cap = int(np.ceil(T / (len(off0) - 1) * 0.8))
+    g, o = make_pair(sc, capi_mod, oracle_mod, exec_mode=capi_mod.EXEC_PERSISTENT, colour_size_cap=cap)
+    order, off = g.tet_order()
+    sizes = np.diff(off)
+    assert len(sizes) >= -(-T // cap) > len(off0) - 1
+    assert sizes.max() <= cap
+    assert np.array_equal(np.sort(order), np.arange(T))
+    tets = np.concatenate([b.tets.astype(np.int64) + sum(len(bb.x0) for bb in sc.bodies[:i])
+                           for i, b in enumerate(sc.bodies)])
+    for c in range(len(off) - 1):
+        v = tets[order[off[c]:off[c + 1]]].ravel()
+        assert len(np.unique(v)) == len(v)
+    g.step(1)
+    o.step(1)
+    err = float(np.abs(g.positions() - o.get()).max())
+    assert err < 2 * oracle_mod.noise_floor(sc, 1, order, off, n_seeds=2) + 1e-7
