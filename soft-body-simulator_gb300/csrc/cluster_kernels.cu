@@ -47,6 +47,16 @@ __device__ __forceinline__ uint32_t cl_count() {
 __device__ __forceinline__ void cluster_sync() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+// the two halves of cluster_sync, for work between a CTA's arrival and the
+// barrier's completion
+__device__ __forceinline__ void cluster_arrive() {
+    __syncwarp();
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+    __syncwarp();
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -368,6 +378,8 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame_plain(SceneD
     // mbarrier is then in its (ph >> 1)-th phase
     uint32_t ph = 0;
     bool stage_bad = false;   // a staging wait expired: this thread projects nothing more
+    ClTet nrec{};             // this thread's first record of the next colour phase, when have_next
+    bool have_next = false;
     if (c.stage && threadIdx.x == 0) {
         mb_init(mb_base);
         mb_init(mb_base + 8);
@@ -571,22 +583,31 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame_plain(SceneD
                     // this CTA's tets of the colour: those owning most of their vertices here
                     const uint32_t b = s_cb[col], e = s_ce[col];
                     float* lb = lam_s + s_lb[col] - b;
+                    // the frame's next colour phase: the next colour, or the
+                    // next iteration's or substep's first one after the last
+                    const bool last_phase = sub + 1 == p.substeps && it + 1 == p.iterations && col + 1 == gd.n_col;
+                    const uint32_t nc = col + 1 == gd.n_col ? 0u : col + 1;
                     if (c.stage) {
                         const uint32_t buf = ph & 1u;
-                        if (threadIdx.x == 0 &&
-                            !(sub + 1 == p.substeps && it + 1 == p.iterations && col + 1 == gd.n_col)) {
+                        if (threadIdx.x == 0 && !last_phase) {
                             // next phase's records into the other buffer, whose
                             // readers all passed the cluster barrier behind us
-                            const uint32_t nc = col + 1 == gd.n_col ? 0u : col + 1;
                             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                             stage_issue(s, c, s_cb[nc], s_ce[nc], stg_base + (buf ^ 1u) * stg_bytes,
                                         mb_base + (buf ^ 1u) * 8u);
                         }
                         if (b + threadIdx.x < e && !stage_bad) {
-                            if (mb_wait(mb_base + buf * 8u, (ph >> 1) & 1u, s.wait_ns)) {
+                            // the first record came in during the last barrier (have_next)
+                            if (have_next || mb_wait(mb_base + buf * 8u, (ph >> 1) & 1u, s.wait_ns)) {
                                 const float4* B = stg + (size_t)buf * 4 * c.stage;
                                 const uint4* I = reinterpret_cast<const uint4*>(B);
-                                for (uint32_t k = threadIdx.x; k < e - b; k += blockDim.x)
+                                const uint32_t k0 = threadIdx.x;
+                                project_tet_dsmem(c, p,
+                                                  have_next ? nrec
+                                                            : cl_make_tet(I[k0], B[c.stage + k0], B[2 * c.stage + k0],
+                                                                          B[3 * c.stage + k0], xi_base),
+                                                  first_lam, lb + b + k0, c.lcap);
+                                for (uint32_t k = k0 + blockDim.x; k < e - b; k += blockDim.x)
                                     project_tet_dsmem(c, p,
                                                       cl_make_tet(I[k], B[c.stage + k], B[2 * c.stage + k],
                                                                   B[3 * c.stage + k], xi_base),
@@ -597,11 +618,32 @@ __global__ void __launch_bounds__(kClusterMaxBlock) k_cluster_frame_plain(SceneD
                             }
                         }
                         ++ph;
+                        // arrive, then take this thread's first record of the next
+                        // phase out of its staging buffer while the other CTAs
+                        // arrive: the wait for the copy and the shared-memory loads
+                        // leave the head of the next phase
+                        cluster_arrive();
+                        have_next = false;
+                        if (!last_phase && !stage_bad && s_cb[nc] + threadIdx.x < s_ce[nc]) {
+                            const uint32_t nbuf = ph & 1u;
+                            if (mb_wait(mb_base + nbuf * 8u, (ph >> 1) & 1u, s.wait_ns)) {
+                                const float4* B = stg + (size_t)nbuf * 4 * c.stage;
+                                const uint4* I = reinterpret_cast<const uint4*>(B);
+                                const uint32_t k0 = threadIdx.x;
+                                nrec = cl_make_tet(I[k0], B[c.stage + k0], B[2 * c.stage + k0], B[3 * c.stage + k0],
+                                                   xi_base);
+                                have_next = true;
+                            } else {
+                                stage_bad = true;
+                                atomicCAS(s.err, 0, kErrTimeoutCl);
+                            }
+                        }
+                        cluster_wait();
                     } else {
                         for (uint32_t tt = b + threadIdx.x; tt < e; tt += blockDim.x)
                             project_tet_dsmem(c, p, cl_load_tet(s, c, tt, xi_base), first_lam, lb + tt, c.lcap);
+                        cluster_sync();
                     }
-                    cluster_sync();
                 }
             }
             // velocity update of own vertices (timestep.cpp:48-57)
