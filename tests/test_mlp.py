@@ -189,3 +189,15 @@ def test_gpu_training_is_reproducible(capi_mod, engine):
         out.append(m.params())
         m.close()
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.gpu
+def test_gemm_engine_argument(capi_mod):
+    m = capi_mod.Mlp(seed=1)
+    with pytest.raises(capi_mod.SbsError):
+        m.set_gemm(2)
+    with pytest.raises(capi_mod.SbsError):
+        m.set_gemm(-1)
+    m.set_gemm(m.GEMM_MMA_SYNC)
+    m.set_gemm(m.GEMM_TC)
+    m.close()
