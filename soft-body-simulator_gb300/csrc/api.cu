@@ -217,6 +217,50 @@ static void invert3(const double m[3][3], double r[3][3], double* det) {
     r[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) / d;
 }
 
+// Moves tets of classes above `cap` into the smallest class they fit (no
+// shared vertex), visiting the tets in `order`.  When K classes cannot hold
+// T tets at `cap`, empty classes are added first (K' = ceil(T / cap)) for the
+// moves to fill.  A tet that fits nowhere stays.  Returns the class count.
+static int balance_classes(const std::vector<uint32_t>& tets, uint32_t n_verts, const std::vector<uint32_t>& order,
+                           std::vector<int32_t>& colour, int K, uint32_t cap) {
+    const size_t T = order.size();
+    if ((uint64_t)K * cap < T) K = std::min(kMaxColours, (int)((T + cap - 1) / cap));
+    cap = std::max(cap, (uint32_t)((T + K - 1) / K));
+    std::vector<uint32_t> size(K, 0);
+    for (uint32_t t : order) size[colour[t]]++;
+    std::vector<std::array<uint64_t, 2>> vm(n_verts, {0ull, 0ull});
+    auto mark = [&](uint32_t t, int c) {
+        for (int k = 0; k < 4; ++k) {
+            if (c < 64) vm[tets[4 * t + k]][0] |= 1ull << c;
+            else vm[tets[4 * t + k]][1] |= 1ull << (c - 64);
+        }
+    };
+    for (uint32_t t : order) mark(t, colour[t]);
+    for (uint32_t t : order) {
+        const int c = colour[t];
+        if (size[c] <= cap) continue;
+        uint64_t f0 = 0, f1 = 0;
+        for (int k = 0; k < 4; ++k) {
+            f0 |= vm[tets[4 * t + k]][0];
+            f1 |= vm[tets[4 * t + k]][1];
+        }
+        int best = -1;
+        for (int d = 0; d < K; ++d) {
+            const bool used = d < 64 ? ((f0 >> d) & 1ull) : ((f1 >> (d - 64)) & 1ull);
+            if (used || size[d] >= cap) continue;
+            if (best < 0 || size[d] < size[best]) best = d;
+        }
+        if (best < 0) continue;
+        // bit c stays set at t's vertices: conservative, as c is oversized
+        // and takes no tets
+        colour[t] = best;
+        size[c]--;
+        size[best]++;
+        mark(t, best);
+    }
+    return K;
+}
+
 // Colours tets (given in `order`, a Morton order) so that no two tets of a
 // colour share a vertex.  First-fit greedy, then a second pass with a size
 // cap of ~T/K per colour to balance colour sizes.  Returns the colour count
@@ -355,44 +399,10 @@ static int colour_tets(const std::vector<uint32_t>& tets, uint32_t n_verts, cons
             K = K2;
         }
     }
-    // balance the classes: move tets of oversized classes into the smallest
-    // class they fit (no shared vertex).  The colour count does not change,
-    // unless a size cap asks for more classes than there are: then empty
-    // classes are added for the moves to fill
-    if (size_cap > 0 && (uint64_t)K * size_cap < T)
-        K = std::min(kMaxColours, (int)((T + size_cap - 1) / size_cap));
-    std::vector<uint32_t> size(K, 0);
-    for (uint32_t t : order) size[colour[t]]++;
+    // balance the classes: at most ~T/K (2% slack), or the size cap
     uint32_t cap = (uint32_t)std::ceil((double)T / K * 1.02) + 1;
-    if (size_cap > 0) cap = std::max((uint32_t)((T + K - 1) / K), std::min(cap, size_cap));
-    for (auto& m : vm) m = {0ull, 0ull};
-    for (uint32_t t : order) mark(t, colour[t]);
-    for (uint32_t t : order) {
-        const int c = colour[t];
-        if (size[c] <= cap) continue;
-        uint64_t f0 = 0, f1 = 0;
-        for (int k = 0; k < 4; ++k) {
-            f0 |= vm[tets[4 * t + k]][0];
-            f1 |= vm[tets[4 * t + k]][1];
-        }
-        int best = -1;
-        for (int d = 0; d < K; ++d) {
-            const bool used = d < 64 ? ((f0 >> d) & 1ull) : ((f1 >> (d - 64)) & 1ull);
-            if (used || size[d] >= cap) continue;
-            if (best < 0 || size[d] < size[best]) best = d;
-        }
-        if (best < 0) continue;
-        // bit c stays set at t's vertices: conservative, as c is oversized
-        // and takes no tets
-        colour[t] = best;
-        size[c]--;
-        size[best]++;
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t v = tets[4 * t + k];
-            if (best < 64) vm[v][0] |= 1ull << best;
-            else vm[v][1] |= 1ull << (best - 64);
-        }
-    }
+    if (size_cap > 0) cap = std::min(cap, size_cap);
+    K = balance_classes(tets, n_verts, order, colour, K, cap);
     return K;
 }
 
@@ -460,9 +470,16 @@ static int plan_sweep(const double* x0, uint32_t V, const uint32_t* tets, uint32
     const int Kh = hint_colouring(tets, T, V, hint, hinted);
     if (bad_hint) *bad_hint = Kh == -2;
     if (Kh > 0 && (K < 0 || Kh <= K)) {
-        // the caller's colouring needs no more colours than the heuristics
+        // the caller's colouring needs no more colours than the heuristics;
+        // under a size cap its oversized classes are rebalanced as above
         K = Kh;
         colour.swap(hinted);
+        if (size_cap > 0) {
+            std::vector<uint32_t> csz(K, 0);
+            for (uint32_t t = 0; t < T; ++t) csz[colour[t]]++;
+            if (*std::max_element(csz.begin(), csz.end()) > size_cap)
+                K = balance_classes(tv, V, morder, colour, K, size_cap);
+        }
     }
     if (K < 0) return -1;
     std::vector<uint32_t> csize(K, 0);

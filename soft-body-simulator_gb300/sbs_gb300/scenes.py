@@ -110,6 +110,40 @@ def lattice_colours_6tet(width: int, height: int, depth: int) -> np.ndarray:
     return (4 * np.arange(6)[None, :] + lat[:, None]).ravel().astype(np.uint32)
 
 
+# A 34-colouring of bar_5tet's tets on the 4 x 4 x 4-cube torus (cubes
+# (i, j, k) mod 4, five tets each in bar_5tet's order), found by TabuCol
+# (Hertz & de Werra 1987) for this project.  Any two tets of a grid that share
+# a vertex also share it on the torus, so the pattern repeated over any grid
+# is a valid colouring.  Every colour holds 9 or 10 of the torus's 320 tets.
+_COLOURS_5TET_P4 = np.array([
+    27, 2, 9, 4, 24, 12, 31, 14, 10, 0, 33, 24, 32, 12, 29, 16, 22, 1, 10, 18,
+    7, 8, 11, 31, 25, 16, 21, 22, 20, 18, 11, 7, 28, 19, 25, 30, 23, 13, 32, 0,
+    30, 2, 29, 17, 33, 10, 31, 24, 14, 32, 29, 30, 5, 33, 12, 22, 27, 18, 1, 16,
+    15, 19, 22, 28, 8, 11, 6, 9, 15, 16, 25, 11, 0, 2, 26, 14, 7, 29, 25, 31,
+    6, 19, 26, 30, 3, 23, 1, 22, 28, 5, 19, 20, 1, 21, 8, 14, 31, 23, 4, 33,
+    17, 12, 32, 20, 15, 6, 16, 33, 13, 14, 2, 0, 27, 6, 17, 26, 14, 5, 19, 9,
+    11, 7, 4, 26, 24, 3, 5, 9, 28, 23, 1, 2, 15, 8, 4, 21, 23, 3, 6, 28,
+    12, 17, 27, 21, 0, 25, 7, 20, 30, 13, 3, 27, 24, 17, 18, 13, 5, 20, 10, 32,
+    24, 11, 14, 20, 10, 29, 24, 9, 4, 32, 26, 10, 4, 29, 30, 28, 8, 7, 16, 22,
+    21, 8, 27, 1, 28, 31, 0, 13, 18, 25, 15, 24, 7, 12, 11, 18, 33, 0, 13, 25,
+    19, 14, 17, 10, 30, 33, 32, 21, 22, 29, 10, 14, 20, 30, 31, 32, 18, 22, 16, 29,
+    4, 18, 8, 31, 2, 15, 11, 16, 33, 12, 17, 2, 11, 6, 0, 25, 12, 33, 15, 9,
+    29, 33, 1, 16, 26, 5, 17, 3, 7, 23, 8, 5, 19, 1, 13, 27, 9, 21, 6, 17,
+    3, 5, 19, 2, 12, 15, 27, 30, 22, 9, 26, 4, 21, 3, 2, 14, 15, 23, 31, 20,
+    4, 0, 26, 9, 6, 28, 3, 23, 19, 1, 17, 13, 8, 5, 6, 27, 26, 11, 7, 10,
+    5, 32, 21, 25, 13, 7, 18, 27, 31, 20, 21, 28, 4, 15, 22, 24, 20, 19, 3, 23,
+], dtype=np.uint32).reshape(4, 4, 4, 5)
+
+
+def lattice_colours_5tet(width: int, height: int, depth: int) -> np.ndarray:
+    """A 34-colouring of bar_5tet's tets (same arguments, in vertices): the
+    torus pattern _COLOURS_5TET_P4 repeated with period 4 cubes.  32 tets meet
+    at the vertices the centre tets use, so 32 colours is the bound; the
+    library's greedy colourings need 36 on the 2.6M-tet block."""
+    i, j, k = np.meshgrid(np.arange(width - 1), np.arange(height - 1), np.arange(depth - 1), indexing="ij")
+    return _COLOURS_5TET_P4[i.ravel() % 4, j.ravel() % 4, k.ravel() % 4].ravel().astype(np.uint32)
+
+
 def signed_volumes(x: np.ndarray, tets: np.ndarray) -> np.ndarray:
     """V = det([x1-x4, x2-x4, x3-x4]) / 6 (green_constraint.cpp:160-173)."""
     t = tets.astype(np.int64)
@@ -358,14 +392,17 @@ def hanging_block(alpha: float = 1e-7, beta: float = 0.0, frames: int = 60, iter
 
 def big_block(nx: int = 128, ny: int = 64, nz: int = 64, h: float = 0.02,
               frames: int = 200, substeps: int = 4, iterations: int = 30,
-              drop: float = 0.5) -> Scene:
+              drop: float = 0.5, lattice: bool = False) -> Scene:
     """Large SNH block (default 2,621,440 tets / 545,025 vertices), E 5e5,
     nu 0.48, dropped onto the ground from ``drop`` metres, with self contacts
-    (vertex against the block's own surface triangles, spatial hash)."""
+    (vertex against the block's own surface triangles, spatial hash).
+    lattice: carry the periodic 34-colouring (lattice_colours_5tet) as the
+    body's colouring."""
     x0, tets = bar_5tet(nx + 1, ny + 1, nz + 1, h)
     x0 = x0 + np.array([0.0, drop, 0.0])
     b = Body(x0=x0, tets=tets, model=MODEL_SNH, young=5e5, poisson=0.48,
-             density=1000.0, x_init=x0.copy())
+             density=1000.0, x_init=x0.copy(),
+             colours=lattice_colours_5tet(nx + 1, ny + 1, nz + 1) if lattice else None)
     return Scene(f"block-{len(tets)}-snh", [b], 1.0 / 60.0, substeps,
                  iterations, frames, ground=((0.0, 1.0, 0.0), 0.0), body_contacts=2)
 

@@ -73,6 +73,27 @@ def test_plan_sweep_colour_count_98k_beam():
         assert len(np.unique(v)) == len(v)
 
 
+@pytest.mark.parametrize("dims", [(9, 9, 9), (10, 7, 6), (13, 5, 9)])
+def test_lattice_colouring_of_the_5tet_split(dims):
+    """The periodic 34-colouring of bar_5tet (4 x 4 x 4-cube torus pattern):
+    no two tets of a colour share a vertex on grids of any size (32 tets meet
+    at a centre tet's vertex), and the planner uses it unless its own
+    colouring of a small grid needs fewer colours."""
+    x0, t = scenes.bar_5tet(*dims, 0.1)
+    col = scenes.lattice_colours_5tet(*dims)
+    assert len(col) == len(t) and len(np.unique(col)) == 34
+    for c in range(34):
+        v = t[col == c].ravel()
+        assert len(np.unique(v)) == len(v)
+    sc = scenes.Scene("b", [scenes.Body(x0=x0, tets=t, colours=col)], 1 / 60, 1, 1, 1)
+    order, off = capi.plan_sweep(sc)
+    assert 32 <= len(off) - 1 <= 34
+    if len(off) - 1 == 34:
+        # the classes are the lattice's own
+        for c in range(34):
+            assert len(np.unique(col[order[off[c]:off[c + 1]]])) == 1
+
+
 def test_plan_sweep_rejects_a_bad_colouring():
     sc = scenes.beam_twist(8, 4, 4, 0.05)
     sc.bodies[0].colours = np.zeros(len(sc.bodies[0].tets), np.uint32)   # one colour: tets share vertices
