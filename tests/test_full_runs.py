@@ -9,9 +9,9 @@ parity is in test_config_parity.py and test_multiframe_parity.py).
   within 1% of rest (nu = 0.48), at rest on the ground at the end (centroid
   at half its height, penetration below 5 cm), inverted tets only where it
   touches the ground (< 0.05%).
-- 512 StVK boxes, 600 frames: finite state.  (The loop itself is unstable at
-  these settings: small stiff boxes invert and are flung out of the arena
-  in the FP64 oracle as on the GPU.)
+- 512 StVK boxes, 600 frames: finite state.  (The loop is unstable at these
+  settings: small stiff boxes invert and are flung out of the arena; the FP64
+  oracle shows the same jitter on a 16-box version.)
 """
 import numpy as np
 import pytest
