@@ -1,12 +1,14 @@
 // Per-vertex warm-start MLP: 16 -> 128 -> 128 -> 128 -> 3, SiLU after the
-// three hidden layers.  BF16 tensor-core GEMMs (mma.sync m16n8k16, FP32
-// accumulate), FP32 master weights, Adam.  Forward, backward and the
-// optimiser are written here; nothing calls a library GEMM.
+// three hidden layers.  The per-layer forward and backward passes, the
+// loss, Adam on FP32 master weights, and the warp-level mma.sync GEMM
+// engine (the tcgen05 engine, the default, is mlp_gemm_tc.cu); nothing
+// calls a library GEMM.
 //
-// Layout: activations row-major [n][features]; weights [out][in] row-major
-// (FP32 master + BF16 copy); inputs are normalised inside the network
-// ((x - mean) / std) and outputs scaled by out_scale, so callers pass raw
-// features and receive raw displacements.
+// Layout: activations row-major [n][features], plus transposed BF16 copies
+// [features][n] for the weight-gradient products; weights [out][in]
+// row-major (FP32 master + BF16 copy + transposed BF16 copy); inputs are
+// normalised inside the network ((x - mean) / std) and outputs scaled by
+// out_scale, so callers pass raw features and receive raw displacements.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
