@@ -160,7 +160,7 @@ cudaError_t gemm_mma_sync(const GemmArgs& g, cudaStream_t st) {
 // the handle's engine; the tcgen05 kernel reports a timed-out wait in tc_err
 static cudaError_t gemm(const MlpDev& d, GemmArgs g, cudaStream_t st) {
     g.err = d.tc_err;
-    g.err_code = 3;
+    g.err_code = (int)SBS_ETIMEOUT;
     return d.engine == kGemmMmaSync ? gemm_mma_sync(g, st) : gemm_tc(g, st);
 }
 

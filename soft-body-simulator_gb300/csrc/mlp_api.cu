@@ -236,7 +236,7 @@ sbs_status sbs_mlp_forward_path(sbs_mlp* m, const float* x, uint32_t n, float* y
     cudaError_t e = cudaMalloc((void**)&dy, (size_t)n * kOut * sizeof(float));
     if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice, m->st);
     if (e == cudaSuccess)
-        e = path == 0 ? mlp_infer_tc(m->d, dx, (int)n, dy, m->d.tc_err, 3, m->d.n_sm, m->st)
+        e = path == 0 ? mlp_infer_tc(m->d, dx, (int)n, dy, m->d.tc_err, (int)SBS_ETIMEOUT, m->d.n_sm, m->st)
                       : mlp_forward_dev(m->d, dx, (int)n, dy, m->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, (size_t)n * kOut * sizeof(float), cudaMemcpyDeviceToHost, m->st);
     int flag = 0;
@@ -261,7 +261,7 @@ sbs_status sbs_mlp_forward_device(sbs_mlp* m, const float* x, uint32_t n, float*
         MCU(m, cudaEventCreate(&e1));
         MCU(m, cudaEventRecord(e0, m->st));
     }
-    cudaError_t e = path == 0 ? mlp_infer_tc(m->d, x, (int)n, y, m->d.tc_err, 3, m->d.n_sm, m->st)
+    cudaError_t e = path == 0 ? mlp_infer_tc(m->d, x, (int)n, y, m->d.tc_err, (int)SBS_ETIMEOUT, m->d.n_sm, m->st)
                               : mlp_forward_dev(m->d, x, (int)n, y, m->st);
     if (e == cudaSuccess && ms) e = cudaEventRecord(e1, m->st);
     int flag = 0;
