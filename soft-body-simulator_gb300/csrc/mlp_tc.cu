@@ -189,7 +189,9 @@ __global__ void __launch_bounds__(kGroupThreads * kGroups, 1) k_mlp_infer_tc(TcA
     uint32_t parity = 0;
     const int tiles = (a.n + kTileRows - 1) / kTileRows;
 
-    for (int tile = blockIdx.x * kGroups + (int)g; tile < tiles; tile += gridDim.x * kGroups) {
+    // slot g of CTA b takes tiles b + g * grid, then every grid * kGroups-th:
+    // with fewer tiles than slots the tiles spread over the SMs, one slot each
+    for (int tile = blockIdx.x + (int)g * gridDim.x; tile < tiles; tile += gridDim.x * kGroups) {
         const int row = tile * kTileRows + (int)r;
         const bool valid = row < a.n;
         // layer-1 A operand: normalised features (this thread's 16 / kSplit of the row)
@@ -293,9 +295,10 @@ cudaError_t mlp_infer_tc(const MlpDev& d, const float* x, int n, float* y, int* 
     a.err = err;
     a.err_code = err_code;
     const int tiles = (n + kTileRows - 1) / kTileRows;
-    const int per_cta = kGroups;
-    const int want = (tiles + per_cta - 1) / per_cta;
-    const int grid = want < n_sm ? want : n_sm;   // one CTA (4 tile slots of 256 threads, 216 KB) per SM
+    // one CTA (4 tile slots of 256 threads, 216 KB) per SM; a small call
+    // (fewer tiles than SMs) takes one CTA per tile rather than packing its
+    // tiles into the slots of a few SMs
+    const int grid = tiles < n_sm ? tiles : n_sm;
     k_mlp_infer_tc<<<grid, kGroupThreads * kGroups, kSmemBytes, st>>>(a);
     count_launch();
     return cudaGetLastError();

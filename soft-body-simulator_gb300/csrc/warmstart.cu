@@ -45,10 +45,35 @@ __global__ void k_tet_f(SceneDev s, WarmDev w) {
     }
 }
 
+// Eight lanes per vertex: each adds the gradients of every eighth incident
+// tet in incidence order, the eight partial sums are added by a fixed
+// shuffle tree, and the group's first lane writes the vertex's features (the
+// loads of a vertex's ~24 incident tets are in flight together).
+constexpr uint32_t kFeatLanes = 8;
+
 __global__ void k_features(SceneDev s, WarmDev w, StepParams p, int dprev_valid) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < s.n_verts; v += gridDim.x * blockDim.x) {
+    const uint32_t sub = threadIdx.x & (kFeatLanes - 1);
+    const uint32_t stride = gridDim.x * blockDim.x / kFeatLanes;
+    // uniform trip count across the warp: every lane takes part in the shuffles
+    const uint32_t n_pad = (s.n_verts + stride - 1) / stride * stride;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) / kFeatLanes; v < n_pad; v += stride) {
+        const bool live = v < s.n_verts;
+        float F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const uint32_t b = live ? w.inc_start[v] : 0u, e = live ? w.inc_start[v + 1] : 0u;
+        for (uint32_t k = b + sub; k < e; k += kFeatLanes) {
+            const uint32_t t = w.inc[k];
+            const float4 r0 = w.tet_f[3ull * t], r1 = w.tet_f[3ull * t + 1], r2 = w.tet_f[3ull * t + 2];
+            F[0] += r0.x; F[1] += r0.y; F[2] += r0.z;
+            F[3] += r1.x; F[4] += r1.y; F[5] += r1.z;
+            F[6] += r2.x; F[7] += r2.y; F[8] += r2.z;
+        }
+#pragma unroll
+        for (uint32_t o = kFeatLanes / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int i = 0; i < 9; ++i) F[i] += __shfl_xor_sync(0xffffffffu, F[i], o);
+        if (!live || sub != 0) continue;
         const float4 xp = s.xi[v], x = s.xn[v];
-        float* f = w.feat + (size_t)v * 16;
+        float f[16];
         f[0] = xp.x - x.x;
         f[1] = xp.y - x.y;
         f[2] = xp.z - x.z;
@@ -60,16 +85,7 @@ __global__ void k_features(SceneDev s, WarmDev w, StepParams p, int dprev_valid)
         } else {
             f[3] = f[4] = f[5] = 0.0f;
         }
-        // mean of the incident tets' gradients (k_tet_f), in incidence order
-        float F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        const uint32_t b = w.inc_start[v], e = w.inc_start[v + 1];
-        for (uint32_t k = b; k < e; ++k) {
-            const uint32_t t = w.inc[k];
-            const float4 r0 = w.tet_f[3ull * t], r1 = w.tet_f[3ull * t + 1], r2 = w.tet_f[3ull * t + 2];
-            F[0] += r0.x; F[1] += r0.y; F[2] += r0.z;
-            F[3] += r1.x; F[4] += r1.y; F[5] += r1.z;
-            F[6] += r2.x; F[7] += r2.y; F[8] += r2.z;
-        }
+        // mean of the incident tets' gradients (k_tet_f)
         const float inv = e > b ? 1.0f / (float)(e - b) : 0.0f;
         for (int i = 0; i < 9; ++i) F[i] *= inv;
         // E = (F^T F - I) / 2 of the mean gradient (F row-major)
@@ -94,6 +110,10 @@ __global__ void k_features(SceneDev s, WarmDev w, StepParams p, int dprev_valid)
         f[13] = ay;
         f[14] = az;
         f[15] = pinned ? 1.0f : 0.0f;
+        // the row's 64 bytes as four 16-byte stores
+        float4* out = reinterpret_cast<float4*>(w.feat + (size_t)v * 16);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
         w.xpred[v] = xp;
     }
 }
@@ -261,7 +281,7 @@ cudaError_t launch_features(const SceneDev& s, const WarmDev& w, const StepParam
     const int tgrid = (int)std::min<uint32_t>(4096, (s.n_tets + 255) / 256);
     k_tet_f<<<tgrid > 0 ? tgrid : 1, 256, 0, st>>>(s, w);
     count_launch();
-    const int grid = (int)std::min<uint32_t>(4096, (s.n_verts + 255) / 256);
+    const int grid = (int)std::min<uint64_t>(4096, ((uint64_t)s.n_verts * kFeatLanes + 255) / 256);
     k_features<<<grid > 0 ? grid : 1, 256, 0, st>>>(s, w, p, dprev_valid);
     count_launch();
     return cudaGetLastError();

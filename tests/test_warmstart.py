@@ -36,6 +36,38 @@ def test_previous_displacement_feature(capi_mod):
     g.close()
 
 
+def test_strain_features_match_numpy(capi_mod):
+    """Features 6..11: the Green strain (F^T F - I) / 2 of the mean
+    deformation gradient of a vertex's incident tets at the predicted
+    positions, against numpy in FP64 (the GPU adds the incident gradients in
+    eight interleaved partial sums and a fixed tree)."""
+    from sbs_gb300 import scenes
+    sc = scenes.beam_twist(10, 4, 4, 0.05)
+    g = capi_mod.Solver(sc, exec_mode=1)
+    g.step(3)
+    g.detect_contacts()
+    g.predict(sc.frame_dt / sc.substeps)
+    f = g.features().astype(np.float64)
+    xp = g.predicted_all().astype(np.float64)
+    b = sc.bodies[0]
+    t = b.tets.astype(np.int64)
+    x0 = b.x0
+    Dm = np.stack([x0[t[:, 0]] - x0[t[:, 3]], x0[t[:, 1]] - x0[t[:, 3]], x0[t[:, 2]] - x0[t[:, 3]]], axis=2)
+    Ds = np.stack([xp[t[:, 0]] - xp[t[:, 3]], xp[t[:, 1]] - xp[t[:, 3]], xp[t[:, 2]] - xp[t[:, 3]]], axis=2)
+    F = Ds @ np.linalg.inv(Dm)
+    Fsum = np.zeros((len(x0), 3, 3))
+    cnt = np.zeros(len(x0))
+    for k in range(4):
+        np.add.at(Fsum, t[:, k], F)
+        np.add.at(cnt, t[:, k], 1)
+    Fm = Fsum / cnt[:, None, None]
+    E = 0.5 * (np.einsum("vki,vkj->vij", Fm, Fm) - np.eye(3))
+    want = np.stack([E[:, 0, 0], E[:, 1, 1], E[:, 2, 2], E[:, 0, 1], E[:, 0, 2], E[:, 1, 2]], axis=1)
+    assert np.abs(f[:, 6:12] - want).max() < 2e-5
+    assert np.abs(want).max() > 1e-4
+    g.close()
+
+
 def test_fit_sweeps_argument(capi_mod):
     sc = warmstart.batch_scene([7])
     g = capi_mod.Solver(sc, exec_mode=1)
