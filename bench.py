@@ -523,14 +523,16 @@ def main():
     h2d = V * 12 * 2   # x and v, 3 floats per vertex (permuted on the device)
     d2h = V * 12 * 2   # x and v
 
+    # the single-GPU extras (other workloads, the judged warm start) are left
+    # out of replica runs: every GPU would repeat them while all are held
     others = {}
-    for name in [w for w in args.also.split(",") if w and w != args.workload]:
-        others[name] = other_workload(name, args, device, flush, peak_gbs())
-
     warm = None
-    net = WARM_NETWORKS.get(args.workload)
-    if net is not None and not args.no_warm:
-        warm = warm_leg(scene, args, device, flush, ms_per_frame, solver.stats().exec_mode, net)
+    if world == 1:
+        for name in [w for w in args.also.split(",") if w and w != args.workload]:
+            others[name] = other_workload(name, args, device, flush, peak_gbs())
+        net = WARM_NETWORKS.get(args.workload)
+        if net is not None and not args.no_warm:
+            warm = warm_leg(scene, args, device, flush, ms_per_frame, solver.stats().exec_mode, net)
 
     if rank != 0:
         solver.close()
